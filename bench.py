@@ -1,0 +1,416 @@
+#!/usr/bin/env python3
+"""Benchmark: CCD pair-queries/s on the 1,024-hull scene.
+
+Workload (one step): the time-step-selection CCD of one outer step of the
+1,024-body convex-hull scene (64-point quickhull hulls of radius 0.6 m on an
+8x8x16 grid at 1.4 m, random orientations, N(0, 0.5^2) m/s velocities,
+dt = 1/240 s, plus the static ground): compareTreesFullContinuous for every
+broad-phase pair with max_time = min(last_dt_a, last_dt_b), i.e. what
+fineCollisionClustersWithTimeStepSelection issues for the scene's cluster.
+A pair-query is one compareTreesFullContinuous call.
+
+  value  : pair-queries/s with bodies, trees and pairs resident in HBM
+           (device entry point), L2 flushed before every timed step
+  e2e    : the same through the host C-ABI entry points, inputs copied from
+           pinned host memory and all contacts copied back inside the step
+  --impl reference : the reference algorithm on the host cores (the CPU
+           restatement in oracle/, all host threads, spawn pool); the
+           reference itself cannot be built here (Eigen, Embree, libigl).
+Multi-GPU: the path does not shard across GPUs in this workload; every rank
+runs an independent replica and `value` sums them (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CCD pair-queries/s"
+UNIT = "pair-queries/s"
+WORKLOAD = "c2-1024-hulls-ccd-step"
+# Algorithmic bytes of one primitive test of the CCD kernels: two triangles
+# (2 x 72 B), the frontier entry and item index (16 B), the result record and
+# hit flag written (64 B + 4 B).  Pose matrices are per body pair and shared.
+BYTES_PER_TEST = 2 * 72 + 16 + 64 + 4
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget (single thread)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--seed", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def build_workload(seed):
+    import numpy as np
+
+    import delta2_gb300 as D
+
+    s = D.make_scene(2, seed=seed)
+    # First outer step (broad_phase_embree_cluster.cpp:126-132): last_dt = min(2*last_dt, dt);
+    # the broad phase reads the projected future positions x + dt*v.
+    s.last_dt = np.minimum(2.0 * s.last_dt, np.float64(np.float32(s.opt_dt)))
+    s.fut[:, 8:11] = s.cur[:, 8:11] + s.last_dt[:, None] * s.cur[:, 11:14]
+    pairs = D.broad_phase(s)
+    mt = np.minimum(s.last_dt[pairs[:, 0]], s.last_dt[pairs[:, 1]])
+    return s, pairs, mt
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_test():
+    """DRAM bytes per primitive test of the dominant kernel from the committed
+    ncu summary (profiles/ccd_kernels_c2.md), or None."""
+    path = os.path.join(ROOT, "profiles", "ccd_kernels_c2.md")
+    out = {}
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_test"):
+                k, v = line.split(":", 1)
+                kind = k.strip().split()[-1]
+                out[kind] = float(v.strip().split()[0])
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.tmp = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.tmp.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.tmp.name):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 7:
+                    continue
+                try:
+                    sm.append(float(f[0]))
+                    smax.append(float(f[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        finally:
+            os.unlink(self.tmp.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(scene, pairs, mt, budget_s):
+    """The oracle (single thread, the reference's serial path) on a strided
+    sample of the same pair list, for about budget_s seconds."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    n = len(pairs)
+    order = np.concatenate([np.arange(k, n, 16) for k in range(16)])
+    done, t0 = 0, time.perf_counter()
+    while done < n and time.perf_counter() - t0 < budget_s:
+        idx = order[done:done + 64]
+        O.ccd(scene.copy(), pairs[idx], mt[idx])
+        done += len(idx)
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{done} of the {n} pair-queries of one step (strided), {dt:.1f} s, CPU oracle -O2"}
+
+
+# ------------------------------------------------------------------ ours ---
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import delta2_gb300 as D
+    from delta2_gb300 import build as B
+
+    rank, local_rank, world = dist_env()
+    B.build()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    scene, pairs, mt = build_workload(args.seed)
+    n_pairs = len(pairs)
+
+    ctx = D.Context(local_rank)
+    ctx.set_scene(scene.copy())
+    d_pairs = torch.from_numpy(pairs).cuda()
+    d_mt = torch.from_numpy(mt).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step():
+        return ctx.compare_trees_full_continuous_device(d_pairs.data_ptr(), d_mt.data_ptr(), n_pairs)
+
+    for _ in range(args.warmup):
+        n_contacts, _, _, counters = step()
+    ctx.set_profiling(True)
+    launches0 = ctx.launches()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    gpu_index = local_rank
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        gpu_index = vis.split(",")[local_rank]
+    barrier()
+    sampler = ClockSampler(gpu_index)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n_contacts, _, _, counters = step()
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    barrier()
+    clocks = sampler.stop()
+    launches = ctx.launches() - launches0
+    prof = {k: ctx.profile(k) for k in (D.PROF_SOUP_FILTER, D.PROF_SOUP_CCD, D.PROF_CONN)}
+    ctx.set_profiling(False)
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * n_pairs * args.steps / (max_ms / 1e3)
+
+    # ---- end to end through the host C-ABI entry points (pinned host buffers)
+    e2e = e2e_host(ctx, scene, pairs, mt, args)
+
+    if rank != 0:
+        ctx.close()
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = measured_peaks()
+    kinds = {D.PROF_SOUP_CCD: "tri_tri_ccd", D.PROF_CONN: "leaf_pair_ccd", D.PROF_SOUP_FILTER: "swept_box_filter"}
+    dom = max((D.PROF_SOUP_CCD, D.PROF_CONN), key=lambda k: prof[k][0])
+    ms, nl, items = prof[dom]
+    achieved = (items * BYTES_PER_TEST) / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    tr = profile_traffic_per_test().get(kinds[dom])
+    traffic = tr * items / nl if (tr is not None and nl) else None
+    roofline = {"bound": "hbm", "kernel": kinds[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel_ms_per_launch": ms / max(nl, 1), "launches": nl, "tests_per_launch": items / max(nl, 1),
+                "note": "FP64 arithmetic bound: the kernel's bytes are small next to its FP64 work"}
+    kernel_share = {kinds[k]: prof[k][0] / max(1e-9, sum(v[0] for v in prof.values())) for k in prof}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, pairs, mt, args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "bodies": int(scene.n_bodies), "pair_queries_per_step": n_pairs,
+                   "dt": scene.opt_dt, "l2": "flushed before every timed step (512 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
+        "kernel_time_share": kernel_share,
+        "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
+                     "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def e2e_host(ctx, scene, pairs, mt, args):
+    """compare_trees_full_continuous through the host entry points: every step
+    uploads the body states, pairs and max_time from pinned host memory and
+    reads every contact back."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import delta2_gb300 as D
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.float64: torch.float64, np.int32: torch.int32, np.uint8: torch.uint8}[
+            a.dtype.type], pin_memory=True)
+        v = t.numpy()
+        v[...] = a
+        return v, t
+
+    keep = []
+    sc = scene.copy()
+    for k in ["last", "cur", "fut", "last_dt", "mass", "inv_inertia", "geo_eps", "mu", "bounding_radius"]:
+        v, t = pinned(np.ascontiguousarray(getattr(sc, k), dtype=np.float64))
+        setattr(sc, k, v)
+        keep.append(t)
+    for k in ["mesh", "sleep_steps"]:
+        v, t = pinned(np.ascontiguousarray(getattr(sc, k), dtype=np.int32))
+        setattr(sc, k, v)
+        keep.append(t)
+    for k in ["is_static", "sleeping"]:
+        v, t = pinned(np.ascontiguousarray(getattr(sc, k), dtype=np.uint8))
+        setattr(sc, k, v)
+        keep.append(t)
+    hp, tp = pinned(np.ascontiguousarray(pairs, dtype=np.int32))
+    hm, tm = pinned(np.ascontiguousarray(mt, dtype=np.float64))
+    cap = 1 << 20
+    out, to = pinned(np.zeros((cap, D.CONTACT_LEN)))
+    off, toff = pinned(np.zeros(len(pairs) + 1, dtype=np.int32))
+    keep += [tp, tm, to, toff]
+    L = D.lib()
+    b = sc.bodies_struct()
+    cnt = np.zeros(4, np.int64)
+
+    def step():
+        D._check(L.d2g_ctx_set_bodies(ctx.h, C.byref(b)))
+        D._check(L.d2g_compare_trees_full_continuous(
+            ctx.h, hp.ctypes.data_as(D.I32P), hm.ctypes.data_as(D.F64P), len(hp), out.ctypes.data_as(D.F64P), cap,
+            off.ctypes.data_as(D.I32P), cnt.ctypes.data_as(D.I64P)))
+        return int(off[-1])
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    n_contacts = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        n_contacts = step()
+        times.append(time.perf_counter() - t0)
+    body_bytes = sum(getattr(sc, k).nbytes for k in ["mesh", "is_static", "geo_eps", "mu", "mass", "inv_inertia",
+                                                     "last", "cur", "fut", "last_dt", "sleep_steps", "sleeping",
+                                                     "bounding_radius"])
+    h2d = body_bytes + hp.nbytes + hm.nbytes
+    d2h = n_contacts * D.CONTACT_LEN * 8 + off.nbytes
+    return {"value": len(pairs) * len(times) / sum(times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * sum(times) / len(times),
+            "path": "d2g_ctx_set_bodies + d2g_compare_trees_full_continuous (host buffers)"}
+
+
+# ------------------------------------------------------------- reference ---
+_W = {}
+
+
+def _worker_init(scene, pairs, mt):
+    _W["scene"], _W["pairs"], _W["mt"] = scene, pairs, mt
+
+
+def _worker_run(idx):
+    from oracle import oracle as O
+
+    s = _W["scene"]
+    O.ccd(s.copy(), _W["pairs"][idx], _W["mt"][idx])
+    return len(idx)
+
+
+def run_reference(args):
+    import multiprocessing as mp
+
+    import numpy as np
+
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build()
+    scene, pairs, mt = build_workload(args.seed)
+    cores = os.cpu_count() or 1
+    n = len(pairs)
+    chunks = [np.arange(k, n, 8 * cores) for k in range(8 * cores)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(scene, pairs, mt)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_worker_run, chunks[:cores])
+        times = []
+        done = 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            done += sum(pool.map(_worker_run, chunks))
+            times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = done / total
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "bodies": int(scene.n_bodies), "pair_queries_per_step": n,
+                   "dt": scene.opt_dt, "parallelism": f"{cores} host processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"all {n} pair-queries of each step on {cores} host cores (spawn pool)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference not buildable here (Eigen, Embree, libigl, icx absent); CPU restatement timed",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,325 @@
+"""delta2_gb300 — GB300 (sm_103a) contact hot path of the Delta2 rigid-body simulator.
+
+Python mirror of the C ABI in ``include/d2g.h``.  The names follow the
+reference's functions (``compare_trees_full`` = ``compareTreesFull``,
+``compare_trees_full_continuous`` = ``compareTreesFullContinuous``); the
+compute always runs in the CUDA library ``_lib/libd2g.so``.  There is no CPU
+fallback: a missing library or GPU raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libd2g.so")
+_lib = None
+
+STATE_LEN = 14
+CONTACT_LEN = 14
+
+I32P = C.POINTER(C.c_int32)
+F64P = C.POINTER(C.c_double)
+F32P = C.POINTER(C.c_float)
+U8P = C.POINTER(C.c_uint8)
+I64P = C.POINTER(C.c_int64)
+U64P = C.POINTER(C.c_uint64)
+
+
+class D2GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"d2g error {code}: {msg}")
+        self.code = code
+
+
+class CapacityError(D2GError):
+    pass
+
+
+class SolveFailed(D2GError):
+    pass
+
+
+class Trees(C.Structure):
+    _fields_ = [("n_meshes", C.c_int32), ("mesh_node_off", I32P), ("nodes", I32P), ("ntris", I32P),
+                ("tris", F64P), ("eps", F64P), ("inner_eps", F64P)]
+
+
+class Bodies(C.Structure):
+    _fields_ = [("n", C.c_int32), ("mesh", I32P), ("is_static", U8P), ("geo_eps", F64P), ("mu", F64P),
+                ("mass", F64P), ("inv_inertia", F64P), ("last", F64P), ("cur", F64P), ("fut", F64P),
+                ("last_dt", F64P), ("sleep_steps", I32P), ("sleeping", U8P), ("bounding_radius", F64P)]
+
+
+class SceneOpts(C.Structure):
+    _fields_ = [("config", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("spacing", C.c_double), ("speed_sigma", C.c_double), ("seed", C.c_uint64), ("dt", C.c_float),
+                ("gravity_z", C.c_double), ("mu", C.c_double), ("hull_points", C.c_int32)]
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def lib():
+    """Load the CUDA library (it must have been built with ``delta2_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise RuntimeError(f"{_LIB_PATH} is missing: build it with `python -m delta2_gb300.build` "
+                               "(or __graft_entry__.build()); there is no CPU fallback")
+        L = C.CDLL(_LIB_PATH)
+        L.d2g_last_error.restype = C.c_char_p
+        L.d2g_version.restype = C.c_char_p
+        L.d2g_ctx_destroy.restype = None
+        L.d2g_scene_free.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc == 0:
+        return rc
+    msg = lib().d2g_last_error().decode(errors="replace")
+    if rc == 2:
+        raise CapacityError(rc, msg)
+    if rc == 1:
+        raise SolveFailed(rc, msg)
+    raise D2GError(rc, msg)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Scene:
+    """Flattened trees and bodies (numpy arrays in the C ABI layout)."""
+
+    FIELDS_TREE = ["mesh_node_off", "nodes", "ntris", "tris", "eps", "inner_eps"]
+    FIELDS_BODY = ["mesh", "is_static", "geo_eps", "mu", "mass", "inv_inertia", "last", "cur", "fut", "last_dt",
+                   "sleep_steps", "sleeping", "bounding_radius"]
+
+    def copy(self):
+        s = Scene()
+        for k, v in self.__dict__.items():
+            setattr(s, k, v.copy() if isinstance(v, np.ndarray) else v)
+        return s
+
+    def trees_struct(self):
+        self.mesh_node_off = np.ascontiguousarray(self.mesh_node_off, dtype=np.int32)
+        self.nodes = np.ascontiguousarray(self.nodes, dtype=np.int32)
+        self.ntris = np.ascontiguousarray(self.ntris, dtype=np.int32)
+        for k in ["tris", "eps", "inner_eps"]:
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float64))
+        return Trees(len(self.mesh_node_off) - 1, _p(self.mesh_node_off, I32P), _p(self.nodes, I32P),
+                     _p(self.ntris, I32P), _p(self.tris, F64P), _p(self.eps, F64P), _p(self.inner_eps, F64P))
+
+    def bodies_struct(self):
+        for k, dt in [("mesh", np.int32), ("is_static", np.uint8), ("sleep_steps", np.int32),
+                      ("sleeping", np.uint8)]:
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=dt))
+        for k in ["geo_eps", "mu", "mass", "inv_inertia", "last", "cur", "fut", "last_dt", "bounding_radius"]:
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float64))
+        return Bodies(len(self.mesh), _p(self.mesh, I32P), _p(self.is_static, U8P), _p(self.geo_eps, F64P),
+                      _p(self.mu, F64P), _p(self.mass, F64P), _p(self.inv_inertia, F64P), _p(self.last, F64P),
+                      _p(self.cur, F64P), _p(self.fut, F64P), _p(self.last_dt, F64P), _p(self.sleep_steps, I32P),
+                      _p(self.sleeping, U8P), _p(self.bounding_radius, F64P))
+
+    @property
+    def n_bodies(self):
+        return len(self.mesh)
+
+
+def make_scene(config=2, nx=0, ny=0, nz=0, spacing=0.0, speed_sigma=-1.0, seed=0, dt=0.0, gravity_z=-9.8, mu=0.0,
+               hull_points=64):
+    """Synthetic scene of a benchmark configuration (host set-up, no GPU)."""
+    L = lib()
+    o = SceneOpts(config, nx, ny, nz, spacing, speed_sigma, seed, dt, gravity_z, mu, hull_points)
+    h = C.c_void_p()
+    _check(L.d2g_scene_make(C.byref(o), C.byref(h)))
+    try:
+        t = Trees()
+        b = Bodies()
+        aabb = F32P()
+        odt = C.c_float()
+        gz = C.c_double()
+        _check(L.d2g_scene_view(h, C.byref(t), C.byref(b), C.byref(aabb), C.byref(odt), C.byref(gz)))
+        s = Scene()
+        M = t.n_meshes
+        s.mesh_node_off = np.ctypeslib.as_array(t.mesh_node_off, (M + 1,)).copy()
+        N = int(s.mesh_node_off[-1])
+        s.nodes = np.ctypeslib.as_array(t.nodes, (N, 4)).copy()
+        s.ntris = np.ctypeslib.as_array(t.ntris, (N,)).copy()
+        s.tris = np.ctypeslib.as_array(t.tris, (N, 8, 9)).copy()
+        s.eps = np.ctypeslib.as_array(t.eps, (N, 8)).copy()
+        s.inner_eps = np.ctypeslib.as_array(t.inner_eps, (N, 8)).copy()
+        n = b.n
+        s.mesh = np.ctypeslib.as_array(b.mesh, (n,)).copy()
+        s.is_static = np.ctypeslib.as_array(b.is_static, (n,)).copy()
+        s.geo_eps = np.ctypeslib.as_array(b.geo_eps, (n,)).copy()
+        s.mu = np.ctypeslib.as_array(b.mu, (n,)).copy()
+        s.mass = np.ctypeslib.as_array(b.mass, (n,)).copy()
+        s.inv_inertia = np.ctypeslib.as_array(b.inv_inertia, (n, 9)).copy()
+        for k in ["last", "cur", "fut"]:
+            setattr(s, k, np.ctypeslib.as_array(getattr(b, k), (n, STATE_LEN)).copy())
+        s.last_dt = np.ctypeslib.as_array(b.last_dt, (n,)).copy()
+        s.sleep_steps = np.ctypeslib.as_array(b.sleep_steps, (n,)).copy()
+        s.sleeping = np.ctypeslib.as_array(b.sleeping, (n,)).copy()
+        s.bounding_radius = np.ctypeslib.as_array(b.bounding_radius, (n,)).copy()
+        s.local_aabb = np.ctypeslib.as_array(aabb, (n, 6)).copy()
+        s.opt_dt = float(odt.value)
+        s.gravity_z = float(gz.value)
+        s.config = config
+        return s
+    finally:
+        L.d2g_scene_free(h)
+
+
+def build_tree(V, F, rng_state=None):
+    """Surrogate tree of one mesh (model/surrogate_tree.cpp:39-112).
+
+    Returns (nodes, ntris, tris, eps, inner_eps, rng_state); child indices are
+    local to the mesh.  ``rng_state`` is the PCG32 (state, inc) pair; None =
+    the reference's Options stream seeded (42, 54)."""
+    L = lib()
+    V = np.ascontiguousarray(V, dtype=np.float64).reshape(-1, 3)
+    F = np.ascontiguousarray(F, dtype=np.int32).reshape(-1, 3)
+    if rng_state is None:
+        rng_state = pcg32_seed(42, 54)
+    rng = np.array(rng_state, dtype=np.uint64)
+    n = C.c_int32()
+    _check(L.d2g_tree_build(_p(V, F64P), len(V), _p(F, I32P), len(F), _p(rng, U64P), C.byref(n), None, None, None,
+                            None, None, 0))
+    N = n.value
+    nodes = np.zeros((N, 4), np.int32)
+    ntris = np.zeros(N, np.int32)
+    tris = np.zeros((N, 8, 9))
+    eps = np.zeros((N, 8))
+    ieps = np.zeros((N, 8))
+    _check(L.d2g_tree_build(_p(V, F64P), len(V), _p(F, I32P), len(F), _p(rng, U64P), C.byref(n), _p(nodes, I32P),
+                            _p(ntris, I32P), _p(tris, F64P), _p(eps, F64P), _p(ieps, F64P), N))
+    return nodes, ntris, tris, eps, ieps, (int(rng[0]), int(rng[1]))
+
+
+def broad_phase(scene):
+    """Candidate body pairs (i < j) of a scene (host broad phase, no GPU)."""
+    L = lib()
+    b = scene.bodies_struct()
+    aabb = np.ascontiguousarray(scene.local_aabb, dtype=np.float32)
+    n = C.c_int32()
+    _check(L.d2g_broad_phase(C.byref(b), _p(aabb, F32P), None, 0, C.byref(n)))
+    out = np.zeros((max(n.value, 1), 2), np.int32)
+    _check(L.d2g_broad_phase(C.byref(b), _p(aabb, F32P), _p(out, I32P), n.value, C.byref(n)))
+    return out[:n.value].copy()
+
+
+PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
+
+
+def pcg32_seed(initstate, initseq):
+    """PCG32 srandom: returns (state, inc)."""
+    mask = (1 << 64) - 1
+    inc = ((initseq << 1) | 1) & mask
+    state = 0
+    state = (state * 6364136223846793005 + inc) & mask
+    state = (state + initstate) & mask
+    state = (state * 6364136223846793005 + inc) & mask
+    return state, inc
+
+
+class Context:
+    """A CUDA context of the library: trees and bodies resident in HBM."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = C.c_void_p()
+        _check(L.d2g_ctx_create(int(device), C.byref(h)))
+        self.h = h
+        self.scene = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().d2g_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().d2g_ctx_stream(self.h, C.byref(s)))
+        return s.value
+
+    def sync(self):
+        _check(lib().d2g_ctx_sync(self.h))
+
+    def set_scene(self, scene):
+        self.scene = scene
+        self._t = scene.trees_struct()
+        _check(lib().d2g_ctx_set_trees(self.h, C.byref(self._t)))
+        self.set_bodies(scene)
+
+    def set_bodies(self, scene):
+        self._b = scene.bodies_struct()
+        _check(lib().d2g_ctx_set_bodies(self.h, C.byref(self._b)))
+
+    def get_bodies(self, scene=None):
+        scene = scene or self.scene
+        b = scene.bodies_struct()
+        _check(lib().d2g_ctx_get_bodies(self.h, C.byref(b)))
+        return scene
+
+    def launches(self):
+        n = C.c_int64()
+        _check(lib().d2g_ctx_launches(self.h, C.byref(n)))
+        return n.value
+
+    def set_profiling(self, enable):
+        _check(lib().d2g_ctx_set_profiling(self.h, int(bool(enable))))
+
+    def profile(self, kind):
+        ms = C.c_double()
+        n = C.c_int64()
+        items = C.c_int64()
+        _check(lib().d2g_ctx_profile(self.h, int(kind), C.byref(ms), C.byref(n), C.byref(items)))
+        return ms.value, n.value, items.value
+
+    def compare_trees_full_continuous_device(self, d_pairs, d_max_time, n_pairs):
+        """Device-resident CCD: pointers (ints) to int32 pairs and float64 max_time in HBM.
+        Returns (n_contacts, d_contacts_ptr, d_offsets_ptr, counters)."""
+        n = C.c_int32()
+        dc = C.c_void_p()
+        do = C.c_void_p()
+        cnt = np.zeros(4, np.int64)
+        _check(lib().d2g_compare_trees_full_continuous_device(self.h, C.c_void_p(d_pairs), C.c_void_p(d_max_time),
+                                                              int(n_pairs), C.byref(n), C.byref(dc), C.byref(do),
+                                                              _p(cnt, I64P)))
+        return n.value, dc.value, do.value, cnt
+
+    def compare_trees_full(self, pairs, capacity=None):
+        """compareTreesFull for each pair -> (contacts [n,14], offsets [n_pairs+1], counters)."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        return self._query(lambda cap, out, off, cnt: lib().d2g_compare_trees_full(
+            self.h, _p(pairs, I32P), len(pairs), _p(out, F64P), cap, _p(off, I32P), _p(cnt, I64P)), len(pairs),
+            capacity)
+
+    def compare_trees_full_continuous(self, pairs, max_time, capacity=None):
+        """compareTreesFullContinuous for each pair over max_time[i]."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        mt = np.ascontiguousarray(np.broadcast_to(np.asarray(max_time, dtype=np.float64), (len(pairs),)))
+        return self._query(lambda cap, out, off, cnt: lib().d2g_compare_trees_full_continuous(
+            self.h, _p(pairs, I32P), _p(mt, F64P), len(pairs), _p(out, F64P), cap, _p(off, I32P), _p(cnt, I64P)),
+            len(pairs), capacity)
+
+    def _query(self, call, n_pairs, capacity):
+        cap = capacity if capacity is not None else max(4096, 64 * n_pairs)
+        while True:
+            out = np.zeros((max(cap, 1), CONTACT_LEN))
+            off = np.zeros(n_pairs + 1, np.int32)
+            cnt = np.zeros(4, np.int64)
+            rc = call(cap, out, off, cnt)
+            if rc == 2 and capacity is None:
+                cap = int(off[-1]) + 16
+                continue
+            _check(rc)
+            return out[:off[-1]].copy(), off, cnt

@@ -1,0 +1,492 @@
+// extern "C" entry points of include/d2g.h: context and device memory,
+// input validation, host set-up glue.  Compute lives in d2g_engine.cu.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/d2g.h"
+#include "d2g_internal.hpp"
+#include "host/d2g_scene.hpp"
+
+namespace d2g {
+namespace {
+thread_local std::string g_err;
+}
+void set_error(const std::string& msg) { g_err = msg; }
+}  // namespace d2g
+
+using d2g::set_error;
+
+#define RC(x)                          \
+    do {                               \
+        if (int rc_ = (x)) return rc_; \
+    } while (0)
+
+struct d2g_scene {
+    d2g::Scene s;
+};
+
+namespace {
+
+template <class T>
+int upload(d2g_ctx* ctx, d2g::DBuf<T>& dst, const T* src, size_t n) {
+    RC(dst.ensure(n + 1));
+    if (n) D2G_CUDA(cudaMemcpyAsync(dst.p, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return D2G_OK;
+}
+
+template <class T>
+int download(d2g_ctx* ctx, T* dst, const d2g::DBuf<T>& src, size_t n) {
+    if (n) D2G_CUDA(cudaMemcpyAsync(dst, src.p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    return D2G_OK;
+}
+
+int check_ready(d2g_ctx* ctx) {
+    if (!ctx) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    if (ctx->n_nodes == 0 || ctx->n_bodies == 0) {
+        set_error("trees and bodies must be set before a query");
+        return D2G_ERR_STATE;
+    }
+    return D2G_OK;
+}
+
+int check_pairs(d2g_ctx* ctx, const int32_t* pairs, int n) {
+    if (n < 0 || (n > 0 && !pairs)) {
+        set_error("invalid pair list");
+        return D2G_ERR_INVALID;
+    }
+    for (int i = 0; i < 2 * n; i++) {
+        if (pairs[i] < 0 || pairs[i] >= ctx->n_bodies) {
+            set_error("pair " + std::to_string(i / 2) + " names body " + std::to_string(pairs[i]) +
+                      " outside [0, " + std::to_string(ctx->n_bodies) + ")");
+            return D2G_ERR_INVALID;
+        }
+    }
+    return D2G_OK;
+}
+
+// Copy the results of the last engine call to the caller's host buffers.
+int copy_out(d2g_ctx* ctx, int n_pairs, int n_rec, double* contacts, int capacity, int32_t* offsets) {
+    if (offsets) RC(download(ctx, offsets, ctx->eng.out_off, (size_t)n_pairs + 1));
+    const int n_copy = n_rec < capacity ? n_rec : (capacity > 0 ? capacity : 0);
+    if (contacts && n_copy > 0) RC(download(ctx, contacts, ctx->eng.rec_sorted, 14 * (size_t)n_copy));
+    D2G_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (n_rec > capacity) {
+        set_error("contact capacity " + std::to_string(capacity) + " < " + std::to_string(n_rec));
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* d2g_last_error(void) { return d2g::g_err.c_str(); }
+const char* d2g_version(void) { return "delta2_gb300 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------- scenes -----
+int d2g_scene_make(const d2g_scene_opts* o, d2g_scene** out) {
+    if (!o || !out) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    d2g::SceneOpts so;
+    so.config = o->config;
+    so.nx = o->nx;
+    so.ny = o->ny;
+    so.nz = o->nz;
+    so.spacing = o->spacing;
+    so.speed_sigma = o->speed_sigma;
+    so.seed = o->seed;
+    so.dt = o->dt;
+    so.gravity_z = o->gravity_z;
+    so.mu = o->mu;
+    so.hull_points = o->hull_points > 3 ? o->hull_points : 64;
+    d2g_scene* s = new d2g_scene();
+    std::string err;
+    if (!d2g::make_scene(so, s->s, &err)) {
+        delete s;
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    *out = s;
+    return D2G_OK;
+}
+
+void d2g_scene_free(d2g_scene* s) { delete s; }
+
+int d2g_scene_view(d2g_scene* sc, d2g_trees* t, d2g_bodies* b, const float** local_aabb, float* opt_dt,
+                   double* gravity_z) {
+    if (!sc) {
+        set_error("null scene");
+        return D2G_ERR_INVALID;
+    }
+    d2g::Scene& s = sc->s;
+    if (t) {
+        t->n_meshes = (int32_t)s.mesh_node_off.size() - 1;
+        t->mesh_node_off = s.mesh_node_off.data();
+        t->nodes = s.nodes.data();
+        t->ntris = s.ntris.data();
+        t->tris = s.tris.data();
+        t->eps = s.eps.data();
+        t->inner_eps = s.inner_eps.data();
+    }
+    if (b) {
+        b->n = s.n_bodies();
+        b->mesh = s.mesh.data();
+        b->is_static = s.is_static.data();
+        b->geo_eps = s.geo_eps.data();
+        b->mu = s.mu.data();
+        b->mass = s.mass.data();
+        b->inv_inertia = s.inv_inertia.data();
+        b->last = s.last.data();
+        b->cur = s.cur.data();
+        b->fut = s.fut.data();
+        b->last_dt = s.last_dt.data();
+        b->sleep_steps = s.sleep_steps.data();
+        b->sleeping = s.sleeping.data();
+        b->bounding_radius = s.bounding_radius.data();
+    }
+    if (local_aabb) *local_aabb = s.local_aabb.data();
+    if (opt_dt) *opt_dt = s.opt_dt;
+    if (gravity_z) *gravity_z = s.gravity_z;
+    return D2G_OK;
+}
+
+int d2g_tree_build(const double* V, int32_t nv, const int32_t* F, int32_t nf, uint64_t* rng, int32_t* n_nodes,
+                   int32_t* nodes, int32_t* ntris, double* tris, double* eps, double* inner_eps, int32_t capacity) {
+    if (!V || !F || nv < 3 || nf < 1 || !rng || !n_nodes) {
+        set_error("invalid mesh");
+        return D2G_ERR_INVALID;
+    }
+    for (int i = 0; i < 3 * nf; i++)
+        if (F[i] < 0 || F[i] >= nv) {
+            set_error("face index out of range");
+            return D2G_ERR_INVALID;
+        }
+    d2g::Mesh m;
+    m.V.assign(V, V + 3 * (size_t)nv);
+    m.F.assign(F, F + 3 * (size_t)nf);
+    d2g::Pcg32 r;
+    r.state = rng[0];
+    r.inc = rng[1];
+    d2g::Tree t;
+    std::string err;
+    if (!d2g::build_tree(m, r, t, &err)) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    *n_nodes = t.n();
+    if (!nodes) return D2G_OK;  // size query: rng untouched
+    if (capacity < t.n()) {
+        set_error("tree capacity too small");
+        return D2G_CAPACITY;
+    }
+    rng[0] = r.state;
+    rng[1] = r.inc;
+    std::memcpy(nodes, t.nodes.data(), t.nodes.size() * sizeof(int32_t));
+    std::memcpy(ntris, t.ntris.data(), t.ntris.size() * sizeof(int32_t));
+    std::memcpy(tris, t.tris.data(), t.tris.size() * sizeof(double));
+    std::memcpy(eps, t.eps.data(), t.eps.size() * sizeof(double));
+    std::memcpy(inner_eps, t.inner_eps.data(), t.inner_eps.size() * sizeof(double));
+    return D2G_OK;
+}
+
+// ------------------------------------------------------------ context -----
+int d2g_ctx_create(int32_t device, d2g_ctx** out) {
+    if (!out) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device");
+        return D2G_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) {
+        set_error("device index out of range");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(device));
+    d2g_ctx* c = new d2g_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_pinned, 64 * sizeof(int32_t));
+    if (e != cudaSuccess) {
+        set_error(std::string("context creation: ") + cudaGetErrorString(e));
+        delete c;
+        return D2G_ERR_CUDA;
+    }
+    *out = c;
+    return D2G_OK;
+}
+
+void d2g_ctx_destroy(d2g_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->mesh_node_off.release();
+    c->ntris.release();
+    c->nodes.release();
+    c->tris.release();
+    c->eps.release();
+    c->inner_eps.release();
+    c->mesh.release();
+    c->sleep_steps.release();
+    c->is_static.release();
+    c->sleeping.release();
+    c->geo_eps.release();
+    c->mu.release();
+    c->mass.release();
+    c->inv_inertia.release();
+    c->last.release();
+    c->cur.release();
+    c->fut.release();
+    c->last_dt.release();
+    c->bounding_radius.release();
+    d2g::Engine& E = c->eng;
+    E.soup.release();
+    E.conn.release();
+    E.soup_next.release();
+    E.conn_next.release();
+    E.entry_hits.release();
+    E.cnt_a.release();
+    E.cnt_b.release();
+    E.off_a.release();
+    E.off_b.release();
+    E.flags.release();
+    E.flag_off.release();
+    E.items.release();
+    E.res.release();
+    E.hit.release();
+    E.pm.release();
+    E.pfut.release();
+    E.search.release();
+    E.last_pair.release();
+    E.rec.release();
+    E.rec_sorted.release();
+    E.rec_pair.release();
+    E.rec_pair_sorted.release();
+    E.rec_idx.release();
+    E.rec_idx_sorted.release();
+    E.out_off.release();
+    E.pair_cnt.release();
+    E.d_pairs.release();
+    E.d_max_time.release();
+    E.cub_tmp.release();
+    E.scratch_i32.release();
+    for (auto& p : E.pending) {
+        cudaEventDestroy(p.e0);
+        cudaEventDestroy(p.e1);
+    }
+    for (auto ev : E.event_pool) cudaEventDestroy(ev);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int d2g_ctx_stream(d2g_ctx* c, void** stream) {
+    if (!c || !stream) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    *stream = (void*)c->stream;
+    return D2G_OK;
+}
+
+int d2g_ctx_sync(d2g_ctx* c) {
+    if (!c) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    return D2G_OK;
+}
+
+int d2g_ctx_set_trees(d2g_ctx* c, const d2g_trees* t) {
+    if (!c || !t || t->n_meshes <= 0 || !t->mesh_node_off) {
+        set_error("invalid trees");
+        return D2G_ERR_INVALID;
+    }
+    const int N = t->mesh_node_off[t->n_meshes];
+    if (N <= 0 || t->mesh_node_off[0] != 0) {
+        set_error("invalid mesh_node_off");
+        return D2G_ERR_INVALID;
+    }
+    for (int m = 0; m < t->n_meshes; m++)
+        if (t->mesh_node_off[m + 1] <= t->mesh_node_off[m]) {
+            set_error("every mesh needs at least one node");
+            return D2G_ERR_INVALID;
+        }
+    for (int g = 0; g < N; g++) {
+        const int32_t* nd = t->nodes + 4 * (size_t)g;
+        if (t->ntris[g] < 0 || t->ntris[g] > 8 || nd[1] < 0 || nd[1] > 8 ||
+            (nd[2] && (nd[0] < 0 || nd[0] + nd[1] > N)) || (!nd[2] && nd[1] != 0)) {
+            set_error("invalid node " + std::to_string(g));
+            return D2G_ERR_INVALID;
+        }
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    RC(upload(c, c->mesh_node_off, t->mesh_node_off, (size_t)t->n_meshes + 1));
+    RC(upload(c, c->nodes, (const int4*)t->nodes, (size_t)N));
+    RC(upload(c, c->ntris, t->ntris, (size_t)N));
+    RC(upload(c, c->tris, t->tris, 72 * (size_t)N));
+    RC(upload(c, c->eps, t->eps, 8 * (size_t)N));
+    RC(upload(c, c->inner_eps, t->inner_eps, 8 * (size_t)N));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    c->n_meshes = t->n_meshes;
+    c->n_nodes = N;
+    return D2G_OK;
+}
+
+int d2g_ctx_set_bodies(d2g_ctx* c, const d2g_bodies* b) {
+    if (!c || !b || b->n <= 0) {
+        set_error("invalid bodies");
+        return D2G_ERR_INVALID;
+    }
+    if (c->n_meshes == 0) {
+        set_error("set trees before bodies");
+        return D2G_ERR_STATE;
+    }
+    for (int i = 0; i < b->n; i++)
+        if (b->mesh[i] < 0 || b->mesh[i] >= c->n_meshes) {
+            set_error("body " + std::to_string(i) + " has mesh id out of range");
+            return D2G_ERR_INVALID;
+        }
+    const size_t n = (size_t)b->n;
+    RC(upload(c, c->mesh, b->mesh, n));
+    RC(upload(c, c->is_static, b->is_static, n));
+    RC(upload(c, c->geo_eps, b->geo_eps, n));
+    RC(upload(c, c->mu, b->mu, n));
+    RC(upload(c, c->mass, b->mass, n));
+    RC(upload(c, c->inv_inertia, b->inv_inertia, 9 * n));
+    RC(upload(c, c->last, (const double*)b->last, 14 * n));
+    RC(upload(c, c->cur, (const double*)b->cur, 14 * n));
+    RC(upload(c, c->fut, (const double*)b->fut, 14 * n));
+    RC(upload(c, c->last_dt, (const double*)b->last_dt, n));
+    if (b->sleep_steps) RC(upload(c, c->sleep_steps, (const int32_t*)b->sleep_steps, n));
+    if (b->sleeping) RC(upload(c, c->sleeping, (const uint8_t*)b->sleeping, n));
+    if (b->bounding_radius) RC(upload(c, c->bounding_radius, b->bounding_radius, n));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    c->n_bodies = b->n;
+    return D2G_OK;
+}
+
+int d2g_ctx_get_bodies(d2g_ctx* c, d2g_bodies* b) {
+    if (!c || !b || b->n != c->n_bodies) {
+        set_error("body count mismatch");
+        return D2G_ERR_INVALID;
+    }
+    const size_t n = (size_t)b->n;
+    RC(download(c, b->last, c->last, 14 * n));
+    RC(download(c, b->cur, c->cur, 14 * n));
+    RC(download(c, b->fut, c->fut, 14 * n));
+    RC(download(c, b->last_dt, c->last_dt, n));
+    if (b->sleep_steps && c->sleep_steps.p) RC(download(c, b->sleep_steps, c->sleep_steps, n));
+    if (b->sleeping && c->sleeping.p) RC(download(c, b->sleeping, c->sleeping, n));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    return D2G_OK;
+}
+
+int d2g_ctx_launches(d2g_ctx* c, int64_t* launches) {
+    if (!c || !launches) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    *launches = c->eng.launches;
+    return D2G_OK;
+}
+
+int d2g_ctx_set_profiling(d2g_ctx* c, int32_t enable) {
+    if (!c) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    d2g::Engine& E = c->eng;
+    for (auto& p : E.pending) {
+        E.event_pool.push_back(p.e0);
+        E.event_pool.push_back(p.e1);
+    }
+    E.pending.clear();
+    for (int k = 0; k < d2g::D2G_PROF_KINDS; k++) {
+        E.prof_ms[k] = 0;
+        E.prof_launches[k] = 0;
+        E.prof_items[k] = 0;
+    }
+    E.profiling = enable != 0;
+    return D2G_OK;
+}
+
+int d2g_ctx_profile(d2g_ctx* c, int32_t kind, double* ms, int64_t* launches, int64_t* items) {
+    if (!c || kind < 0 || kind >= d2g::D2G_PROF_KINDS) {
+        set_error("invalid profile query");
+        return D2G_ERR_INVALID;
+    }
+    if (ms) *ms = c->eng.prof_ms[kind];
+    if (launches) *launches = c->eng.prof_launches[kind];
+    if (items) *items = c->eng.prof_items[kind];
+    return D2G_OK;
+}
+
+// ------------------------------------------------------------ queries -----
+int d2g_compare_trees_full(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, double* contacts, int32_t capacity,
+                           int32_t* offsets, int64_t* counters) {
+    RC(check_ready(c));
+    RC(check_pairs(c, pairs, n_pairs));
+    D2G_CUDA(cudaSetDevice(c->device));
+    RC(upload(c, c->eng.d_pairs, pairs, 2 * (size_t)n_pairs));
+    int n_rec = 0;
+    RC(d2g::run_narrowphase(c, c->eng.d_pairs.p, n_pairs, &n_rec, counters));
+    return copy_out(c, n_pairs, n_rec, contacts, capacity, offsets);
+}
+
+int d2g_compare_trees_full_continuous(d2g_ctx* c, const int32_t* pairs, const double* max_time, int32_t n_pairs,
+                                      double* contacts, int32_t capacity, int32_t* offsets, int64_t* counters) {
+    RC(check_ready(c));
+    RC(check_pairs(c, pairs, n_pairs));
+    if (n_pairs > 0 && !max_time) {
+        set_error("null max_time");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    RC(upload(c, c->eng.d_pairs, pairs, 2 * (size_t)n_pairs));
+    RC(upload(c, c->eng.d_max_time, max_time, (size_t)n_pairs));
+    int n_rec = 0;
+    RC(d2g::run_ccd(c, c->eng.d_pairs.p, c->eng.d_max_time.p, n_pairs, &n_rec, counters));
+    return copy_out(c, n_pairs, n_rec, contacts, capacity, offsets);
+}
+
+int d2g_compare_trees_full_continuous_device(d2g_ctx* c, const int32_t* d_pairs, const double* d_max_time,
+                                             int32_t n_pairs, int32_t* n_contacts, const double** d_contacts,
+                                             const int32_t** d_offsets, int64_t* counters) {
+    RC(check_ready(c));
+    if (n_pairs < 0 || (n_pairs > 0 && (!d_pairs || !d_max_time))) {
+        set_error("invalid device pair list");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    if (c->validated_pairs != d_pairs || c->validated_n != n_pairs) {  // index check once per pair buffer
+        std::vector<int32_t> h(2 * (size_t)n_pairs);
+        if (n_pairs) D2G_CUDA(cudaMemcpy(h.data(), d_pairs, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        RC(check_pairs(c, h.data(), n_pairs));
+        c->validated_pairs = d_pairs;
+        c->validated_n = n_pairs;
+    }
+    int n_rec = 0;
+    RC(d2g::run_ccd(c, d_pairs, d_max_time, n_pairs, &n_rec, counters));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    if (n_contacts) *n_contacts = n_rec;
+    if (d_contacts) *d_contacts = c->eng.rec_sorted.p;
+    if (d_offsets) *d_offsets = c->eng.out_off.p;
+    return D2G_OK;
+}
+
+}  // extern "C"

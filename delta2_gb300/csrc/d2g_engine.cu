@@ -1,0 +1,726 @@
+// Level-synchronous surrogate-tree traversal on the GPU, for all body pairs
+// of a call at once.
+//
+// The reference walks one body pair at a time, level by level
+// (collision_detection/full_tree_comparison.h:13-219).  Here every frontier
+// holds the node pairs of ALL body pairs, sorted by body pair and, within a
+// pair, in the reference's order; every expansion is an ordered compaction
+// (prefix sums), so the contacts of each pair come out in exactly the order
+// the reference's sequential loops produce them.  Each level of each stage
+// is three kinds of launches:
+//   1. a cheap filter over all primitive slots (swept boxes in the CCD soup
+//      stage), compacted into a dense work list;
+//   2. one thread per primitive test (triangle-triangle CCD, point-triangle
+//      CCD, edge-edge CCD or discrete triangle distance) writing its result
+//      and hit flag;
+//   3. ordered compaction of the contacts of leaf-leaf node pairs and
+//      expansion of the node pairs that hit into the next frontiers.
+// All arithmetic is FP64 with -fmad=false, in the order declared in
+// d2g_geom.cuh, so results equal the CPU restatement bit for bit.
+#include <cub/cub.cuh>
+
+#include "d2g_geom.cuh"
+#include "d2g_internal.hpp"
+
+namespace d2g {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+__device__ __forceinline__ int4 ld_node(const int4* nodes, int g) { return nodes[g]; }
+
+// ------------------------------------------------------------- CCD prep ----
+// Projects both futures over the pair's max_time (model/state.cpp:90-102,
+// full_tree_comparison.h:78-79) and forms the pose matrices.
+__global__ void k_ccd_prep(int n, const int32_t* __restrict__ pairs, const double* __restrict__ max_time,
+                           const double* __restrict__ cur, const double* __restrict__ ii,
+                           const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
+                           const double* __restrict__ geo_eps, double* __restrict__ pm, double* __restrict__ pfut,
+                           float* __restrict__ search, Entry* __restrict__ soup) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int a = pairs[2 * p], b = pairs[2 * p + 1];
+    const double mt = max_time[p];
+    const State ca = load_state(cur + 14 * (size_t)a);
+    const State cb = load_state(cur + 14 * (size_t)b);
+    const State fa = extrapolate(ca, mt, ii + 9 * (size_t)a);
+    const State fb = extrapolate(cb, mt, ii + 9 * (size_t)b);
+    pair_mats(ca, fa, cb, fb, pm + (size_t)PM_SIZE * p);
+    store_state(pfut + 28 * (size_t)p, fa);
+    store_state(pfut + 28 * (size_t)p + 14, fb);
+    search[p] = (float)(geo_eps[a] + geo_eps[b]);
+    Entry e;
+    e.pair = p;
+    e.na = mesh_node_off[mesh[a]];
+    e.nb = mesh_node_off[mesh[b]];
+    soup[p] = e;
+}
+
+// Discrete narrow phase prep: future transforms of a and b (comparison_dist.h:225,229).
+__global__ void k_np_prep(int n, const int32_t* __restrict__ pairs, const double* __restrict__ fut,
+                          const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
+                          const double* __restrict__ geo_eps, double* __restrict__ pm, float* __restrict__ search,
+                          Entry* __restrict__ front) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int a = pairs[2 * p], b = pairs[2 * p + 1];
+    const State fa = load_state(fut + 14 * (size_t)a);
+    const State fb = load_state(fut + 14 * (size_t)b);
+    transformation(fa.q, fa.x, pm + 32 * (size_t)p);
+    transformation(fb.q, fb.x, pm + 32 * (size_t)p + 16);
+    search[p] = (float)(geo_eps[a] + geo_eps[b]);
+    Entry e;
+    e.pair = p;
+    e.na = mesh_node_off[mesh[a]];
+    e.nb = mesh_node_off[mesh[b]];
+    front[p] = e;
+}
+
+// ------------------------------------------------------------ soup stage ---
+// Swept-box filter of every (node pair, a-triangle, b-triangle) slot
+// (continuous_comparison.h:804-812).
+__global__ void k_soup_filter(int n_slots, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
+                              const double* __restrict__ pm, const int32_t* __restrict__ ntris,
+                              const double* __restrict__ tris, const double* __restrict__ geo_eps,
+                              int32_t* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_slots) return;
+    const Entry e = soup[i >> 6];
+    const int ta = (i >> 3) & 7, tb = i & 7;
+    int f = 0;
+    if (ta < ntris[e.na] && tb < ntris[e.nb]) {
+        const double* M = pm + (size_t)PM_SIZE * e.pair;
+        const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
+        const Tri at = load_tri(tris + (size_t)e.na * 72 + ta * 9);
+        const Tri bt = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
+        const Box ba = swept_box(at, M + PM_AS, M + PM_AE, geo_eps[a]);
+        const Box bb = swept_box(bt, M + PM_BS, M + PM_BE, geo_eps[b]);
+        f = box_overlap(ba, bb) ? 1 : 0;
+    }
+    flags[i] = f;
+}
+
+__global__ void k_compact(int n, const int32_t* __restrict__ flags, const int32_t* __restrict__ off,
+                          int32_t* __restrict__ items) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (flags[i]) items[off[i]] = i;
+}
+
+__device__ __forceinline__ void put_result(PrimResult& r, double dist, V3 A, V3 B, double toc) {
+    r.dist = dist;
+    r.P[0] = A.x;
+    r.P[1] = A.y;
+    r.P[2] = A.z;
+    r.Q[0] = B.x;
+    r.Q[1] = B.y;
+    r.Q[2] = B.z;
+    r.toc = toc;
+}
+
+// Triangle-triangle CCD of each surviving slot (continuous_comparison.h:815-820).
+__global__ void __launch_bounds__(kBlock) k_soup_ccd(int n_items, const int32_t* __restrict__ items,
+                                                     const Entry* __restrict__ soup, const double* __restrict__ pm,
+                                                     const double* __restrict__ tris,
+                                                     const float* __restrict__ search, PrimResult* __restrict__ res,
+                                                     int32_t* __restrict__ hit, int32_t* __restrict__ entry_hits) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    const int i = items[k];
+    const Entry e = soup[i >> 6];
+    const int ta = (i >> 3) & 7, tb = i & 7;
+    const double* M = pm + (size_t)PM_SIZE * e.pair;
+    const Tri at = load_tri(tris + (size_t)e.na * 72 + ta * 9);
+    const Tri bt = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
+    const Ccd r = tri_tri_ccd(at, bt, M);
+    put_result(res[k], r.dist, r.P, r.Q, r.toc);
+    const int h = r.dist < (double)search[e.pair] ? 1 : 0;
+    hit[k] = h;
+    if (h) atomicAdd(&entry_hits[i >> 6], 1);
+}
+
+// ------------------------------------------------------- connected stage ---
+// Primitive tests of a leaf-leaf node pair (continuous_comparison.h:831-910):
+// 3*na*nb point(a)-triangle(b), 3*nb*na point(b)-triangle(a), 9*na*nb edge-edge.
+__global__ void k_conn_count(int n, const Entry* __restrict__ conn, const int32_t* __restrict__ ntris,
+                             int32_t* __restrict__ cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Entry e = conn[i];
+    cnt[i] = 15 * ntris[e.na] * ntris[e.nb];
+}
+
+__global__ void __launch_bounds__(kBlock) k_conn(int n_items, int n_entries, const int32_t* __restrict__ off,
+                                                 const Entry* __restrict__ conn, const double* __restrict__ pm,
+                                                 const int32_t* __restrict__ ntris,
+                                                 const double* __restrict__ tris, const float* __restrict__ search,
+                                                 PrimResult* __restrict__ res, int32_t* __restrict__ hit) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    int lo = 0, hi = n_entries;  // last entry with off[e] <= k
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= k)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const Entry e = conn[lo];
+    const int l = k - off[lo];
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    const double* M = pm + (size_t)PM_SIZE * e.pair;
+    const double* ta = tris + (size_t)e.na * 72;
+    const double* tb = tris + (size_t)e.nb * 72;
+    const int n1 = 3 * na * nb, n2 = 3 * nb * na;
+    Ccd r;
+    V3 A, B;
+    if (l < n1) {
+        const int vi = l / nb, j = l % nb;
+        const Tri t = load_tri(ta + (vi / 3) * 9);
+        r = point_tri_ccd(tvert(t, vi % 3), M + PM_ABS, M + PM_ABE, load_tri(tb + j * 9), M + PM_BS, M + PM_BE);
+        A = r.P;
+        B = r.Q;
+    } else if (l < n1 + n2) {
+        const int m = l - n1;
+        const int vi = m / na, j = m % na;
+        const Tri t = load_tri(tb + (vi / 3) * 9);
+        r = point_tri_ccd(tvert(t, vi % 3), M + PM_BAS, M + PM_BAE, load_tri(ta + j * 9), M + PM_AS, M + PM_AE);
+        A = r.Q;
+        B = r.P;
+    } else {
+        const int m = l - n1 - n2;
+        const int ei = m / (3 * nb), ej = m % (3 * nb);
+        const Edge ea = tedge(load_tri(ta + (ei / 3) * 9), ei % 3);
+        const Edge eb = tedge(load_tri(tb + (ej / 3) * 9), ej % 3);
+        Edge aS, aE, bS, bE;
+        aS.A = xform_rigid(ea.A, M + PM_AS);
+        aS.B = xform_rigid(ea.B, M + PM_AS);
+        aE.A = xform_rigid(ea.A, M + PM_AE);
+        aE.B = xform_rigid(ea.B, M + PM_AE);
+        bS.A = xform_rigid(eb.A, M + PM_BS);
+        bS.B = xform_rigid(eb.B, M + PM_BS);
+        bE.A = xform_rigid(eb.A, M + PM_BE);
+        bE.B = xform_rigid(eb.B, M + PM_BE);
+        r = edge_edge_ccd(aS, aE, bS, bE);
+        A = r.Q;
+        B = r.P;
+    }
+    put_result(res[k], r.dist, A, B, r.toc);
+    hit[k] = r.dist < (double)search[e.pair] ? 1 : 0;
+}
+
+// ----------------------------------------------------------- discrete -----
+// All 64 slots of a node pair: triangle distance at the future poses and the
+// hit test dist < float(search) + eps_a + eps_b (comparison_dist.h:223-236).
+__global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restrict__ front,
+                                               const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
+                                               const double* __restrict__ eps, const double* __restrict__ inner_eps,
+                                               const double* __restrict__ geo_eps,
+                                               const float* __restrict__ search, PrimResult* __restrict__ res,
+                                               double* __restrict__ res_eps, int32_t* __restrict__ hit,
+                                               int32_t* __restrict__ entry_hits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_slots) return;
+    const Entry e = front[i >> 6];
+    const int ta = (i >> 3) & 7, tb = i & 7;
+    int h = 0;
+    if (ta < ntris[e.na] && tb < ntris[e.nb]) {
+        const double* M = pm + 32 * (size_t)e.pair;
+        const Tri A = tri_xform_rigid(load_tri(tris + (size_t)e.na * 72 + ta * 9), M);
+        const Tri B = tri_xform_rigid(load_tri(tris + (size_t)e.nb * 72 + tb * 9), M + 16);
+        V3 P, Q;
+        const double d = tri_tri_dist(A, B, P, Q);
+        const double ea = eps[(size_t)e.na * 8 + ta], eb = eps[(size_t)e.nb * 8 + tb];
+        h = d < ((double)search[e.pair] + ea) + eb ? 1 : 0;
+        if (h) {
+            const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
+            put_result(res[i], d, P, Q, 0.0);
+            res_eps[4 * (size_t)i + 0] = geo_eps[a] + ea;
+            res_eps[4 * (size_t)i + 1] = geo_eps[b] + eb;
+            res_eps[4 * (size_t)i + 2] = inner_eps[(size_t)e.na * 8 + ta];
+            res_eps[4 * (size_t)i + 3] = inner_eps[(size_t)e.nb * 8 + tb];
+            atomicAdd(&entry_hits[i >> 6], 1);
+        }
+    }
+    hit[i] = h;
+}
+
+// --------------------------------------------------- finals / expansion ----
+// Final-contact flag of each result: a hit inside a leaf-leaf node pair.
+// `slot_entry` maps a result to its entry: item >> 6 through `items` when
+// given (soup stage), else the slot index >> 6 (discrete stage).
+__global__ void k_final_flags(int n, const int32_t* __restrict__ items, const Entry* __restrict__ front,
+                              const int4* __restrict__ nodes, const int32_t* __restrict__ hit,
+                              int32_t* __restrict__ flags) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int slot = items ? items[k] : k;
+    int f = 0;
+    if (hit[k]) {
+        const Entry e = front[slot >> 6];
+        f = (!ld_node(nodes, e.na).z && !ld_node(nodes, e.nb).z) ? 1 : 0;
+    }
+    flags[k] = f;
+}
+
+// Append flagged results as contact records (collision_detection/contact.h).
+__global__ void k_emit(int n, const int32_t* __restrict__ flags, const int32_t* __restrict__ off,
+                       const int32_t* __restrict__ items, int slot_shift, const Entry* __restrict__ front,
+                       const int32_t* __restrict__ conn_off, int n_conn, const int32_t* __restrict__ pairs,
+                       const PrimResult* __restrict__ res, const double* __restrict__ res_eps,
+                       const double* __restrict__ geo_eps, double* __restrict__ rec, int32_t* __restrict__ rec_pair,
+                       int base) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || !flags[k]) return;
+    int ei;
+    if (conn_off) {
+        int lo = 0, hi = n_conn;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (conn_off[mid] <= k)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        ei = lo;
+    } else {
+        ei = (items ? items[k] : k) >> slot_shift;
+    }
+    const Entry e = front[ei];
+    const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
+    const PrimResult& r = res[k];
+    double* o = rec + 14 * (size_t)(base + off[k]);
+    o[0] = r.P[0];
+    o[1] = r.P[1];
+    o[2] = r.P[2];
+    o[3] = r.Q[0];
+    o[4] = r.Q[1];
+    o[5] = r.Q[2];
+    if (res_eps) {
+        o[6] = res_eps[4 * (size_t)k + 0];
+        o[7] = res_eps[4 * (size_t)k + 1];
+        o[8] = res_eps[4 * (size_t)k + 2];
+        o[9] = res_eps[4 * (size_t)k + 3];
+    } else {
+        o[6] = geo_eps[a];
+        o[7] = geo_eps[b];
+        o[8] = 0.0;
+        o[9] = 0.0;
+    }
+    o[10] = r.toc;
+    o[11] = (double)a;
+    o[12] = (double)b;
+    o[13] = 0.0;
+    rec_pair[base + off[k]] = e.pair;
+}
+
+// Expansion rule of full_tree_comparison.h:27-59: leaf-leaf keeps its hits,
+// otherwise the shallower inner side (b on ties, the inner one when the other
+// is a leaf) is replaced by its children.  `split` separates children into
+// the soup (some inner node) and connected (both leaves) frontiers.
+__global__ void k_expand_count(int n, const Entry* __restrict__ front, const int32_t* __restrict__ entry_hits,
+                               const int4* __restrict__ nodes, int split, int32_t* __restrict__ cnt_s,
+                               int32_t* __restrict__ cnt_c) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = 0, c = 0;
+    if (entry_hits[i] > 0) {
+        const Entry e = front[i];
+        const int4 A = ld_node(nodes, e.na), B = ld_node(nodes, e.nb);
+        int rule;
+        if (!A.z && !B.z)
+            rule = 0;
+        else if (!A.z)
+            rule = 2;
+        else if (!B.z)
+            rule = 1;
+        else
+            rule = A.w < B.w ? 1 : 2;
+        if (rule) {
+            const int4 P = rule == 1 ? A : B;
+            for (int ch = 0; ch < P.y; ch++) {
+                const int ga = rule == 1 ? P.x + ch : e.na;
+                const int gb = rule == 1 ? e.nb : P.x + ch;
+                const bool inner = ld_node(nodes, ga).z || ld_node(nodes, gb).z;
+                if (!split || inner)
+                    s++;
+                else
+                    c++;
+            }
+        }
+    }
+    cnt_s[i] = s;
+    cnt_c[i] = c;
+}
+
+__global__ void k_expand_write(int n, const Entry* __restrict__ front, const int32_t* __restrict__ entry_hits,
+                               const int4* __restrict__ nodes, int split, const int32_t* __restrict__ off_s,
+                               const int32_t* __restrict__ off_c, Entry* __restrict__ next_s,
+                               Entry* __restrict__ next_c) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || entry_hits[i] <= 0) return;
+    const Entry e = front[i];
+    const int4 A = ld_node(nodes, e.na), B = ld_node(nodes, e.nb);
+    int rule;
+    if (!A.z && !B.z)
+        rule = 0;
+    else if (!A.z)
+        rule = 2;
+    else if (!B.z)
+        rule = 1;
+    else
+        rule = A.w < B.w ? 1 : 2;
+    if (!rule) return;
+    const int4 P = rule == 1 ? A : B;
+    int s = off_s[i], c = off_c[i];
+    for (int ch = 0; ch < P.y; ch++) {
+        Entry x;
+        x.pair = e.pair;
+        x.na = rule == 1 ? P.x + ch : e.na;
+        x.nb = rule == 1 ? e.nb : P.x + ch;
+        const bool inner = ld_node(nodes, x.na).z || ld_node(nodes, x.nb).z;
+        if (!split || inner)
+            next_s[s++] = x;
+        else
+            next_c[c++] = x;
+    }
+}
+
+// ---------------------------------------------------------- output sort ----
+__global__ void k_iota(int n, int32_t* __restrict__ v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = i;
+}
+__global__ void k_count_pairs(int n, const int32_t* __restrict__ rec_pair, int32_t* __restrict__ cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[rec_pair[i]], 1);
+}
+__global__ void k_gather(int n, const int32_t* __restrict__ idx, const double* __restrict__ in,
+                         double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* s = in + 14 * (size_t)idx[i];
+    double* d = out + 14 * (size_t)i;
+#pragma unroll
+    for (int k = 0; k < 14; k++) d[k] = s[k];
+}
+
+// Future state left on each body: the projection of the last pair containing it.
+__global__ void k_last_pair(int n, const int32_t* __restrict__ pairs, int32_t* __restrict__ last) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    atomicMax(&last[pairs[2 * p]], p);
+    atomicMax(&last[pairs[2 * p + 1]], p);
+}
+__global__ void k_write_fut(int n, const int32_t* __restrict__ pairs, const int32_t* __restrict__ last,
+                            const double* __restrict__ pfut, double* __restrict__ fut) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int a = pairs[2 * p], b = pairs[2 * p + 1];
+    if (last[a] == p)
+        for (int k = 0; k < 14; k++) fut[14 * (size_t)a + k] = pfut[28 * (size_t)p + k];
+    if (last[b] == p)
+        for (int k = 0; k < 14; k++) fut[14 * (size_t)b + k] = pfut[28 * (size_t)p + 14 + k];
+}
+
+__global__ void k_fill(int n, int32_t* __restrict__ v, int32_t x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = x;
+}
+
+// ------------------------------------------------------------ host side ----
+#define LAUNCH(kern, n, ...)                                                \
+    do {                                                                    \
+        kern<<<nblocks(n), kBlock, 0, ctx->stream>>>(__VA_ARGS__);          \
+        ctx->eng.launches++;                                                \
+    } while (0)
+
+// Profiling mode: an event pair around a dominant kernel's launch; the
+// elapsed times are collected at the next stream synchronisation.
+int prof_begin(d2g_ctx* ctx, int kind, long long items) {
+    Engine& E = ctx->eng;
+    if (!E.profiling) return -1;
+    cudaEvent_t ev[2];
+    for (int i = 0; i < 2; i++) {
+        if (!E.event_pool.empty()) {
+            ev[i] = E.event_pool.back();
+            E.event_pool.pop_back();
+        } else if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+            return -1;
+        }
+    }
+    cudaEventRecord(ev[0], ctx->stream);
+    E.pending.push_back(Engine::Pending{kind, ev[0], ev[1], items});
+    return (int)E.pending.size() - 1;
+}
+void prof_end(d2g_ctx* ctx, int idx) {
+    if (idx >= 0) cudaEventRecord(ctx->eng.pending[idx].e1, ctx->stream);
+}
+// Call only after the stream has been synchronised.
+void prof_collect(d2g_ctx* ctx) {
+    Engine& E = ctx->eng;
+    for (auto& p : E.pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.e0, p.e1) == cudaSuccess) {
+            E.prof_ms[p.kind] += ms;
+            E.prof_launches[p.kind] += 1;
+            E.prof_items[p.kind] += p.items;
+        }
+        E.event_pool.push_back(p.e0);
+        E.event_pool.push_back(p.e1);
+    }
+    E.pending.clear();
+}
+
+// Exclusive prefix sum of in[0..n) into out[0..n], out[n] = total.
+int scan(d2g_ctx* ctx, const int32_t* in, int32_t* out, int n) {
+    Engine& E = ctx->eng;
+    D2G_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), ctx->stream));
+    if (n == 0) return D2G_OK;
+    size_t bytes = 0;
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out + 1, n, ctx->stream));
+    if (int rc = E.cub_tmp.ensure(bytes + 16)) return rc;
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, in, out + 1, n, ctx->stream));
+    return D2G_OK;
+}
+
+// Read k device int32 scalars (after the stream's pending work).
+int read_scalars(d2g_ctx* ctx, const int32_t* const* src, int k, int32_t* dst) {
+    for (int i = 0; i < k; i++)
+        D2G_CUDA(cudaMemcpyAsync(ctx->h_pinned + i, src[i], sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    D2G_CUDA(cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
+    for (int i = 0; i < k; i++) dst[i] = ctx->h_pinned[i];
+    return D2G_OK;
+}
+
+#define RC(x)                     \
+    do {                          \
+        if (int rc_ = (x)) return rc_; \
+    } while (0)
+
+// Append the flagged results of a stage to the record buffer.
+int append_records(d2g_ctx* ctx, int n, const int32_t* flags, const int32_t* items, int slot_shift,
+                   const Entry* front, const int32_t* conn_off, int n_conn, const int32_t* d_pairs,
+                   const double* res_eps, int& n_rec) {
+    Engine& E = ctx->eng;
+    RC(E.flag_off.ensure(n + 1));
+    RC(scan(ctx, flags, E.flag_off.p, n));
+    int32_t tot;
+    const int32_t* src = E.flag_off.p + n;
+    RC(read_scalars(ctx, &src, 1, &tot));
+    if (tot == 0) return D2G_OK;
+    RC(E.rec.ensure(14 * (size_t)(n_rec + tot)));
+    RC(E.rec_pair.ensure(n_rec + tot));
+    LAUNCH(k_emit, n, n, flags, E.flag_off.p, items, slot_shift, front, conn_off, n_conn,
+                                                   d_pairs, E.res.p, res_eps, ctx->geo_eps.p, E.rec.p,
+                                                   E.rec_pair.p, n_rec);
+    n_rec += tot;
+    return D2G_OK;
+}
+
+// Sort records by pair (stable) into rec_sorted and write offsets [n_pairs+1].
+int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
+    Engine& E = ctx->eng;
+    RC(E.out_off.ensure(n_pairs + 1));
+    RC(E.pair_cnt.ensure(n_pairs + 1));
+    RC(E.rec_sorted.ensure(14 * (size_t)n_rec + 14));
+    D2G_CUDA(cudaMemsetAsync(E.pair_cnt.p, 0, sizeof(int32_t) * (n_pairs + 1), ctx->stream));
+    if (n_rec > 0) {
+        RC(E.rec_idx.ensure(n_rec));
+        RC(E.rec_idx_sorted.ensure(n_rec));
+        RC(E.rec_pair_sorted.ensure(n_rec));
+        LAUNCH(k_iota, n_rec, n_rec, E.rec_idx.p);
+        int bits = 1;
+        while ((1 << bits) < n_pairs + 1 && bits < 31) bits++;
+        size_t bytes = 0;
+        D2G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, bytes, E.rec_pair.p, E.rec_pair_sorted.p, E.rec_idx.p,
+                                                 E.rec_idx_sorted.p, n_rec, 0, bits, ctx->stream));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceRadixSort::SortPairs(E.cub_tmp.p, bytes, E.rec_pair.p, E.rec_pair_sorted.p, E.rec_idx.p,
+                                                 E.rec_idx_sorted.p, n_rec, 0, bits, ctx->stream));
+        LAUNCH(k_gather, n_rec, n_rec, E.rec_idx_sorted.p, E.rec.p, E.rec_sorted.p);
+        LAUNCH(k_count_pairs, n_rec, n_rec, E.rec_pair.p, E.pair_cnt.p);
+    }
+    RC(scan(ctx, E.pair_cnt.p, E.out_off.p, n_pairs));
+    return D2G_OK;
+}
+
+}  // namespace
+
+int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
+            int64_t* counters) {
+    Engine& E = ctx->eng;
+    cudaStream_t s = ctx->stream;
+    int64_t c_node = 0, c_tri = 0, c_leaf = 0, c_levels = 0;
+    RC(E.pm.ensure((size_t)PM_SIZE * n_pairs + 1));
+    RC(E.pfut.ensure(28 * (size_t)n_pairs + 1));
+    RC(E.search.ensure(n_pairs + 1));
+    RC(E.soup.ensure(n_pairs + 1));
+    int n_rec = 0;
+    if (n_pairs > 0)
+        LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p,
+                                                      ctx->mesh.p, ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p,
+                                                      E.pfut.p, E.search.p, E.soup.p);
+    int n_soup = n_pairs, n_conn = 0;
+    while (n_soup > 0 || n_conn > 0) {
+        c_levels++;
+        c_node += n_soup + n_conn;
+        c_leaf += n_conn;
+        if (n_soup > 0) {
+            const int n_slots = 64 * n_soup;
+            RC(E.flags.ensure(n_slots));
+            RC(E.flag_off.ensure(n_slots + 1));
+            RC(E.entry_hits.ensure(n_soup));
+            D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
+            const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
+            LAUNCH(k_soup_filter, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p,
+                                                              ctx->tris.p, ctx->geo_eps.p, E.flags.p);
+            prof_end(ctx, pff);
+            RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
+            int32_t n_items;
+            const int32_t* src = E.flag_off.p + n_slots;
+            RC(read_scalars(ctx, &src, 1, &n_items));
+            c_tri += n_items;
+            if (n_items > 0) {
+                RC(E.items.ensure(n_items));
+                RC(E.res.ensure(n_items));
+                RC(E.hit.ensure(n_items));
+                LAUNCH(k_compact, n_slots, n_slots, E.flags.p, E.flag_off.p, E.items.p);
+                const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_items);
+                LAUNCH(k_soup_ccd, n_items, n_items, E.items.p, E.soup.p, E.pm.p, ctx->tris.p,
+                                                               E.search.p, E.res.p, E.hit.p, E.entry_hits.p);
+                prof_end(ctx, pf);
+                // contacts of leaf-leaf soup node pairs are final (full_tree_comparison.h:104-105)
+                RC(E.flags.ensure(n_items));
+                LAUNCH(k_final_flags, n_items, n_items, E.items.p, E.soup.p, ctx->nodes.p,
+                                                                  E.hit.p, E.flags.p);
+                RC(append_records(ctx, n_items, E.flags.p, E.items.p, 6, E.soup.p, nullptr, 0, d_pairs, nullptr,
+                                  n_rec));
+            }
+        }
+        if (n_conn > 0) {
+            RC(E.cnt_b.ensure(n_conn));
+            RC(E.off_b.ensure(n_conn + 1));
+            LAUNCH(k_conn_count, n_conn, n_conn, E.conn.p, ctx->ntris.p, E.cnt_b.p);
+            RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_conn));
+            int32_t n_items;
+            const int32_t* src = E.off_b.p + n_conn;
+            RC(read_scalars(ctx, &src, 1, &n_items));
+            c_tri += n_items;
+            if (n_items > 0) {
+                RC(E.res.ensure(n_items));
+                RC(E.hit.ensure(n_items));
+                const int pf = prof_begin(ctx, PROF_CONN, n_items);
+                LAUNCH(k_conn, n_items, n_items, n_conn, E.off_b.p, E.conn.p, E.pm.p, ctx->ntris.p,
+                                                           ctx->tris.p, E.search.p, E.res.p, E.hit.p);
+                prof_end(ctx, pf);
+                RC(append_records(ctx, n_items, E.hit.p, nullptr, 0, E.conn.p, E.off_b.p, n_conn, d_pairs, nullptr,
+                                  n_rec));
+            }
+        }
+        int32_t tot[2] = {0, 0};
+        if (n_soup > 0) {
+            RC(E.cnt_a.ensure(n_soup));
+            RC(E.cnt_b.ensure(n_soup));
+            RC(E.off_a.ensure(n_soup + 1));
+            RC(E.off_b.ensure(n_soup + 1));
+            LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1,
+                                                              E.cnt_a.p, E.cnt_b.p);
+            RC(scan(ctx, E.cnt_a.p, E.off_a.p, n_soup));
+            RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_soup));
+            const int32_t* src[2] = {E.off_a.p + n_soup, E.off_b.p + n_soup};
+            RC(read_scalars(ctx, src, 2, tot));
+            RC(E.soup_next.ensure(tot[0] + 1));
+            RC(E.conn_next.ensure(tot[1] + 1));
+            LAUNCH(k_expand_write, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1,
+                                                              E.off_a.p, E.off_b.p, E.soup_next.p, E.conn_next.p);
+        }
+        std::swap(E.soup, E.soup_next);
+        std::swap(E.conn, E.conn_next);
+        n_soup = tot[0];
+        n_conn = tot[1];
+    }
+    RC(finish_records(ctx, n_pairs, n_rec));
+    if (n_pairs > 0) {
+        RC(E.last_pair.ensure(ctx->n_bodies + 1));
+        LAUNCH(k_fill, ctx->n_bodies, ctx->n_bodies, E.last_pair.p, -1);
+        LAUNCH(k_last_pair, n_pairs, n_pairs, d_pairs, E.last_pair.p);
+        LAUNCH(k_write_fut, n_pairs, n_pairs, d_pairs, E.last_pair.p, E.pfut.p, ctx->fut.p);
+    }
+    D2G_CUDA(cudaGetLastError());
+    *n_out = n_rec;
+    if (counters) {
+        counters[0] = c_node;
+        counters[1] = c_tri;
+        counters[2] = c_leaf;
+        counters[3] = c_levels;
+    }
+    return D2G_OK;
+}
+
+int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters) {
+    Engine& E = ctx->eng;
+    cudaStream_t s = ctx->stream;
+    int64_t c_node = 0, c_tri = 0, c_leaf = 0, c_levels = 0;
+    RC(E.pm.ensure(32 * (size_t)n_pairs + 1));
+    RC(E.search.ensure(n_pairs + 1));
+    RC(E.soup.ensure(n_pairs + 1));
+    if (n_pairs > 0)
+        LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, ctx->fut.p, ctx->mesh.p, ctx->mesh_node_off.p,
+                                                     ctx->geo_eps.p, E.pm.p, E.search.p, E.soup.p);
+    int n = n_pairs, n_rec = 0;
+    DBuf<double>& res_eps = E.pfut;  // reused as the per-slot eps record buffer
+    while (n > 0) {
+        c_levels++;
+        c_node += n;
+        const int n_slots = 64 * n;
+        c_tri += n_slots;
+        RC(E.res.ensure(n_slots));
+        RC(res_eps.ensure(4 * (size_t)n_slots));
+        RC(E.hit.ensure(n_slots));
+        RC(E.flags.ensure(n_slots));
+        RC(E.entry_hits.ensure(n));
+        D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n, s));
+        const int pf = prof_begin(ctx, PROF_NP, n_slots);
+        LAUNCH(k_np, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
+                                                 ctx->eps.p, ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p,
+                                                 res_eps.p, E.hit.p, E.entry_hits.p);
+        prof_end(ctx, pf);
+        LAUNCH(k_final_flags, n_slots, n_slots, nullptr, E.soup.p, ctx->nodes.p, E.hit.p,
+                                                          E.flags.p);
+        RC(append_records(ctx, n_slots, E.flags.p, nullptr, 6, E.soup.p, nullptr, 0, d_pairs, res_eps.p, n_rec));
+        RC(E.cnt_a.ensure(n));
+        RC(E.cnt_b.ensure(n));
+        RC(E.off_a.ensure(n + 1));
+        RC(E.off_b.ensure(n + 1));
+        LAUNCH(k_expand_count, n, n, E.soup.p, E.entry_hits.p, ctx->nodes.p, 0, E.cnt_a.p,
+                                                     E.cnt_b.p);
+        RC(scan(ctx, E.cnt_a.p, E.off_a.p, n));
+        D2G_CUDA(cudaMemsetAsync(E.off_b.p, 0, sizeof(int32_t) * (n + 1), s));
+        int32_t tot;
+        const int32_t* src = E.off_a.p + n;
+        RC(read_scalars(ctx, &src, 1, &tot));
+        RC(E.soup_next.ensure(tot + 1));
+        LAUNCH(k_expand_write, n, n, E.soup.p, E.entry_hits.p, ctx->nodes.p, 0, E.off_a.p,
+                                                     E.off_b.p, E.soup_next.p, E.conn_next.p);
+        std::swap(E.soup, E.soup_next);
+        n = tot;
+    }
+    RC(finish_records(ctx, n_pairs, n_rec));
+    D2G_CUDA(cudaGetLastError());
+    *n_out = n_rec;
+    if (counters) {
+        counters[0] = c_node;
+        counters[1] = c_tri;
+        counters[2] = c_leaf;
+        counters[3] = c_levels;
+    }
+    return D2G_OK;
+}
+
+}  // namespace d2g

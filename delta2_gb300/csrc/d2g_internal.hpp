@@ -1,0 +1,130 @@
+// Internal context of the C ABI: device-resident trees and bodies, the
+// growable work buffers of the traversal engine, and error reporting.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/d2g.h"
+
+namespace d2g {
+
+// Kernels timed in profiling mode (d2g_ctx_profile kinds).
+enum { PROF_SOUP_FILTER = 0, PROF_SOUP_CCD = 1, PROF_CONN = 2, PROF_NP = 3, PROF_SOLVE = 4, D2G_PROF_KINDS = 8 };
+
+void set_error(const std::string& msg);
+
+#define D2G_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            ::d2g::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+            return D2G_ERR_CUDA;                                                                    \
+        }                                                                                           \
+    } while (0)
+
+// Device buffer that grows geometrically (capacity in elements).
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n) {
+        if (n <= cap) return D2G_OK;
+        if (p) {
+            cudaDeviceSynchronize();  // no launch still reads the old buffer
+            cudaFree(p);
+        }
+        p = nullptr;
+        size_t c = n + n / 2 + 64;
+        cudaError_t e = cudaMalloc((void**)&p, c * sizeof(T));
+        if (e != cudaSuccess) {
+            cap = 0;
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return D2G_ERR_CUDA;
+        }
+        cap = c;
+        return D2G_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// One frontier entry: body pair index and the two node ids.
+struct Entry {
+    int32_t pair, na, nb;
+};
+
+// Result of one primitive test (tri-tri CCD, point-triangle, edge-edge or
+// discrete tri-tri): distance, the two points, time of contact.
+struct PrimResult {
+    double dist, P[3], Q[3], toc;
+};
+
+struct Engine {
+    // frontiers
+    DBuf<Entry> soup, conn, soup_next, conn_next;
+    // per-entry counters / offsets
+    DBuf<int32_t> entry_hits, cnt_a, cnt_b, off_a, off_b;
+    // items of a stage
+    DBuf<int32_t> flags, flag_off, items;
+    DBuf<PrimResult> res;
+    DBuf<int32_t> hit;
+    // per pair
+    DBuf<double> pm;    // [pairs][128] pose matrices
+    DBuf<double> pfut;  // [pairs][28] projected futures of a and b
+    DBuf<float> search;
+    DBuf<int32_t> last_pair;
+    // results (processing order) and the sorted output
+    DBuf<double> rec, rec_sorted;
+    DBuf<int32_t> rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted, out_off, pair_cnt;
+    DBuf<int32_t> d_pairs;
+    DBuf<double> d_max_time;
+    DBuf<uint8_t> cub_tmp;
+    DBuf<int32_t> scratch_i32;  // small device scalars
+    // instrumentation: kernel launches issued, and optional per-kernel event timing
+    long long launches = 0;
+    bool profiling = false;
+    struct Pending {
+        int kind;
+        cudaEvent_t e0, e1;
+        long long items;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double prof_ms[D2G_PROF_KINDS] = {0};
+    long long prof_launches[D2G_PROF_KINDS] = {0};
+    long long prof_items[D2G_PROF_KINDS] = {0};
+};
+
+}  // namespace d2g
+
+struct d2g_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // trees
+    int n_meshes = 0, n_nodes = 0;
+    d2g::DBuf<int32_t> mesh_node_off, ntris;
+    d2g::DBuf<int4> nodes;
+    d2g::DBuf<double> tris, eps, inner_eps;
+    // bodies
+    int n_bodies = 0;
+    d2g::DBuf<int32_t> mesh, sleep_steps;
+    d2g::DBuf<uint8_t> is_static, sleeping;
+    d2g::DBuf<double> geo_eps, mu, mass, inv_inertia, last, cur, fut, last_dt, bounding_radius;
+    d2g::Engine eng;
+    int32_t* h_pinned = nullptr;  // small pinned scratch for counts
+    const int32_t* validated_pairs = nullptr;  // device pair buffer last checked in range
+    int validated_n = -1;
+};
+
+namespace d2g {
+// Engine entry points (d2g_engine.cu).
+int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
+            int64_t* counters);
+int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
+}  // namespace d2g

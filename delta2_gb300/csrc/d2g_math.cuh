@@ -1,0 +1,161 @@
+// Portable transcendental functions shared by host set-up code and the
+// sm_103a kernels.  The reference's quaternion exponential
+// (common/basic_utils.cpp:36-44) calls std::sin/std::cos, its slerp
+// (model/state.cpp:55-70, through Eigen) calls acos/sin, and the edge-edge
+// Newton step (collision_detection/continuous_comparison.h:631) calls
+// pow(S, 3/2).  CUDA's and glibc's versions of these differ in the last bit
+// for some arguments, so this library evaluates them with its own code:
+//
+//   sin, cos : Cody & Waite (1980) reduction x = k*pi/2 + r with pi/2 split
+//              into three parts (33-bit head), then the Maclaurin series of
+//              sin(r) through r^19 and cos(r) through r^18 by Horner's rule.
+//   acos     : pi/2 - asin(x) for x <= 1/2, else 2*asin(sqrt((1-x)/2)); asin
+//              by its Maclaurin series (30 terms) on [0, 1/2].
+//   log      : frexp reduction and log(m) = 2*atanh((m-1)/(m+1)) (set-up only).
+//   x^(3/2)  : x*sqrt(x).
+//
+// Every kernel translation unit is compiled with -fmad=false and every host
+// unit with -ffp-contract=off, so each operation is rounded on its own and
+// the results are the same bits on the GPU, on x86-64 and on Arm.
+#pragma once
+#include <cmath>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define D2G_HD __host__ __device__ __forceinline__
+#else
+#define D2G_HD inline
+#endif
+
+namespace d2g {
+
+D2G_HD double m_kernel_sin(double r) {
+    const double z = r * r;
+    double p = -8.22063524662433e-18;
+    p = 2.8114572543455206e-15 + z * p;
+    p = -7.647163731819816e-13 + z * p;
+    p = 1.6059043836821613e-10 + z * p;
+    p = -2.505210838544172e-08 + z * p;
+    p = 2.7557319223985893e-06 + z * p;
+    p = -0.0001984126984126984 + z * p;
+    p = 0.008333333333333333 + z * p;
+    p = -0.16666666666666666 + z * p;
+    return r + (r * z) * p;
+}
+
+D2G_HD double m_kernel_cos(double r) {
+    const double z = r * r;
+    double p = -1.5619206968586225e-16;
+    p = 4.779477332387385e-14 + z * p;
+    p = -1.1470745597729725e-11 + z * p;
+    p = 2.08767569878681e-09 + z * p;
+    p = -2.755731922398589e-07 + z * p;
+    p = 2.48015873015873e-05 + z * p;
+    p = -0.001388888888888889 + z * p;
+    p = 0.041666666666666664 + z * p;
+    p = -0.5 + z * p;
+    return 1.0 + z * p;
+}
+
+// x = k*pi/2 + r, |r| <= pi/4 (for |x| <= pi/4 no reduction).
+D2G_HD void m_reduce(double x, double& r, int& q) {
+    const double ax = x < 0.0 ? -x : x;
+    if (ax <= 0.7853981633974483) {
+        r = x;
+        q = 0;
+        return;
+    }
+#ifdef __CUDA_ARCH__
+    const double k = rint(x * 0.6366197723675814);
+#else
+    const double k = std::nearbyint(x * 0.6366197723675814);
+#endif
+    r = ((x - k * 1.5707963267341256) - k * 6.077100506506192e-11) - k * 3.5215598651832e-27;
+    const long long ki = (long long)k;
+    q = (int)(ki & 3LL);
+}
+
+D2G_HD double m_sin(double x) {
+    const double ax = x < 0.0 ? -x : x;
+    if (!(ax < 1e9)) return x - x;
+    double r;
+    int q;
+    m_reduce(x, r, q);
+    if (q == 0) return m_kernel_sin(r);
+    if (q == 1) return m_kernel_cos(r);
+    if (q == 2) return -m_kernel_sin(r);
+    return -m_kernel_cos(r);
+}
+
+D2G_HD double m_cos(double x) {
+    const double ax = x < 0.0 ? -x : x;
+    if (!(ax < 1e9)) return x - x;
+    double r;
+    int q;
+    m_reduce(x, r, q);
+    if (q == 0) return m_kernel_cos(r);
+    if (q == 1) return -m_kernel_sin(r);
+    if (q == 2) return -m_kernel_cos(r);
+    return m_kernel_sin(r);
+}
+
+D2G_HD double m_series_asin(double y) {
+    const double z = y * y;
+    double p = 0.0017680811205154183;
+    p = 0.0018622264064031275 + z * p;
+    p = 0.0019650336162772837 + z * p;
+    p = 0.0020776610325181676 + z * p;
+    p = 0.0022014739737101384 + z * p;
+    p = 0.002338091892111975 + z * p;
+    p = 0.0024894486782468836 + z * p;
+    p = 0.00265787063820729 + z * p;
+    p = 0.002846178401108942 + z * p;
+    p = 0.0030578216492580306 + z * p;
+    p = 0.003297059503473485 + z * p;
+    p = 0.0035692053938259347 + z * p;
+    p = 0.003880964558837669 + z * p;
+    p = 0.004240907093679363 + z * p;
+    p = 0.004660143486915096 + z * p;
+    p = 0.005153309682319905 + z * p;
+    p = 0.005740037670841924 + z * p;
+    p = 0.006447210311889649 + z * p;
+    p = 0.0073125258735988454 + z * p;
+    p = 0.008390335809616815 + z * p;
+    p = 0.009761609529194078 + z * p;
+    p = 0.011551800896139705 + z * p;
+    p = 0.01396484375 + z * p;
+    p = 0.017352764423076924 + z * p;
+    p = 0.022372159090909092 + z * p;
+    p = 0.030381944444444444 + z * p;
+    p = 0.044642857142857144 + z * p;
+    p = 0.075 + z * p;
+    p = 0.16666666666666666 + z * p;
+    p = 1.0 + z * p;
+    return y * p;
+}
+
+// acos on [0, 1].
+D2G_HD double m_acos(double x) {
+    if (x <= 0.5) return 1.5707963267948966 - m_series_asin(x);
+    return 2.0 * m_series_asin(sqrt((1.0 - x) / 2.0));
+}
+
+D2G_HD double m_pow15(double x) { return x * sqrt(x); }
+
+// Host-only natural logarithm for scene generation.
+inline double m_log(double x) {
+    int e;
+    double m = std::frexp(x, &e);
+    if (m < 0.7071067811865476) {
+        m = m * 2.0;
+        e = e - 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double z = s * s;
+    double p = 1.0 / 41.0;
+    for (int n = 19; n >= 1; n--) p = 1.0 / (2.0 * n + 1.0) + z * p;
+    const double ls = 2.0 * (s + (s * z) * p);
+    return ls + (double)e * 0.6931471805599453;
+}
+
+}  // namespace d2g

@@ -1,0 +1,175 @@
+/*
+ * d2g.h — C ABI of the GB300 contact hot path (delta2_gb300).
+ *
+ * The reference (Peter-Noble/Delta2) has no C ABI: its hot path is reached
+ * through C++ virtual strategies and free functions.  Each entry point below
+ * names the reference interface it replaces (file:line within the reference
+ * project).  Conventions:
+ *   - plain pointers and sizes, no C++ or torch types;
+ *   - every call returns an int status: 0 = ok, > 0 = recoverable
+ *     (D2G_SOLVE_FAILED, D2G_CAPACITY, D2G_SPIN_LIMIT), < 0 = fatal;
+ *     d2g_last_error() gives the message of the calling thread's last error;
+ *   - "host" entry points take host buffers and copy in and out inside the
+ *     call; "_device" entry points take pointers in the GPU's memory;
+ *   - one host thread per context; all work is ordered on the context's stream.
+ *
+ * Records shared by all entry points:
+ *   body state (14 doubles): time, qw qx qy qz, L(3), x(3), v(3)
+ *   contact (14 doubles): A(3) B(3) eps_a eps_b eps_inner_a eps_inner_b toc pa pb 0
+ *     (collision_detection/contact.h:9-28 Contact and :73-83 ContinuousContact;
+ *      pa/pb are body indices stored as doubles)
+ *   tree node (4 int32): child_first (global node index, -1 for leaves),
+ *     num_children, is_inner, depth; node i owns bucket i (<= 8 triangles of
+ *     9 doubles, eps[8], inner_eps[8])  (model/surrogate_components.h:11-88)
+ */
+#ifndef D2G_H
+#define D2G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    D2G_OK = 0,
+    D2G_SOLVE_FAILED = 1, /* SequentialImpulses::solve returned false */
+    D2G_CAPACITY = 2,     /* output larger than the caller's buffer; counts still written */
+    D2G_SPIN_LIMIT = 3,   /* a bounded device wait gave up */
+    D2G_ERR_INVALID = -1,
+    D2G_ERR_CUDA = -2,
+    D2G_ERR_NO_DEVICE = -3,
+    D2G_ERR_STATE = -4
+};
+
+#define D2G_STATE_LEN 14
+#define D2G_CONTACT_LEN 14
+
+/* Surrogate trees of all meshes, concatenated (model/surrogate_tree.h:15-29). */
+typedef struct d2g_trees {
+    int32_t n_meshes;
+    const int32_t* mesh_node_off; /* [n_meshes+1] first node of each mesh */
+    const int32_t* nodes;         /* [N][4] */
+    const int32_t* ntris;         /* [N] */
+    const double* tris;           /* [N][8][9] */
+    const double* eps;            /* [N][8] */
+    const double* inner_eps;      /* [N][8] */
+} d2g_trees;
+
+/* Bodies (model/particle.h:9-64); index == reference Particle::id. */
+typedef struct d2g_bodies {
+    int32_t n;
+    const int32_t* mesh;
+    const uint8_t* is_static;
+    const double* geo_eps;
+    const double* mu;
+    const double* mass;
+    const double* inv_inertia; /* [n][9] body-frame inverse inertia, row major */
+    double* last;              /* [n][14] */
+    double* cur;               /* [n][14] */
+    double* fut;               /* [n][14] */
+    double* last_dt;           /* [n] */
+    int32_t* sleep_steps;      /* [n] */
+    uint8_t* sleeping;         /* [n] */
+    const double* bounding_radius;
+} d2g_bodies;
+
+/* ------------------------------------------------------------ errors ---- */
+const char* d2g_last_error(void);
+const char* d2g_version(void);
+
+/* --------------------------------------------------- scene set-up (host) --
+ * Synthetic scenes of the benchmark configurations and their surrogate trees
+ * (the reference builds scenes in src/runner/main.cpp:65-126 and trees in
+ * model/surrogate_tree.cpp:39-112).  No GPU is used. */
+typedef struct d2g_scene_opts {
+    int32_t config;     /* 1 cubes, 2 convex hulls, 3 mixed shapes, 5 noisy icospheres */
+    int32_t nx, ny, nz; /* grid size, 0 = the configuration's default */
+    double spacing;     /* 0 = default */
+    double speed_sigma; /* initial velocity std-dev per axis; < 0 = default */
+    uint64_t seed;
+    float dt;           /* 0 = default */
+    double gravity_z;
+    double mu;          /* 0 = default */
+    int32_t hull_points;
+} d2g_scene_opts;
+
+typedef struct d2g_scene d2g_scene;
+int d2g_scene_make(const d2g_scene_opts* opts, d2g_scene** out);
+void d2g_scene_free(d2g_scene* s);
+/* Pointers into the scene's own storage (valid until d2g_scene_free). */
+int d2g_scene_view(d2g_scene* s, d2g_trees* trees, d2g_bodies* bodies, const float** local_aabb, float* opt_dt,
+                   double* gravity_z);
+/* Build one mesh's surrogate tree from a triangle mesh, drawing from the PCG32
+ * stream (state, inc) in rng[2] (updated).  Sizes first, then a second call
+ * with buffers: nodes [n][4] (child_first local to this mesh), ntris, tris
+ * [n][72], eps [n][8], inner_eps [n][8].  Replaces SurrogateTree(V, F, opt). */
+int d2g_tree_build(const double* V, int32_t nv, const int32_t* F, int32_t nf, uint64_t* rng, int32_t* n_nodes,
+                   int32_t* nodes, int32_t* ntris, double* tris, double* eps, double* inner_eps, int32_t capacity);
+
+/* Broad phase (host): body pairs i < j, not both static, whose float bounds
+ * overlap (the mesh box through the float transform for static bodies, the
+ * bounding-sphere box at last/current/future positions for moving ones, grown
+ * by geo_eps) and whose swept bounding spheres meet within max(last_dt).
+ * Replaces broadPhaseEmbree(ParticleHandler&)
+ * (collision_detection/broad_phase_embree.cpp:87-116, 186-238, 266-289);
+ * pairs come in ascending (i, j).  pairs may be NULL to count only. */
+int d2g_broad_phase(const d2g_bodies* bodies, const float* local_aabb, int32_t* pairs, int32_t capacity,
+                    int32_t* n_pairs);
+
+/* ------------------------------------------------------------ context ---- */
+typedef struct d2g_ctx d2g_ctx;
+int d2g_ctx_create(int32_t device, d2g_ctx** out);
+void d2g_ctx_destroy(d2g_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t) for ordering caller work. */
+int d2g_ctx_stream(d2g_ctx* ctx, void** stream);
+int d2g_ctx_sync(d2g_ctx* ctx);
+/* Copy trees / bodies into HBM (replaces the reference's in-memory
+ * MeshData / ParticleHandler ownership). */
+int d2g_ctx_set_trees(d2g_ctx* ctx, const d2g_trees* trees);
+int d2g_ctx_set_bodies(d2g_ctx* ctx, const d2g_bodies* bodies);
+/* Copy the device body states (last/cur/fut, last_dt, sleep_steps, sleeping) back. */
+int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
+
+/* Instrumentation (no reference counterpart): the number of kernels this
+ * library launched on the context, and, with profiling on, CUDA-event times
+ * of the dominant kernels: kind 0 swept-box filter, 1 triangle-triangle CCD,
+ * 2 leaf-pair CCD, 3 discrete triangle distance, 4 sequential-impulse solve.
+ * Enabling (or disabling) profiling resets the totals. */
+int d2g_ctx_launches(d2g_ctx* ctx, int64_t* launches);
+int d2g_ctx_set_profiling(d2g_ctx* ctx, int32_t enable);
+int d2g_ctx_profile(d2g_ctx* ctx, int32_t kind, double* ms, int64_t* launches, int64_t* items);
+
+/* ------------------------------------------------- discrete narrow phase --
+ * compareTreesFull<double,8,8> for each body pair (a, b), using the bodies'
+ * current device future states (collision_detection/full_tree_comparison.h:
+ * 13-67 with ContactDetectionComparison, comparison_dist.h:205-240).
+ * pairs [n][2]; contacts [capacity][14]; offsets [n+1].  Contacts of pair i
+ * are contacts[offsets[i] .. offsets[i+1]) in the reference's order.
+ * counters (optional, 4 int64): node pairs, triangle pairs, leaf pairs, levels.
+ * Returns D2G_CAPACITY when the total exceeds capacity (offsets still valid). */
+int d2g_compare_trees_full(d2g_ctx* ctx, const int32_t* pairs, int32_t n_pairs, double* contacts,
+                           int32_t capacity, int32_t* offsets, int64_t* counters);
+
+/* ------------------------------------------- continuous collision detection
+ * compareTreesFullContinuous<double,8,8> for each pair over its max_time
+ * (collision_detection/full_tree_comparison.h:69-219).  Each pair first
+ * projects both bodies' futures from their current states over max_time; the
+ * device future state of a body afterwards is the projection of the LAST pair
+ * (in array order) that contains it, as the reference's sequential calls
+ * leave it.  The reference's min_time_out is not produced (its live caller,
+ * separate_clusters.cpp:494, ignores it). */
+int d2g_compare_trees_full_continuous(d2g_ctx* ctx, const int32_t* pairs, const double* max_time, int32_t n_pairs,
+                                      double* contacts, int32_t capacity, int32_t* offsets, int64_t* counters);
+/* Same with pairs and max_time already in HBM; results stay on the device:
+ * *d_contacts / *d_offsets point into context-owned buffers valid until the
+ * next call.  *n_contacts receives the total. */
+int d2g_compare_trees_full_continuous_device(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time,
+                                             int32_t n_pairs, int32_t* n_contacts, const double** d_contacts,
+                                             const int32_t** d_offsets, int64_t* counters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* D2G_H */

