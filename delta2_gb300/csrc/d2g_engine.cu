@@ -395,15 +395,19 @@ __global__ void k_iota(int n, int32_t* __restrict__ v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
 }
-__global__ void k_count_pairs(int n, const int32_t* __restrict__ rec_pair, int32_t* __restrict__ cnt) {
+__global__ void k_count_pairs(int n, int n_pairs, const int32_t* __restrict__ rec_pair, int32_t* __restrict__ cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[rec_pair[i]], 1);
+    if (i >= n) return;
+    const int p = rec_pair[i];
+    if (p >= 0 && p < n_pairs) atomicAdd(&cnt[p], 1);
 }
 __global__ void k_gather(int n, const int32_t* __restrict__ idx, const double* __restrict__ in,
                          double* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double* s = in + 14 * (size_t)idx[i];
+    const int j = idx[i];
+    if (j < 0 || j >= n) return;
+    const double* s = in + 14 * (size_t)j;
     double* d = out + 14 * (size_t)i;
 #pragma unroll
     for (int k = 0; k < 14; k++) d[k] = s[k];
@@ -514,8 +518,9 @@ int append_records(d2g_ctx* ctx, int n, const int32_t* flags, const int32_t* ite
     const int32_t* src = E.flag_off.p + n;
     RC(read_scalars(ctx, &src, 1, &tot));
     if (tot == 0) return D2G_OK;
-    RC(E.rec.ensure(14 * (size_t)(n_rec + tot)));
-    RC(E.rec_pair.ensure(n_rec + tot));
+    // records accumulate across levels and stages: grow without losing them
+    RC(E.rec.ensure_keep(14 * (size_t)(n_rec + tot), 14 * (size_t)n_rec, ctx->stream));
+    RC(E.rec_pair.ensure_keep((size_t)(n_rec + tot), (size_t)n_rec, ctx->stream));
     LAUNCH(k_emit, n, n, flags, E.flag_off.p, items, slot_shift, front, conn_off, n_conn,
                                                    d_pairs, E.res.p, res_eps, ctx->geo_eps.p, E.rec.p,
                                                    E.rec_pair.p, n_rec);
@@ -544,7 +549,7 @@ int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
         D2G_CUDA(cub::DeviceRadixSort::SortPairs(E.cub_tmp.p, bytes, E.rec_pair.p, E.rec_pair_sorted.p, E.rec_idx.p,
                                                  E.rec_idx_sorted.p, n_rec, 0, bits, ctx->stream));
         LAUNCH(k_gather, n_rec, n_rec, E.rec_idx_sorted.p, E.rec.p, E.rec_sorted.p);
-        LAUNCH(k_count_pairs, n_rec, n_rec, E.rec_pair.p, E.pair_cnt.p);
+        LAUNCH(k_count_pairs, n_rec, n_rec, n_pairs, E.rec_pair.p, E.pair_cnt.p);
     }
     RC(scan(ctx, E.pair_cnt.p, E.out_off.p, n_pairs));
     return D2G_OK;

@@ -47,6 +47,33 @@ struct DBuf {
         cap = c;
         return D2G_OK;
     }
+    // Grow to n elements keeping the first `used` ones (accumulating buffers).
+    int ensure_keep(size_t n, size_t used, cudaStream_t stream) {
+        if (n <= cap) return D2G_OK;
+        size_t c = n + n / 2 + 64;
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc((void**)&q, c * sizeof(T));
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return D2G_ERR_CUDA;
+        }
+        if (p) {
+            if (used) {
+                e = cudaMemcpyAsync(q, p, used * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) {
+                    cudaFree(q);
+                    set_error(std::string("buffer growth: ") + cudaGetErrorString(e));
+                    return D2G_ERR_CUDA;
+                }
+            }
+            cudaDeviceSynchronize();
+            cudaFree(p);
+        }
+        p = q;
+        cap = c;
+        return D2G_OK;
+    }
     void release() {
         if (p) cudaFree(p);
         p = nullptr;

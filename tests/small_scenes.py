@@ -67,7 +67,15 @@ class SmallScene:
         self.sleeping = np.zeros(n, dtype=np.uint8)
         self.bounding_radius = np.array([b["br"] for b in B], dtype=np.float64)
         self.local_aabb = np.array([b["aabb"] for b in B], dtype=np.float32)
+        self.opt_dt = 0.01
         return self
+
+    def to_product(self):
+        """The same arrays as a delta2_gb300.Scene (for the C-ABI entry points)."""
+        import delta2_gb300 as D
+        s = D.Scene()
+        s.__dict__.update({k: v for k, v in self.__dict__.items() if not k.startswith("_")})
+        return s
 
 
 def tris_from(V, F):

@@ -81,7 +81,7 @@ def test_bucket_golden_on_gpu(ctx):
     m_pl = s.add_leaf_mesh(tris_from(V, F))
     s.add_body(m_pyr, 0.01, cur=state(x=(0, 0, 1.0)), fut=state(x=(0, 0, 1.0)), is_static=True)
     s.add_body(m_pl, 0.01, cur=state(x=(0, 0, 1.105)), fut=state(x=(0, 0, 1.105)))
-    sc = s.build()
+    sc = s.build().to_product()
     ctx.set_scene(sc)
     c, off, _ = ctx.compare_trees_full([[0, 1]])
     assert off.tolist() == [0, 8]
