@@ -51,6 +51,30 @@ class Bodies(C.Structure):
                 ("last_dt", F64P), ("sleep_steps", I32P), ("sleeping", U8P), ("bounding_radius", F64P)]
 
 
+class DeviceScene(C.Structure):
+    _fields_ = [("n_meshes", C.c_int32), ("n_nodes", C.c_int32), ("mesh_node_off", C.c_void_p),
+                ("nodes", C.c_void_p), ("ntris", C.c_void_p), ("tris", C.c_void_p), ("eps", C.c_void_p),
+                ("inner_eps", C.c_void_p), ("n_bodies", C.c_int32), ("mesh", C.c_void_p), ("fut", C.c_void_p),
+                ("geo_eps", C.c_void_p)]
+
+
+NOALLOC_MAX_PAIRS = 4096
+NOALLOC_MAX_NODE_PAIRS = 2048
+NOALLOC_MAX_CONTACTS = 32768
+
+
+def compare_trees_full_noalloc(device_scene, d_pairs, n_pairs, d_contacts, capacity, d_offsets, stream=0):
+    """Allocation-free compareTreesFull over device buffers (see include/d2g.h).
+
+    ``device_scene`` is a DeviceScene of device pointers; the other pointers
+    are device addresses (ints).  Returns the number of contacts."""
+    n = C.c_int32()
+    _check(lib().d2g_compare_trees_full_noalloc(C.byref(device_scene), C.c_void_p(d_pairs), int(n_pairs),
+                                                C.c_void_p(d_contacts), int(capacity), C.c_void_p(d_offsets),
+                                                C.byref(n), C.c_void_p(stream)))
+    return n.value
+
+
 class SceneOpts(C.Structure):
     _fields_ = [("config", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("spacing", C.c_double), ("speed_sigma", C.c_double), ("seed", C.c_uint64), ("dt", C.c_float),

@@ -19,6 +19,9 @@
 // d2g_geom.cuh, so results equal the CPU restatement bit for bit.
 #include <cub/cub.cuh>
 
+#include <mutex>
+#include <string>
+
 #include "d2g_geom.cuh"
 #include "d2g_internal.hpp"
 
@@ -729,3 +732,251 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
 }
 
 }  // namespace d2g
+
+// ============================================================================
+// Allocation-free discrete narrow phase.
+//
+// For callers that may not allocate device memory while they run: code inside
+// a CUDA-graph capture (cudaMalloc is not capturable), a host that hands this
+// library a fixed memory budget up front (game or robotics loops with
+// real-time limits, where an allocation can stall or fail mid-frame), or an
+// embedding runtime that owns every allocation itself.  Every intermediate
+// buffer of the traversal is carved out of the file-scope array below, which
+// each GPU that loads this library holds until the process exits.
+//
+// Limits (checked before any work; larger requests are rejected with
+// D2G_ERR_INVALID and a message):
+//   body pairs per call          <= D2G_NOALLOC_MAX_PAIRS      (4096)
+//   node pairs per tree level    <= D2G_NOALLOC_MAX_NODE_PAIRS (2048)
+//   contacts found per call      <= D2G_NOALLOC_MAX_CONTACTS   (32768)
+// All calls share the array and it keeps the previous call's contents: the
+// counters that must start at zero are cleared on every call, and two calls
+// whose work overlaps on the GPU (different streams, or different threads)
+// race on it.  The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) and caches it; make that first call before any stream
+// capture.
+// ============================================================================
+namespace d2g {
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)24 << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array on the current device.
+int noalloc_base(void** out) {
+    int dev = 0;
+    D2G_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device index beyond the allocation-free path's table");
+        return D2G_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+            return D2G_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return D2G_OK;
+}
+
+// Bump carve-out of 256-byte aligned pieces.
+struct Carve {
+    unsigned char* base;
+    size_t used, cap;
+    template <class T>
+    T* take(size_t n) {
+        const size_t off = (used + 255) & ~(size_t)255;
+        const size_t bytes = n * sizeof(T);
+        if (off + bytes > cap) return nullptr;
+        used = off + bytes;
+        return (T*)(base + off);
+    }
+};
+
+// Index checks of the caller's device inputs: pair body ids, their mesh ids,
+// node links and bucket sizes.  Sets *err to 1 on any violation.
+__global__ void k_noalloc_validate(int n_pairs, const int32_t* __restrict__ pairs, int n_bodies,
+                                   const int32_t* __restrict__ mesh, int n_meshes,
+                                   const int32_t* __restrict__ mesh_node_off, int n_nodes,
+                                   const int4* __restrict__ nodes, const int32_t* __restrict__ ntris,
+                                   int32_t* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_meshes && (mesh_node_off[i] < 0 || mesh_node_off[i] >= n_nodes)) atomicExch(err, 1);
+    if (i < n_pairs) {
+        const int a = pairs[2 * i], b = pairs[2 * i + 1];
+        if (a < 0 || a >= n_bodies || b < 0 || b >= n_bodies)
+            atomicExch(err, 1);
+        else if (mesh[a] < 0 || mesh[a] >= n_meshes || mesh[b] < 0 || mesh[b] >= n_meshes)
+            atomicExch(err, 1);
+    }
+    if (i < n_nodes) {
+        const int4 nd = nodes[i];
+        if (ntris[i] < 0 || ntris[i] > 8 || nd.y < 0 || nd.y > 8 || (nd.z && (nd.x < 0 || nd.x + nd.y > n_nodes)))
+            atomicExch(err, 1);
+    }
+}
+
+int noalloc_read(cudaStream_t s, const int32_t* src, int32_t* dst) {
+    D2G_CUDA(cudaMemcpyAsync(dst, src, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaStreamSynchronize(s));
+    return D2G_OK;
+}
+
+int noalloc_scan(cudaStream_t s, void* tmp, size_t tmp_bytes, const int32_t* in, int32_t* out, int n) {
+    D2G_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
+    if (n == 0) return D2G_OK;
+    size_t need = 0;
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, need, in, out + 1, n, s));
+    if (need > tmp_bytes) {
+        set_error("allocation-free scratch: prefix-sum temporary storage too small");
+        return D2G_ERR_INVALID;
+    }
+    size_t avail = tmp_bytes;
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(tmp, avail, in, out + 1, n, s));
+    return D2G_OK;
+}
+
+#define NA_LAUNCH(kern, n, ...) kern<<<nblocks(n), kBlock, 0, s>>>(__VA_ARGS__)
+
+}  // namespace
+}  // namespace d2g
+
+extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const int32_t* d_pairs, int32_t n_pairs,
+                                              double* d_contacts, int32_t capacity, int32_t* d_offsets,
+                                              int32_t* n_contacts, void* stream) {
+    using namespace d2g;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!sc || !d_offsets || !n_contacts || n_pairs < 0 || (n_pairs > 0 && !d_pairs) || capacity < 0 ||
+        (capacity > 0 && !d_contacts) || sc->n_meshes <= 0 || sc->n_bodies <= 0 || !sc->mesh_node_off ||
+        !sc->nodes || !sc->ntris || !sc->tris || !sc->eps || !sc->inner_eps || !sc->mesh || !sc->fut ||
+        !sc->geo_eps || sc->n_nodes <= 0) {
+        set_error("invalid allocation-free narrow-phase arguments");
+        return D2G_ERR_INVALID;
+    }
+    if (n_pairs > D2G_NOALLOC_MAX_PAIRS) {
+        set_error("allocation-free narrow phase: " + std::to_string(n_pairs) + " pairs exceed the limit of " +
+                  std::to_string(D2G_NOALLOC_MAX_PAIRS));
+        return D2G_ERR_INVALID;
+    }
+    void* base = nullptr;
+    if (int rc = noalloc_base(&base)) return rc;
+    const int MP = D2G_NOALLOC_MAX_PAIRS, MN = D2G_NOALLOC_MAX_NODE_PAIRS, MR = D2G_NOALLOC_MAX_CONTACTS;
+    Carve cv{(unsigned char*)base, 0, kNoAllocBytes};
+    double* pm = cv.take<double>(32 * (size_t)MP);
+    float* search = cv.take<float>(MP);
+    Entry* front = cv.take<Entry>(MN);
+    Entry* next = cv.take<Entry>(MN);
+    int32_t* entry_hits = cv.take<int32_t>(MN);
+    int32_t* cnt_a = cv.take<int32_t>(MN);
+    int32_t* cnt_b = cv.take<int32_t>(MN);
+    int32_t* off_a = cv.take<int32_t>(MN + 1);
+    int32_t* off_b = cv.take<int32_t>(MN + 1);
+    PrimResult* res = cv.take<PrimResult>(64 * (size_t)MN);
+    double* res_eps = cv.take<double>(4 * 64 * (size_t)MN);
+    int32_t* hit = cv.take<int32_t>(64 * (size_t)MN);
+    int32_t* flags = cv.take<int32_t>(64 * (size_t)MN);
+    int32_t* flag_off = cv.take<int32_t>(64 * (size_t)MN + 1);
+    double* rec = cv.take<double>(14 * (size_t)MR);
+    int32_t* rec_pair = cv.take<int32_t>(MR);
+    int32_t* rec_pair_sorted = cv.take<int32_t>(MR);
+    int32_t* rec_idx = cv.take<int32_t>(MR);
+    int32_t* rec_idx_sorted = cv.take<int32_t>(MR);
+    int32_t* pair_cnt = cv.take<int32_t>(MP + 1);
+    int32_t* err = cv.take<int32_t>(1);
+    const size_t tmp_bytes = kNoAllocBytes - ((cv.used + 255) & ~(size_t)255) - 256;
+    void* tmp = cv.take<unsigned char>(tmp_bytes);
+    if (!tmp || !err) {
+        set_error("allocation-free scratch layout does not fit");
+        return D2G_ERR_INVALID;
+    }
+    const int4* nodes = (const int4*)sc->nodes;
+    int32_t h_err = 0;
+    D2G_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
+    int nv = n_pairs > sc->n_nodes ? n_pairs : sc->n_nodes;
+    nv = nv > sc->n_meshes ? nv : sc->n_meshes;
+    NA_LAUNCH(k_noalloc_validate, nv, n_pairs, d_pairs, sc->n_bodies, sc->mesh, sc->n_meshes, sc->mesh_node_off,
+              sc->n_nodes, nodes, sc->ntris, err);
+    if (int rc = noalloc_read(s, err, &h_err)) return rc;
+    if (h_err) {
+        set_error("allocation-free narrow phase: a body, mesh or node index is out of range");
+        return D2G_ERR_INVALID;
+    }
+    if (n_pairs > 0)
+        NA_LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, sc->fut, sc->mesh, sc->mesh_node_off, sc->geo_eps, pm, search,
+                  front);
+    int n = n_pairs, n_rec = 0, level = 0;
+    while (n > 0) {
+        if (n > MN) {
+            set_error("allocation-free narrow phase: " + std::to_string(n) + " node pairs at level " +
+                      std::to_string(level) + " exceed the limit of " + std::to_string(MN));
+            return D2G_ERR_INVALID;
+        }
+        const int n_slots = 64 * n;
+        D2G_CUDA(cudaMemsetAsync(entry_hits, 0, sizeof(int32_t) * n, s));
+        NA_LAUNCH(k_np, n_slots, n_slots, front, d_pairs, pm, sc->ntris, sc->tris, sc->eps, sc->inner_eps,
+                  sc->geo_eps, search, res, res_eps, hit, entry_hits);
+        NA_LAUNCH(k_final_flags, n_slots, n_slots, nullptr, front, nodes, hit, flags);
+        if (int rc = noalloc_scan(s, tmp, tmp_bytes, flags, flag_off, n_slots)) return rc;
+        int32_t tot = 0;
+        if (int rc = noalloc_read(s, flag_off + n_slots, &tot)) return rc;
+        if (n_rec + tot > MR) {
+            set_error("allocation-free narrow phase: contacts exceed the limit of " + std::to_string(MR));
+            return D2G_ERR_INVALID;
+        }
+        if (tot > 0)
+            NA_LAUNCH(k_emit, n_slots, n_slots, flags, flag_off, nullptr, 6, front, nullptr, 0, d_pairs, res, res_eps,
+                      sc->geo_eps, rec, rec_pair, n_rec);
+        n_rec += tot;
+        NA_LAUNCH(k_expand_count, n, n, front, entry_hits, nodes, 0, cnt_a, cnt_b);
+        if (int rc = noalloc_scan(s, tmp, tmp_bytes, cnt_a, off_a, n)) return rc;
+        D2G_CUDA(cudaMemsetAsync(off_b, 0, sizeof(int32_t) * (n + 1), s));
+        int32_t nn = 0;
+        if (int rc = noalloc_read(s, off_a + n, &nn)) return rc;
+        if (nn > MN) {
+            set_error("allocation-free narrow phase: " + std::to_string(nn) + " node pairs at level " +
+                      std::to_string(level + 1) + " exceed the limit of " + std::to_string(MN));
+            return D2G_ERR_INVALID;
+        }
+        NA_LAUNCH(k_expand_write, n, n, front, entry_hits, nodes, 0, off_a, off_b, next, next);
+        Entry* t = front;
+        front = next;
+        next = t;
+        n = nn;
+        level++;
+    }
+    D2G_CUDA(cudaMemsetAsync(pair_cnt, 0, sizeof(int32_t) * (n_pairs + 1), s));
+    if (n_rec > 0) {
+        NA_LAUNCH(k_iota, n_rec, n_rec, rec_idx);
+        int bits = 1;
+        while ((1 << bits) < n_pairs + 1 && bits < 31) bits++;
+        size_t need = 0;
+        D2G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, need, rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted,
+                                                 n_rec, 0, bits, s));
+        if (need > tmp_bytes) {
+            set_error("allocation-free scratch: sort temporary storage too small");
+            return D2G_ERR_INVALID;
+        }
+        size_t avail = tmp_bytes;
+        D2G_CUDA(cub::DeviceRadixSort::SortPairs(tmp, avail, rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted,
+                                                 n_rec, 0, bits, s));
+        if (n_rec <= capacity) NA_LAUNCH(k_gather, n_rec, n_rec, rec_idx_sorted, rec, d_contacts);
+        NA_LAUNCH(k_count_pairs, n_rec, n_rec, n_pairs, rec_pair, pair_cnt);
+    }
+    if (int rc = noalloc_scan(s, tmp, tmp_bytes, pair_cnt, d_offsets, n_pairs)) return rc;
+    D2G_CUDA(cudaGetLastError());
+    D2G_CUDA(cudaStreamSynchronize(s));
+    *n_contacts = n_rec;
+    if (n_rec > capacity) {
+        set_error("contact capacity " + std::to_string(capacity) + " < " + std::to_string(n_rec));
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
+}

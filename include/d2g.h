@@ -168,6 +168,45 @@ int d2g_compare_trees_full_continuous_device(d2g_ctx* ctx, const int32_t* d_pair
                                              int32_t n_pairs, int32_t* n_contacts, const double** d_contacts,
                                              const int32_t** d_offsets, int64_t* counters);
 
+/* ------------------------------------ allocation-free discrete narrow phase
+ * No counterpart in the reference.  The same compareTreesFull traversal and
+ * contacts as d2g_compare_trees_full, for callers that may not allocate
+ * device memory during the call: code that runs inside a CUDA-graph capture,
+ * hosts with a fixed up-front memory budget (real-time game or robotics loops
+ * where an allocation can stall or fail mid-frame), or embedding runtimes that
+ * own every allocation.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine and needs no context: the caller passes the scene, pairs and output
+ * buffers in device memory, and a stream.  Intermediate buffers live in one
+ * file-scope device array of 24 MiB that every GPU loading this library holds
+ * until the process exits.  Limits per call (larger requests fail with
+ * D2G_ERR_INVALID before or during the traversal): */
+#define D2G_NOALLOC_MAX_PAIRS 4096       /* body pairs */
+#define D2G_NOALLOC_MAX_NODE_PAIRS 2048  /* node pairs in one tree level */
+#define D2G_NOALLOC_MAX_CONTACTS 32768   /* contacts found */
+/* All calls share that array: counters are cleared on every call, and calls
+ * whose GPU work overlaps (other streams or threads) race on it.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) and
+ * caches it: make that first call before any stream capture.  Returns
+ * D2G_CAPACITY when the contacts exceed `capacity` (offsets and *n_contacts
+ * are still written; contacts are not). */
+typedef struct d2g_device_scene {
+    int32_t n_meshes;
+    int32_t n_nodes;
+    const int32_t* mesh_node_off; /* device pointers, layout as d2g_trees / d2g_bodies */
+    const int32_t* nodes;
+    const int32_t* ntris;
+    const double* tris;
+    const double* eps;
+    const double* inner_eps;
+    int32_t n_bodies;
+    const int32_t* mesh;
+    const double* fut; /* [n_bodies][14] future states used as the poses */
+    const double* geo_eps;
+} d2g_device_scene;
+int d2g_compare_trees_full_noalloc(const d2g_device_scene* scene, const int32_t* d_pairs, int32_t n_pairs,
+                                   double* d_contacts, int32_t capacity, int32_t* d_offsets, int32_t* n_contacts,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif
