@@ -157,13 +157,14 @@ def cpu_baseline(scene, pairs, mt, budget_s):
     n = len(pairs)
     order = np.concatenate([np.arange(k, n, 16) for k in range(16)])
     done, t0 = 0, time.perf_counter()
-    while done < n and time.perf_counter() - t0 < budget_s:
-        idx = order[done:done + 64]
+    while time.perf_counter() - t0 < budget_s:  # whole passes over the step, chunked in a strided order
+        idx = order[(done % n):(done % n) + 64]
         O.ccd(scene.copy(), pairs[idx], mt[idx])
         done += len(idx)
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{done} of the {n} pair-queries of one step (strided), {dt:.1f} s, CPU oracle -O2"}
+            "sample": f"{done} pair-queries ({done / n:.1f} passes over the {n} of one step, strided chunks), "
+                      f"{dt:.1f} s single-threaded, CPU oracle g++ -O2"}
 
 
 # ------------------------------------------------------------------ ours ---
@@ -245,7 +246,7 @@ def run_ours(args):
         return
 
     peak, peak_kind = measured_peaks()
-    kinds = {D.PROF_SOUP_CCD: "tri_tri_ccd", D.PROF_CONN: "leaf_pair_ccd", D.PROF_SOUP_FILTER: "swept_box_filter"}
+    kinds = {D.PROF_SOUP_CCD: "point_tri_ccd", D.PROF_CONN: "edge_edge_ccd", D.PROF_SOUP_FILTER: "swept_box_filter"}
     dom = max((D.PROF_SOUP_CCD, D.PROF_CONN), key=lambda k: prof[k][0])
     ms, nl, items = prof[dom]
     achieved = (items * BYTES_PER_TEST) / (ms / 1e3) / 1e9 if ms > 0 else 0.0

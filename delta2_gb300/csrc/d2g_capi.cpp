@@ -266,6 +266,13 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     E.items.release();
     E.res.release();
     E.hit.release();
+    E.sub.release();
+    E.cres.release();
+    E.chit.release();
+    E.cflag_off.release();
+    E.nn_cnt.release();
+    E.nn_off.release();
+    E.citem_off.release();
     E.pm.release();
     E.pfut.release();
     E.search.release();

@@ -215,6 +215,191 @@ __global__ void __launch_bounds__(kBlock) k_conn(int n_items, int n_entries, con
     hit[k] = r.dist < (double)search[e.pair] ? 1 : 0;
 }
 
+// ------------------------------------------- flattened primitive tests -----
+// One level of the CCD as two homogeneous work lists: every point-triangle
+// test and every edge-edge test of the level, from the soup stage (the 15
+// sub-tests of each surviving triangle pair, continuous_comparison.h:692-777)
+// and from the connected stage (all tests of each leaf pair, :855-907).
+// Point-triangle list: 6 per soup triangle pair, then 6*na*nb per leaf pair;
+// edge-edge list: 9 per soup triangle pair, then 9*na*nb per leaf pair.  The
+// soup sub-results are folded afterwards in the reference's order.
+constexpr int kPrimBlock = 64;
+
+__global__ void k_conn_nn(int n, const Entry* __restrict__ conn, const int32_t* __restrict__ ntris,
+                          int32_t* __restrict__ cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Entry e = conn[i];
+    cnt[i] = ntris[e.na] * ntris[e.nb];
+}
+
+__global__ void k_scale(int n, const int32_t* __restrict__ in, int32_t m, int32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = m * in[i];
+}
+
+// Last entry e with m*off[e] <= k (off[0] == 0).
+__device__ __forceinline__ int find_entry(const int32_t* __restrict__ off, int n_entries, int m, int k) {
+    int lo = 0, hi = n_entries;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (m * off[mid] <= k)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void store_prim(PrimResult* __restrict__ r, double dist, V3 A, V3 B, double toc) {
+    r->dist = dist;
+    r->P[0] = A.x;
+    r->P[1] = A.y;
+    r->P[2] = A.z;
+    r->Q[0] = B.x;
+    r->Q[1] = B.y;
+    r->Q[2] = B.z;
+    r->toc = toc;
+}
+
+__global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, const int32_t* __restrict__ items,
+                                                        const Entry* __restrict__ soup, const Entry* __restrict__ conn,
+                                                        const int32_t* __restrict__ nn_off, int n_conn,
+                                                        const double* __restrict__ pm,
+                                                        const int32_t* __restrict__ ntris,
+                                                        const double* __restrict__ tris,
+                                                        const float* __restrict__ search,
+                                                        PrimResult* __restrict__ sub, PrimResult* __restrict__ cres,
+                                                        int32_t* __restrict__ chit) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_total) return;
+    if (j < 6 * n_tp) {
+        const int k = j / 6, w = j % 6;
+        const int slot = items[k];
+        const Entry e = soup[slot >> 6];
+        const double* M = pm + (size_t)PM_SIZE * e.pair;
+        const Tri ta = load_tri(tris + (size_t)e.na * 72 + ((slot >> 3) & 7) * 9);
+        const Tri tb = load_tri(tris + (size_t)e.nb * 72 + (slot & 7) * 9);
+        const int i = w >> 1;
+        const Ccd r = (w & 1) ? point_tri_ccd(tvert(tb, i), M + PM_BAS, M + PM_BAE, ta, M + PM_AS, M + PM_AE)
+                              : point_tri_ccd(tvert(ta, i), M + PM_ABS, M + PM_ABE, tb, M + PM_BS, M + PM_BE);
+        store_prim(sub + 15 * (size_t)k + 5 * i + (w & 1), r.dist, r.P, r.Q, r.toc);
+        return;
+    }
+    const int jp = j - 6 * n_tp;
+    const int ei = find_entry(nn_off, n_conn, 6, jp);
+    const Entry e = conn[ei];
+    const int l = jp - 6 * nn_off[ei];
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    const double* M = pm + (size_t)PM_SIZE * e.pair;
+    const double* pa = tris + (size_t)e.na * 72;
+    const double* pb = tris + (size_t)e.nb * 72;
+    const int n1 = 3 * na * nb;
+    Ccd r;
+    V3 A, B;
+    if (l < n1) {
+        const int vi = l / nb, jj = l % nb;
+        r = point_tri_ccd(tvert(load_tri(pa + (vi / 3) * 9), vi % 3), M + PM_ABS, M + PM_ABE, load_tri(pb + jj * 9),
+                          M + PM_BS, M + PM_BE);
+        A = r.P;
+        B = r.Q;
+    } else {
+        const int m = l - n1;
+        const int vi = m / na, jj = m % na;
+        r = point_tri_ccd(tvert(load_tri(pb + (vi / 3) * 9), vi % 3), M + PM_BAS, M + PM_BAE, load_tri(pa + jj * 9),
+                          M + PM_AS, M + PM_AE);
+        A = r.Q;
+        B = r.P;
+    }
+    const size_t item = 15 * (size_t)nn_off[ei] + l;
+    store_prim(cres + item, r.dist, A, B, r.toc);
+    chit[item] = r.dist < (double)search[e.pair] ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(kPrimBlock) k_prim_ee(int n_tp, int n_total, const int32_t* __restrict__ items,
+                                                        const Entry* __restrict__ soup, const Entry* __restrict__ conn,
+                                                        const int32_t* __restrict__ nn_off, int n_conn,
+                                                        const double* __restrict__ pm,
+                                                        const int32_t* __restrict__ ntris,
+                                                        const double* __restrict__ tris,
+                                                        const float* __restrict__ search,
+                                                        PrimResult* __restrict__ sub, PrimResult* __restrict__ cres,
+                                                        int32_t* __restrict__ chit) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_total) return;
+    Entry e;
+    int aTri, aEdge, bTri, bEdge;
+    size_t item = 0;
+    int k = -1, s = 0;
+    if (j < 9 * n_tp) {
+        k = j / 9;
+        const int w = j % 9;
+        const int slot = items[k];
+        e = soup[slot >> 6];
+        aTri = (slot >> 3) & 7;
+        bTri = slot & 7;
+        aEdge = w / 3;
+        bEdge = w % 3;
+        s = 5 * aEdge + 2 + bEdge;
+    } else {
+        const int jp = j - 9 * n_tp;
+        const int ei = find_entry(nn_off, n_conn, 9, jp);
+        e = conn[ei];
+        const int m = jp - 9 * nn_off[ei];
+        const int na = ntris[e.na], nb = ntris[e.nb];
+        const int ea = m / (3 * nb), eb = m % (3 * nb);
+        aTri = ea / 3;
+        aEdge = ea % 3;
+        bTri = eb / 3;
+        bEdge = eb % 3;
+        item = 15 * (size_t)nn_off[ei] + 6 * (size_t)na * nb + m;
+    }
+    const double* M = pm + (size_t)PM_SIZE * e.pair;
+    const Edge ea = tedge(load_tri(tris + (size_t)e.na * 72 + aTri * 9), aEdge);
+    const Edge eb = tedge(load_tri(tris + (size_t)e.nb * 72 + bTri * 9), bEdge);
+    Edge aS, aE, bS, bE;
+    aS.A = xform_rigid(ea.A, M + PM_AS);
+    aS.B = xform_rigid(ea.B, M + PM_AS);
+    aE.A = xform_rigid(ea.A, M + PM_AE);
+    aE.B = xform_rigid(ea.B, M + PM_AE);
+    bS.A = xform_rigid(eb.A, M + PM_BS);
+    bS.B = xform_rigid(eb.B, M + PM_BS);
+    bE.A = xform_rigid(eb.A, M + PM_BE);
+    bE.B = xform_rigid(eb.B, M + PM_BE);
+    const Ccd r = edge_edge_ccd(aS, aE, bS, bE);
+    if (k >= 0) {
+        store_prim(sub + 15 * (size_t)k + s, r.dist, r.P, r.Q, r.toc);
+    } else {
+        store_prim(cres + item, r.dist, r.Q, r.P, r.toc);
+        chit[item] = r.dist < (double)search[e.pair] ? 1 : 0;
+    }
+}
+
+// triTriCCDLinear's sequential (dist, toc) selection over its 15 sub-tests
+// (continuous_comparison.h:682-778), then the soup hit test (:817).
+__global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entry* __restrict__ soup,
+                            const PrimResult* __restrict__ sub, const float* __restrict__ search,
+                            PrimResult* __restrict__ res, int32_t* __restrict__ hit,
+                            int32_t* __restrict__ entry_hits) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    PrimResult best;
+    best.dist = 1.0 / 0.0;
+    best.P[0] = best.P[1] = best.P[2] = 0.0;
+    best.Q[0] = best.Q[1] = best.Q[2] = 0.0;
+    best.toc = 1.0;
+    for (int s = 0; s < 15; s++) {
+        const PrimResult c = sub[15 * (size_t)k + s];
+        if (c.dist < best.dist || (c.dist == best.dist && c.toc < best.toc)) best = c;
+    }
+    res[k] = best;
+    const int slot = items[k];
+    const Entry e = soup[slot >> 6];
+    const int h = best.dist < (double)search[e.pair] ? 1 : 0;
+    hit[k] = h;
+    if (h) atomicAdd(&entry_hits[slot >> 6], 1);
+}
+
 // ----------------------------------------------------------- discrete -----
 // All 64 slots of a node pair: triangle distance at the future poses and the
 // hit test dist < float(search) + eps_a + eps_b (comparison_dist.h:223-236).
@@ -560,6 +745,22 @@ int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
 
 }  // namespace
 
+// Launch with an explicit block size.
+#define LAUNCHB(kern, n, block, ...)                                                  \
+    do {                                                                              \
+        kern<<<nblocks(n, block), block, 0, ctx->stream>>>(__VA_ARGS__);              \
+        ctx->eng.launches++;                                                          \
+    } while (0)
+
+// Append flagged results (already scanned into `off`) as contact records at `base`.
+void emit_records(d2g_ctx* ctx, int n, const int32_t* flags, const int32_t* off, const int32_t* items, int shift,
+                  const Entry* front, const int32_t* conn_off, int n_conn, const int32_t* d_pairs,
+                  const PrimResult* res, int base) {
+    Engine& E = ctx->eng;
+    LAUNCH(k_emit, n, n, flags, off, items, shift, front, conn_off, n_conn, d_pairs, res, nullptr, ctx->geo_eps.p,
+           E.rec.p, E.rec_pair.p, base);
+}
+
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters) {
     Engine& E = ctx->eng;
@@ -571,87 +772,97 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     RC(E.soup.ensure(n_pairs + 1));
     int n_rec = 0;
     if (n_pairs > 0)
-        LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p,
-                                                      ctx->mesh.p, ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p,
-                                                      E.pfut.p, E.search.p, E.soup.p);
+        LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
+               ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
     int n_soup = n_pairs, n_conn = 0;
     while (n_soup > 0 || n_conn > 0) {
         c_levels++;
         c_node += n_soup + n_conn;
         c_leaf += n_conn;
+        // (1) soup swept-box filter and leaf-pair sizes, one synchronisation
+        const int n_slots = 64 * n_soup;
+        RC(E.flags.ensure(n_slots + 1));
+        RC(E.flag_off.ensure(n_slots + 1));
+        RC(E.entry_hits.ensure(n_soup + 1));
+        RC(E.nn_cnt.ensure(n_conn + 1));
+        RC(E.nn_off.ensure(n_conn + 1));
+        RC(E.citem_off.ensure(n_conn + 1));
         if (n_soup > 0) {
-            const int n_slots = 64 * n_soup;
-            RC(E.flags.ensure(n_slots));
-            RC(E.flag_off.ensure(n_slots + 1));
-            RC(E.entry_hits.ensure(n_soup));
             D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
             const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
-            LAUNCH(k_soup_filter, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p,
-                                                              ctx->tris.p, ctx->geo_eps.p, E.flags.p);
+            LAUNCH(k_soup_filter, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
+                   ctx->geo_eps.p, E.flags.p);
             prof_end(ctx, pff);
-            RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
-            int32_t n_items;
-            const int32_t* src = E.flag_off.p + n_slots;
-            RC(read_scalars(ctx, &src, 1, &n_items));
-            c_tri += n_items;
-            if (n_items > 0) {
-                RC(E.items.ensure(n_items));
-                RC(E.res.ensure(n_items));
-                RC(E.hit.ensure(n_items));
-                LAUNCH(k_compact, n_slots, n_slots, E.flags.p, E.flag_off.p, E.items.p);
-                const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_items);
-                LAUNCH(k_soup_ccd, n_items, n_items, E.items.p, E.soup.p, E.pm.p, ctx->tris.p,
-                                                               E.search.p, E.res.p, E.hit.p, E.entry_hits.p);
-                prof_end(ctx, pf);
-                // contacts of leaf-leaf soup node pairs are final (full_tree_comparison.h:104-105)
-                RC(E.flags.ensure(n_items));
-                LAUNCH(k_final_flags, n_items, n_items, E.items.p, E.soup.p, ctx->nodes.p,
-                                                                  E.hit.p, E.flags.p);
-                RC(append_records(ctx, n_items, E.flags.p, E.items.p, 6, E.soup.p, nullptr, 0, d_pairs, nullptr,
-                                  n_rec));
-            }
         }
-        if (n_conn > 0) {
-            RC(E.cnt_b.ensure(n_conn));
-            RC(E.off_b.ensure(n_conn + 1));
-            LAUNCH(k_conn_count, n_conn, n_conn, E.conn.p, ctx->ntris.p, E.cnt_b.p);
-            RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_conn));
-            int32_t n_items;
-            const int32_t* src = E.off_b.p + n_conn;
-            RC(read_scalars(ctx, &src, 1, &n_items));
-            c_tri += n_items;
-            if (n_items > 0) {
-                RC(E.res.ensure(n_items));
-                RC(E.hit.ensure(n_items));
-                const int pf = prof_begin(ctx, PROF_CONN, n_items);
-                LAUNCH(k_conn, n_items, n_items, n_conn, E.off_b.p, E.conn.p, E.pm.p, ctx->ntris.p,
-                                                           ctx->tris.p, E.search.p, E.res.p, E.hit.p);
-                prof_end(ctx, pf);
-                RC(append_records(ctx, n_items, E.hit.p, nullptr, 0, E.conn.p, E.off_b.p, n_conn, d_pairs, nullptr,
-                                  n_rec));
-            }
+        RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
+        if (n_conn > 0) LAUNCH(k_conn_nn, n_conn, n_conn, E.conn.p, ctx->ntris.p, E.nn_cnt.p);
+        RC(scan(ctx, E.nn_cnt.p, E.nn_off.p, n_conn));
+        int32_t tot1[2];
+        const int32_t* src1[2] = {E.flag_off.p + n_slots, E.nn_off.p + n_conn};
+        RC(read_scalars(ctx, src1, 2, tot1));
+        const int K = tot1[0], P = tot1[1];  // soup triangle pairs, leaf-pair triangle pairs
+        c_tri += (int64_t)K + 15 * (int64_t)P;
+        // (2) all primitive tests of the level
+        RC(E.items.ensure(K + 1));
+        RC(E.sub.ensure(15 * (size_t)K + 1));
+        RC(E.res.ensure(K + 1));
+        RC(E.hit.ensure(K + 1));
+        RC(E.cres.ensure(15 * (size_t)P + 1));
+        RC(E.chit.ensure(15 * (size_t)P + 1));
+        RC(E.cflag_off.ensure(15 * (size_t)P + 1));
+        if (n_soup > 0) LAUNCH(k_compact, n_slots, n_slots, E.flags.p, E.flag_off.p, E.items.p);
+        const int n_pt = 6 * K + 6 * P, n_ee = 9 * K + 9 * P;
+        if (n_pt > 0) {
+            const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_pt);
+            LAUNCHB(k_prim_pt, n_pt, kPrimBlock, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
+                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p);
+            prof_end(ctx, pf);
         }
-        int32_t tot[2] = {0, 0};
-        if (n_soup > 0) {
-            RC(E.cnt_a.ensure(n_soup));
-            RC(E.cnt_b.ensure(n_soup));
-            RC(E.off_a.ensure(n_soup + 1));
-            RC(E.off_b.ensure(n_soup + 1));
-            LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1,
-                                                              E.cnt_a.p, E.cnt_b.p);
-            RC(scan(ctx, E.cnt_a.p, E.off_a.p, n_soup));
-            RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_soup));
-            const int32_t* src[2] = {E.off_a.p + n_soup, E.off_b.p + n_soup};
-            RC(read_scalars(ctx, src, 2, tot));
-            RC(E.soup_next.ensure(tot[0] + 1));
-            RC(E.conn_next.ensure(tot[1] + 1));
-            LAUNCH(k_expand_write, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1,
-                                                              E.off_a.p, E.off_b.p, E.soup_next.p, E.conn_next.p);
+        if (n_ee > 0) {
+            const int pf = prof_begin(ctx, PROF_CONN, n_ee);
+            LAUNCHB(k_prim_ee, n_ee, kPrimBlock, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
+                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p);
+            prof_end(ctx, pf);
         }
+        // (3) soup fold and finals, leaf-pair finals, expansion; one synchronisation
+        if (K > 0) {
+            LAUNCH(k_soup_fold, K, K, E.items.p, E.soup.p, E.sub.p, E.search.p, E.res.p, E.hit.p, E.entry_hits.p);
+            LAUNCH(k_final_flags, K, K, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p, E.flags.p);
+        }
+        RC(scan(ctx, E.flags.p, E.flag_off.p, K));
+        RC(scan(ctx, E.chit.p, E.cflag_off.p, 15 * P));
+        RC(E.cnt_a.ensure(n_soup + 1));
+        RC(E.cnt_b.ensure(n_soup + 1));
+        RC(E.off_a.ensure(n_soup + 1));
+        RC(E.off_b.ensure(n_soup + 1));
+        if (n_soup > 0)
+            LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1, E.cnt_a.p, E.cnt_b.p);
+        RC(scan(ctx, E.cnt_a.p, E.off_a.p, n_soup));
+        RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_soup));
+        int32_t tot2[4];
+        const int32_t* src2[4] = {E.flag_off.p + K, E.cflag_off.p + 15 * P, E.off_a.p + n_soup, E.off_b.p + n_soup};
+        RC(read_scalars(ctx, src2, 4, tot2));
+        const int fin_soup = tot2[0], fin_conn = tot2[1];
+        RC(E.rec.ensure_keep(14 * (size_t)(n_rec + fin_soup + fin_conn + 1), 14 * (size_t)n_rec, s));
+        RC(E.rec_pair.ensure_keep((size_t)(n_rec + fin_soup + fin_conn + 1), (size_t)n_rec, s));
+        if (fin_soup > 0)
+            emit_records(ctx, K, E.flags.p, E.flag_off.p, E.items.p, 6, E.soup.p, nullptr, 0, d_pairs, E.res.p, n_rec);
+        n_rec += fin_soup;
+        if (fin_conn > 0) {
+            LAUNCH(k_scale, n_conn + 1, n_conn + 1, E.nn_off.p, 15, E.citem_off.p);
+            emit_records(ctx, 15 * P, E.chit.p, E.cflag_off.p, nullptr, 0, E.conn.p, E.citem_off.p, n_conn, d_pairs,
+                         E.cres.p, n_rec);
+        }
+        n_rec += fin_conn;
+        RC(E.soup_next.ensure(tot2[2] + 1));
+        RC(E.conn_next.ensure(tot2[3] + 1));
+        if (n_soup > 0)
+            LAUNCH(k_expand_write, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1, E.off_a.p, E.off_b.p,
+                   E.soup_next.p, E.conn_next.p);
         std::swap(E.soup, E.soup_next);
         std::swap(E.conn, E.conn_next);
-        n_soup = tot[0];
-        n_conn = tot[1];
+        n_soup = tot2[2];
+        n_conn = tot2[3];
     }
     RC(finish_records(ctx, n_pairs, n_rec));
     if (n_pairs > 0) {

@@ -101,6 +101,10 @@ struct Engine {
     DBuf<int32_t> flags, flag_off, items;
     DBuf<PrimResult> res;
     DBuf<int32_t> hit;
+    // flattened primitive tests of a CCD level: soup sub-test results, leaf-pair
+    // results, their hit flags and offsets
+    DBuf<PrimResult> sub, cres;
+    DBuf<int32_t> chit, cflag_off, nn_cnt, nn_off, citem_off;
     // per pair
     DBuf<double> pm;    // [pairs][128] pose matrices
     DBuf<double> pfut;  // [pairs][28] projected futures of a and b

@@ -133,8 +133,9 @@ int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
 
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library launched on the context, and, with profiling on, CUDA-event times
- * of the dominant kernels: kind 0 swept-box filter, 1 triangle-triangle CCD,
- * 2 leaf-pair CCD, 3 discrete triangle distance, 4 sequential-impulse solve.
+ * of the dominant kernels: kind 0 swept-box filter, 1 point-triangle CCD
+ * tests, 2 edge-edge CCD tests, 3 discrete triangle distance,
+ * 4 sequential-impulse solve.
  * Enabling (or disabling) profiling resets the totals. */
 int d2g_ctx_launches(d2g_ctx* ctx, int64_t* launches);
 int d2g_ctx_set_profiling(d2g_ctx* ctx, int32_t enable);
