@@ -124,97 +124,6 @@ __device__ __forceinline__ void put_result(PrimResult& r, double dist, V3 A, V3 
     r.toc = toc;
 }
 
-// Triangle-triangle CCD of each surviving slot (continuous_comparison.h:815-820).
-__global__ void __launch_bounds__(kBlock) k_soup_ccd(int n_items, const int32_t* __restrict__ items,
-                                                     const Entry* __restrict__ soup, const double* __restrict__ pm,
-                                                     const double* __restrict__ tris,
-                                                     const float* __restrict__ search, PrimResult* __restrict__ res,
-                                                     int32_t* __restrict__ hit, int32_t* __restrict__ entry_hits) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_items) return;
-    const int i = items[k];
-    const Entry e = soup[i >> 6];
-    const int ta = (i >> 3) & 7, tb = i & 7;
-    const double* M = pm + (size_t)PM_SIZE * e.pair;
-    const Tri at = load_tri(tris + (size_t)e.na * 72 + ta * 9);
-    const Tri bt = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
-    const Ccd r = tri_tri_ccd(at, bt, M);
-    put_result(res[k], r.dist, r.P, r.Q, r.toc);
-    const int h = r.dist < (double)search[e.pair] ? 1 : 0;
-    hit[k] = h;
-    if (h) atomicAdd(&entry_hits[i >> 6], 1);
-}
-
-// ------------------------------------------------------- connected stage ---
-// Primitive tests of a leaf-leaf node pair (continuous_comparison.h:831-910):
-// 3*na*nb point(a)-triangle(b), 3*nb*na point(b)-triangle(a), 9*na*nb edge-edge.
-__global__ void k_conn_count(int n, const Entry* __restrict__ conn, const int32_t* __restrict__ ntris,
-                             int32_t* __restrict__ cnt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const Entry e = conn[i];
-    cnt[i] = 15 * ntris[e.na] * ntris[e.nb];
-}
-
-__global__ void __launch_bounds__(kBlock) k_conn(int n_items, int n_entries, const int32_t* __restrict__ off,
-                                                 const Entry* __restrict__ conn, const double* __restrict__ pm,
-                                                 const int32_t* __restrict__ ntris,
-                                                 const double* __restrict__ tris, const float* __restrict__ search,
-                                                 PrimResult* __restrict__ res, int32_t* __restrict__ hit) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_items) return;
-    int lo = 0, hi = n_entries;  // last entry with off[e] <= k
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (off[mid] <= k)
-            lo = mid;
-        else
-            hi = mid;
-    }
-    const Entry e = conn[lo];
-    const int l = k - off[lo];
-    const int na = ntris[e.na], nb = ntris[e.nb];
-    const double* M = pm + (size_t)PM_SIZE * e.pair;
-    const double* ta = tris + (size_t)e.na * 72;
-    const double* tb = tris + (size_t)e.nb * 72;
-    const int n1 = 3 * na * nb, n2 = 3 * nb * na;
-    Ccd r;
-    V3 A, B;
-    if (l < n1) {
-        const int vi = l / nb, j = l % nb;
-        const Tri t = load_tri(ta + (vi / 3) * 9);
-        r = point_tri_ccd(tvert(t, vi % 3), M + PM_ABS, M + PM_ABE, load_tri(tb + j * 9), M + PM_BS, M + PM_BE);
-        A = r.P;
-        B = r.Q;
-    } else if (l < n1 + n2) {
-        const int m = l - n1;
-        const int vi = m / na, j = m % na;
-        const Tri t = load_tri(tb + (vi / 3) * 9);
-        r = point_tri_ccd(tvert(t, vi % 3), M + PM_BAS, M + PM_BAE, load_tri(ta + j * 9), M + PM_AS, M + PM_AE);
-        A = r.Q;
-        B = r.P;
-    } else {
-        const int m = l - n1 - n2;
-        const int ei = m / (3 * nb), ej = m % (3 * nb);
-        const Edge ea = tedge(load_tri(ta + (ei / 3) * 9), ei % 3);
-        const Edge eb = tedge(load_tri(tb + (ej / 3) * 9), ej % 3);
-        Edge aS, aE, bS, bE;
-        aS.A = xform_rigid(ea.A, M + PM_AS);
-        aS.B = xform_rigid(ea.B, M + PM_AS);
-        aE.A = xform_rigid(ea.A, M + PM_AE);
-        aE.B = xform_rigid(ea.B, M + PM_AE);
-        bS.A = xform_rigid(eb.A, M + PM_BS);
-        bS.B = xform_rigid(eb.B, M + PM_BS);
-        bE.A = xform_rigid(eb.A, M + PM_BE);
-        bE.B = xform_rigid(eb.B, M + PM_BE);
-        r = edge_edge_ccd(aS, aE, bS, bE);
-        A = r.Q;
-        B = r.P;
-    }
-    put_result(res[k], r.dist, A, B, r.toc);
-    hit[k] = r.dist < (double)search[e.pair] ? 1 : 0;
-}
-
 // ------------------------------------------- flattened primitive tests -----
 // One level of the CCD as two homogeneous work lists: every point-triangle
 // test and every edge-edge test of the level, from the soup stage (the 15
@@ -366,7 +275,39 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_ee(int n_tp, int n_total, c
     bS.B = xform_rigid(eb.B, M + PM_BS);
     bE.A = xform_rigid(eb.A, M + PM_BE);
     bE.B = xform_rigid(eb.B, M + PM_BE);
-    const Ccd r = edge_edge_ccd(aS, aE, bS, bE);
+    // Every distance edgeEdgeCCD can return is between points of the two
+    // swept segments, which lie in the boxes of their four endpoint positions.
+    // A box gap beyond the search distance (plus 1e-7 m, far above FP64
+    // rounding at scene scale) means no hit, and such a sub-test can never be
+    // the best of a triangle pair that hits: skip it, recording +inf.
+    const double lim = (double)search[e.pair] + 1e-7;
+    double gap2 = 0.0;
+    {
+        const double ax[4] = {aS.A.x, aS.B.x, aE.A.x, aE.B.x}, ay[4] = {aS.A.y, aS.B.y, aE.A.y, aE.B.y},
+                     az[4] = {aS.A.z, aS.B.z, aE.A.z, aE.B.z};
+        const double bx[4] = {bS.A.x, bS.B.x, bE.A.x, bE.B.x}, by[4] = {bS.A.y, bS.B.y, bE.A.y, bE.B.y},
+                     bz[4] = {bS.A.z, bS.B.z, bE.A.z, bE.B.z};
+        const double* av[3] = {ax, ay, az};
+        const double* bv[3] = {bx, by, bz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const double alo = fmin(fmin(av[d][0], av[d][1]), fmin(av[d][2], av[d][3]));
+            const double ahi = fmax(fmax(av[d][0], av[d][1]), fmax(av[d][2], av[d][3]));
+            const double blo = fmin(fmin(bv[d][0], bv[d][1]), fmin(bv[d][2], bv[d][3]));
+            const double bhi = fmax(fmax(bv[d][0], bv[d][1]), fmax(bv[d][2], bv[d][3]));
+            const double g = fmax(blo - ahi, alo - bhi);
+            if (g > 0.0) gap2 = gap2 + g * g;
+        }
+    }
+    Ccd r;
+    if (gap2 > lim * lim) {
+        r.dist = 1.0 / 0.0;
+        r.P = mk(0, 0, 0);
+        r.Q = mk(0, 0, 0);
+        r.toc = 1.0;
+    } else {
+        r = edge_edge_ccd(aS, aE, bS, bE);
+    }
     if (k >= 0) {
         store_prim(sub + 15 * (size_t)k + s, r.dist, r.P, r.Q, r.toc);
     } else {

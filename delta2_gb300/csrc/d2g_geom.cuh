@@ -652,8 +652,13 @@ D2G_HD Ccd edge_edge_ccd(const Edge& aS, const Edge& aE, const Edge& bS, const E
             const double pb = edge_project(btA, btB, Q);
             double td, td2;
             ee_newton_terms(aS, aE, bS, bE, pa, pb, t, td, td2);
+            const double t_prev = t;
             t = t - td / td2;
             t = clamp01(t);
+            // Each iteration is a function of t alone: once t repeats (or is
+            // NaN) the remaining iterations recompute the same distance, which
+            // cannot lower min_dist, so stopping gives the same result.
+            if (t == t_prev || t != t) break;
         }
     }
     r.dist = min_dist;
