@@ -116,6 +116,10 @@ def _p(a, t):
     return a.ctypes.data_as(t)
 
 
+WORLD_STATS = ["ccd_pairs", "ccd_contacts", "np_pairs", "np_contacts", "solves", "failures", "normal_iters",
+               "friction_iters", "ccd_node_pairs", "ccd_tri_pairs", "ccd_leaf_pairs", "np_node_pairs", "np_tri_pairs"]
+
+
 class Scene:
     """Flattened trees and bodies (numpy arrays in the C ABI layout)."""
 
@@ -319,6 +323,104 @@ class Context:
                                                               int(n_pairs), C.byref(n), C.byref(dc), C.byref(do),
                                                               _p(cnt, I64P)))
         return n.value, dc.value, do.value, cnt
+
+    def select_time_steps(self, pairs, clusters, opt_dt):
+        """fineCollisionClustersWithTimeStepSelection + clamp for clusters given as
+        a list of (particles, interaction index range) -> array of steps.
+
+        ``pairs`` [n,2] holds every cluster's interactions, cluster after
+        cluster; ``clusters`` is a list of (particle_list, n_interactions)."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        pair_off = np.zeros(len(clusters) + 1, np.int32)
+        part_off = np.zeros(len(clusters) + 1, np.int32)
+        parts = []
+        for k, (plist, ni) in enumerate(clusters):
+            pair_off[k + 1] = pair_off[k] + ni
+            part_off[k + 1] = part_off[k] + len(plist)
+            parts += list(plist)
+        parts = np.ascontiguousarray(parts, dtype=np.int32)
+        out = np.zeros(max(1, len(clusters)))
+        cnt = np.zeros(4, np.int64)
+        _check(lib().d2g_select_time_steps(self.h, _p(pairs, I32P), len(pairs), _p(pair_off, I32P),
+                                           _p(part_off, I32P), _p(parts, I32P), len(clusters), C.c_float(opt_dt),
+                                           _p(out, F64P), _p(cnt, I64P)))
+        return out[:len(clusters)].copy(), cnt
+
+    def filter_contacts(self, contacts, offsets, margin=0.0):
+        """filterContacts per group -> (kept contacts [m,14], out_offsets [n_groups+1])."""
+        c = np.ascontiguousarray(contacts, dtype=np.float64).reshape(-1, CONTACT_LEN)
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        ng = len(off) - 1
+        cap = max(1, len(c))
+        out = np.zeros((cap, CONTACT_LEN))
+        out_off = np.zeros(ng + 1, np.int32)
+        _check(lib().d2g_filter_contacts(self.h, _p(c, F64P), _p(off, I32P), ng, C.c_double(margin), _p(out, F64P),
+                                         cap, _p(out_off, I32P)))
+        return out[:out_off[-1]].copy(), out_off
+
+    def solve_clusters(self, clusters, gravity_z=-9.8):
+        """SequentialImpulses::solve for clusters given as a list of
+        (particles, step, contacts [m,14], pair_count [m], warm [m] (NaN = none)).
+        Updates the device future states; returns (status [k], iterations [k,2],
+        impulses and body pairs per cluster in the solver's sorted order)."""
+        part_off = np.zeros(len(clusters) + 1, np.int32)
+        con_off = np.zeros(len(clusters) + 1, np.int32)
+        parts, steps, recs, cnts, warms = [], [], [], [], []
+        for k, (plist, step, con, cnt, warm) in enumerate(clusters):
+            con = np.asarray(con, dtype=np.float64).reshape(-1, CONTACT_LEN)
+            part_off[k + 1] = part_off[k] + len(plist)
+            con_off[k + 1] = con_off[k] + len(con)
+            parts += list(plist)
+            steps.append(step)
+            recs.append(con)
+            cnts.append(np.asarray(cnt, dtype=np.int32).reshape(-1))
+            warms.append(np.asarray(warm, dtype=np.float64).reshape(-1))
+        parts = np.ascontiguousarray(parts, dtype=np.int32)
+        steps = np.ascontiguousarray(steps, dtype=np.float64)
+        rec = np.ascontiguousarray(np.concatenate(recs) if recs else np.zeros((0, CONTACT_LEN)))
+        cnt = np.ascontiguousarray(np.concatenate(cnts) if cnts else np.zeros(0, np.int32), dtype=np.int32)
+        warm = np.ascontiguousarray(np.concatenate(warms) if warms else np.zeros(0), dtype=np.float64)
+        n = len(rec)
+        status = np.zeros(max(1, len(clusters)), np.int32)
+        iters = np.zeros((max(1, len(clusters)), 2), np.int32)
+        imp = np.zeros(max(1, n))
+        ab = np.zeros((max(1, n), 2), np.int32)
+        rc = lib().d2g_solve_clusters(self.h, len(clusters), _p(part_off, I32P), _p(parts, I32P), _p(steps, F64P),
+                                      _p(rec, F64P), _p(con_off, I32P), _p(cnt, I32P), _p(warm, F64P),
+                                      C.c_double(gravity_z), _p(status, I32P), _p(iters, I32P), _p(imp, F64P),
+                                      _p(ab, I32P))
+        if rc not in (0, 1):
+            _check(rc)
+        k = len(clusters)
+        return (status[:k].copy(), iters[:k].copy(),
+                [imp[con_off[i]:con_off[i + 1]].copy() for i in range(k)],
+                [ab[con_off[i]:con_off[i + 1]].copy() for i in range(k)])
+
+    def world_configure(self, scene=None, opt_dt=None, gravity_z=None):
+        """Set up the adaptive cluster stepper over the context's bodies."""
+        scene = scene or self.scene
+        self._aabb = np.ascontiguousarray(scene.local_aabb, dtype=np.float32)
+        dt = scene.opt_dt if opt_dt is None else opt_dt
+        g = scene.gravity_z if gravity_z is None else gravity_z
+        _check(lib().d2g_world_configure(self.h, _p(self._aabb, F32P), C.c_float(dt), C.c_double(g)))
+
+    def world_step(self, n=1):
+        """n outer steps (BroadPhaseEmbreeCluster::step) on the GPU."""
+        _check(lib().d2g_world_step(self.h, int(n)))
+
+    def world_stats(self):
+        out = np.zeros(13, dtype=np.int64)
+        _check(lib().d2g_world_stats(self.h, _p(out, I64P)))
+        return dict(zip(WORLD_STATS, out.tolist()))
+
+    def world_warm(self):
+        n = C.c_int32()
+        _check(lib().d2g_world_warm(self.h, None, None, 0, C.byref(n)))
+        m = max(1, n.value)
+        keys = np.zeros((m, 2), np.int32)
+        vals = np.zeros(m)
+        _check(lib().d2g_world_warm(self.h, _p(keys, I32P), _p(vals, F64P), m, C.byref(n)))
+        return {(int(keys[i, 0]), int(keys[i, 1])): float(vals[i]) for i in range(n.value)}
 
     def compare_trees_full(self, pairs, capacity=None):
         """compareTreesFull for each pair -> (contacts [n,14], offsets [n_pairs+1], counters)."""

@@ -232,6 +232,8 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    d2g::world_free(c->world);
+    c->world = nullptr;
     c->mesh_node_off.release();
     c->ntris.release();
     c->nodes.release();
@@ -273,6 +275,14 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     E.nn_cnt.release();
     E.nn_off.release();
     E.citem_off.release();
+    E.st_mt.release();
+    E.st_new_dt.release();
+    E.st_step.release();
+    E.st_out.release();
+    E.st_has.release();
+    E.st_cl_pair_off.release();
+    E.st_cl_part_off.release();
+    E.st_cl_parts.release();
     E.pm.release();
     E.pfut.release();
     E.search.release();
@@ -381,6 +391,20 @@ int d2g_ctx_set_bodies(d2g_ctx* c, const d2g_bodies* b) {
     if (b->sleep_steps) RC(upload(c, c->sleep_steps, (const int32_t*)b->sleep_steps, n));
     if (b->sleeping) RC(upload(c, c->sleeping, (const uint8_t*)b->sleeping, n));
     if (b->bounding_radius) RC(upload(c, c->bounding_radius, b->bounding_radius, n));
+    if (!b->sleep_steps) {
+        RC(c->sleep_steps.ensure(n));
+        D2G_CUDA(cudaMemsetAsync(c->sleep_steps.p, 0, n * sizeof(int32_t), c->stream));
+    }
+    if (!b->sleeping) {
+        RC(c->sleeping.ensure(n));
+        D2G_CUDA(cudaMemsetAsync(c->sleeping.p, 0, n, c->stream));
+    }
+    c->h_is_static.assign(b->is_static, b->is_static + n);
+    c->h_geo_eps.assign(b->geo_eps, b->geo_eps + n);
+    if (b->bounding_radius)
+        c->h_bounding_radius.assign(b->bounding_radius, b->bounding_radius + n);
+    else
+        c->h_bounding_radius.clear();
     D2G_CUDA(cudaStreamSynchronize(c->stream));
     c->n_bodies = b->n;
     return D2G_OK;
@@ -493,6 +517,168 @@ int d2g_compare_trees_full_continuous_device(d2g_ctx* c, const int32_t* d_pairs,
     if (n_contacts) *n_contacts = n_rec;
     if (d_contacts) *d_contacts = c->eng.rec_sorted.p;
     if (d_offsets) *d_offsets = c->eng.out_off.p;
+    return D2G_OK;
+}
+
+int d2g_filter_contacts(d2g_ctx* c, const double* contacts, const int32_t* offsets, int32_t n_groups, double margin,
+                        double* out, int32_t capacity, int32_t* out_offsets) {
+    RC(check_ready(c));
+    if (n_groups < 0 || !offsets || !out_offsets || offsets[0] != 0) {
+        set_error("invalid contact groups");
+        return D2G_ERR_INVALID;
+    }
+    for (int g = 0; g < n_groups; g++)
+        if (offsets[g + 1] < offsets[g]) {
+            set_error("contact group offsets decrease");
+            return D2G_ERR_INVALID;
+        }
+    const int n = offsets[n_groups];
+    if (n > 0 && !contacts) {
+        set_error("null contacts");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.up_rec, contacts, 14 * (size_t)n));
+    RC(upload(c, E.up_off, offsets, (size_t)n_groups + 1));
+    int kept = 0;
+    RC(d2g::run_filter(c, E.up_off.p, E.up_rec.p, n_groups, n, margin, &kept));
+    RC(download(c, out_offsets, E.flt_off, (size_t)n_groups + 1));
+    if (out && kept <= capacity) RC(download(c, out, E.flt, 14 * (size_t)kept));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    if (kept > capacity) {
+        set_error("filtered contacts exceed the capacity");
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
+}
+
+int d2g_solve_clusters(d2g_ctx* c, int32_t n_clusters, const int32_t* particle_off, const int32_t* particles,
+                       const double* step, const double* contacts, const int32_t* contact_off,
+                       const int32_t* pair_count, const double* warm, double gravity_z, int32_t* status,
+                       int32_t* iterations, double* impulse_out, int32_t* pair_out) {
+    RC(check_ready(c));
+    if (n_clusters < 0 || !particle_off || !contact_off || (n_clusters > 0 && (!particles || !step || !status))) {
+        set_error("invalid cluster arrays");
+        return D2G_ERR_INVALID;
+    }
+    if (particle_off[0] != 0 || contact_off[0] != 0) {
+        set_error("cluster offsets must start at 0");
+        return D2G_ERR_INVALID;
+    }
+    const int nb = c->n_bodies;
+    std::vector<int32_t> owner(nb, -1);
+    for (int k = 0; k < n_clusters; k++) {
+        if (particle_off[k + 1] < particle_off[k] || contact_off[k + 1] < contact_off[k]) {
+            set_error("cluster " + std::to_string(k) + " has decreasing offsets");
+            return D2G_ERR_INVALID;
+        }
+        for (int i = particle_off[k]; i < particle_off[k + 1]; i++) {
+            const int g = particles[i];
+            if (g < 0 || g >= nb) {
+                set_error("cluster particle index out of range");
+                return D2G_ERR_INVALID;
+            }
+            if (!c->h_is_static[g]) {  // a moving body's work area is per body
+                if (owner[g] >= 0) {
+                    set_error("moving body " + std::to_string(g) + " is in more than one cluster or listed twice");
+                    return D2G_ERR_INVALID;
+                }
+                owner[g] = k;
+            }
+        }
+    }
+    const int np = particle_off[n_clusters];
+    const int n = contact_off[n_clusters];
+    if (n > 0 && (!contacts || !pair_count || !warm)) {
+        set_error("null contact arrays");
+        return D2G_ERR_INVALID;
+    }
+    for (int k = 0; k < n_clusters; k++)
+        for (int i = contact_off[k]; i < contact_off[k + 1]; i++) {
+            const double* h = contacts + 14 * (size_t)i;
+            for (int q = 11; q <= 12; q++) {
+                const double v = h[q];
+                const int g = (v >= 0.0 && v < (double)nb) ? (int)v : -1;
+                bool in = g >= 0 && (double)g == v;
+                if (in) {
+                    bool found = false;
+                    for (int j = particle_off[k]; j < particle_off[k + 1] && !found; j++) found = particles[j] == g;
+                    in = found;
+                }
+                if (!in) {
+                    set_error("contact " + std::to_string(i) + " names a body outside its cluster");
+                    return D2G_ERR_INVALID;
+                }
+            }
+            if (pair_count[i] < 1) {
+                set_error("contact pair counts must be positive");
+                return D2G_ERR_INVALID;
+            }
+        }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.up_part_off, particle_off, (size_t)n_clusters + 1));
+    RC(upload(c, E.up_parts, particles, (size_t)np));
+    RC(upload(c, E.up_step, step, (size_t)n_clusters));
+    RC(upload(c, E.up_con_off, contact_off, (size_t)n_clusters + 1));
+    RC(upload(c, E.up_rec, contacts, 14 * (size_t)n));
+    RC(upload(c, E.up_cnt, pair_count, (size_t)n));
+    RC(upload(c, E.up_warm, warm, (size_t)n));
+    RC(E.up_status.ensure(n_clusters + 1));
+    RC(E.up_iters.ensure(2 * (size_t)n_clusters + 2));
+    RC(E.up_imp.ensure(n + 1));
+    RC(E.up_ab.ensure(2 * (size_t)n + 2));
+    RC(d2g::run_solve(c, n_clusters, E.up_part_off.p, E.up_parts.p, np, E.up_con_off.p, n, E.up_rec.p, E.up_cnt.p,
+                      E.up_warm.p, E.up_step.p, gravity_z, E.up_status.p, E.up_iters.p, E.up_imp.p, E.up_ab.p, nullptr,
+                      nullptr));
+    RC(download(c, status, E.up_status, (size_t)n_clusters));
+    if (iterations) RC(download(c, iterations, E.up_iters, 2 * (size_t)n_clusters));
+    if (impulse_out) RC(download(c, impulse_out, E.up_imp, (size_t)n));
+    if (pair_out) RC(download(c, pair_out, E.up_ab, 2 * (size_t)n));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < n_clusters; k++)
+        if (status[k] != 0) return D2G_SOLVE_FAILED;
+    return D2G_OK;
+}
+
+int d2g_select_time_steps(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, const int32_t* cluster_pair_off,
+                          const int32_t* cluster_particle_off, const int32_t* cluster_particles, int32_t n_clusters,
+                          float opt_dt, double* step_out, int64_t* counters) {
+    RC(check_ready(c));
+    RC(check_pairs(c, pairs, n_pairs));
+    if (n_clusters < 0 || !cluster_pair_off || !cluster_particle_off || (n_clusters > 0 && (!cluster_particles ||
+        !step_out))) {
+        set_error("invalid cluster arrays");
+        return D2G_ERR_INVALID;
+    }
+    if (cluster_pair_off[0] != 0 || cluster_pair_off[n_clusters] != n_pairs || cluster_particle_off[0] != 0) {
+        set_error("cluster offsets must start at 0 and end at the pair count");
+        return D2G_ERR_INVALID;
+    }
+    for (int k = 0; k < n_clusters; k++) {
+        if (cluster_pair_off[k + 1] < cluster_pair_off[k] || cluster_particle_off[k + 1] <= cluster_particle_off[k]) {
+            set_error("cluster " + std::to_string(k) + " has decreasing offsets or no particles");
+            return D2G_ERR_INVALID;
+        }
+    }
+    const int np = cluster_particle_off[n_clusters];
+    for (int i = 0; i < np; i++)
+        if (cluster_particles[i] < 0 || cluster_particles[i] >= c->n_bodies) {
+            set_error("cluster particle index out of range");
+            return D2G_ERR_INVALID;
+        }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.d_pairs, pairs, 2 * (size_t)n_pairs));
+    RC(upload(c, E.st_cl_pair_off, cluster_pair_off, (size_t)n_clusters + 1));
+    RC(upload(c, E.st_cl_part_off, cluster_particle_off, (size_t)n_clusters + 1));
+    RC(upload(c, E.st_cl_parts, cluster_particles, (size_t)np));
+    RC(E.st_out.ensure(n_clusters + 1));
+    RC(d2g::run_select_steps(c, E.d_pairs.p, n_pairs, E.st_cl_pair_off.p, E.st_cl_part_off.p, E.st_cl_parts.p,
+                             n_clusters, (double)opt_dt, E.st_out.p, counters));
+    RC(download(c, step_out, E.st_out, (size_t)n_clusters));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
     return D2G_OK;
 }
 

@@ -351,11 +351,12 @@ __global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restr
                                                const double* __restrict__ geo_eps,
                                                const float* __restrict__ search, PrimResult* __restrict__ res,
                                                double* __restrict__ res_eps, int32_t* __restrict__ hit,
-                                               int32_t* __restrict__ entry_hits) {
+                                               int32_t* __restrict__ entry_hits, int32_t* __restrict__ tri_pairs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_slots) return;
     const Entry e = front[i >> 6];
     const int ta = (i >> 3) & 7, tb = i & 7;
+    if (tri_pairs && (i & 63) == 0) atomicAdd(tri_pairs, ntris[e.na] * ntris[e.nb]);  // statistics only
     int h = 0;
     if (ta < ntris[e.na] && tb < ntris[e.nb]) {
         const double* M = pm + 32 * (size_t)e.pair;
@@ -830,6 +831,8 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     RC(E.pm.ensure(32 * (size_t)n_pairs + 1));
     RC(E.search.ensure(n_pairs + 1));
     RC(E.soup.ensure(n_pairs + 1));
+    RC(E.np_tri.ensure(1));
+    D2G_CUDA(cudaMemsetAsync(E.np_tri.p, 0, sizeof(int32_t), s));
     if (n_pairs > 0)
         LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, ctx->fut.p, ctx->mesh.p, ctx->mesh_node_off.p,
                                                      ctx->geo_eps.p, E.pm.p, E.search.p, E.soup.p);
@@ -839,7 +842,6 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
         c_levels++;
         c_node += n;
         const int n_slots = 64 * n;
-        c_tri += n_slots;
         RC(E.res.ensure(n_slots));
         RC(res_eps.ensure(4 * (size_t)n_slots));
         RC(E.hit.ensure(n_slots));
@@ -849,7 +851,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
         const int pf = prof_begin(ctx, PROF_NP, n_slots);
         LAUNCH(k_np, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
                                                  ctx->eps.p, ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p,
-                                                 res_eps.p, E.hit.p, E.entry_hits.p);
+                                                 res_eps.p, E.hit.p, E.entry_hits.p, E.np_tri.p);
         prof_end(ctx, pf);
         LAUNCH(k_final_flags, n_slots, n_slots, nullptr, E.soup.p, ctx->nodes.p, E.hit.p,
                                                           E.flags.p);
@@ -862,9 +864,11 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
                                                      E.cnt_b.p);
         RC(scan(ctx, E.cnt_a.p, E.off_a.p, n));
         D2G_CUDA(cudaMemsetAsync(E.off_b.p, 0, sizeof(int32_t) * (n + 1), s));
-        int32_t tot;
-        const int32_t* src = E.off_a.p + n;
-        RC(read_scalars(ctx, &src, 1, &tot));
+        int32_t vals[2];
+        const int32_t* srcs[2] = {E.off_a.p + n, E.np_tri.p};
+        RC(read_scalars(ctx, srcs, 2, vals));
+        const int32_t tot = vals[0];
+        c_tri = vals[1];
         RC(E.soup_next.ensure(tot + 1));
         LAUNCH(k_expand_write, n, n, E.soup.p, E.entry_hits.p, ctx->nodes.p, 0, E.off_a.p,
                                                      E.off_b.p, E.soup_next.p, E.conn_next.p);
@@ -1074,7 +1078,7 @@ extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const 
         const int n_slots = 64 * n;
         D2G_CUDA(cudaMemsetAsync(entry_hits, 0, sizeof(int32_t) * n, s));
         NA_LAUNCH(k_np, n_slots, n_slots, front, d_pairs, pm, sc->ntris, sc->tris, sc->eps, sc->inner_eps,
-                  sc->geo_eps, search, res, res_eps, hit, entry_hits);
+                  sc->geo_eps, search, res, res_eps, hit, entry_hits, nullptr);
         NA_LAUNCH(k_final_flags, n_slots, n_slots, nullptr, front, nodes, hit, flags);
         if (int rc = noalloc_scan(s, tmp, tmp_bytes, flags, flag_off, n_slots)) return rc;
         int32_t tot = 0;

@@ -11,6 +11,9 @@
 
 namespace d2g {
 
+struct WorldState;
+void world_free(WorldState* w);
+
 // Kernels timed in profiling mode (d2g_ctx_profile kinds).
 enum { PROF_SOUP_FILTER = 0, PROF_SOUP_CCD = 1, PROF_CONN = 2, PROF_NP = 3, PROF_SOLVE = 4, D2G_PROF_KINDS = 8 };
 
@@ -25,11 +28,30 @@ void set_error(const std::string& msg);
         }                                                                                           \
     } while (0)
 
-// Device buffer that grows geometrically (capacity in elements).
+// Device buffer that grows geometrically (capacity in elements); owns its
+// memory (freed on destruction, movable, not copyable).
 template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t cap = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), cap(o.cap) {
+        o.p = nullptr;
+        o.cap = 0;
+    }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            cap = o.cap;
+            o.p = nullptr;
+            o.cap = 0;
+        }
+        return *this;
+    }
+    ~DBuf() { release(); }
     int ensure(size_t n) {
         if (n <= cap) return D2G_OK;
         if (p) {
@@ -105,6 +127,20 @@ struct Engine {
     // results, their hit flags and offsets
     DBuf<PrimResult> sub, cres;
     DBuf<int32_t> chit, cflag_off, nn_cnt, nn_off, citem_off;
+    // time-step selection
+    DBuf<double> st_mt, st_new_dt, st_step, st_out;
+    DBuf<int32_t> st_has, st_cl_pair_off, st_cl_part_off, st_cl_parts;
+    // contact filtering
+    DBuf<int32_t> flt_idx, flt_keep, flt_cnt, flt_off, np_tri;
+    DBuf<double> flt;
+    // sequential-impulse solve
+    DBuf<unsigned long long> sv_keys, sv_keys_out;
+    DBuf<int32_t> sv_vals, sv_order, sv_wave_idx, sv_wave_off, sv_wave_cursor;
+    DBuf<double> sv_static_imp;
+    DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
+    // inputs / outputs of the host filter and solve entry points
+    DBuf<double> up_rec, up_warm, up_step, up_imp;
+    DBuf<int32_t> up_off, up_part_off, up_parts, up_con_off, up_cnt, up_status, up_iters, up_ab;
     // per pair
     DBuf<double> pm;    // [pairs][128] pose matrices
     DBuf<double> pfut;  // [pairs][28] projected futures of a and b
@@ -147,7 +183,11 @@ struct d2g_ctx {
     d2g::DBuf<int32_t> mesh, sleep_steps;
     d2g::DBuf<uint8_t> is_static, sleeping;
     d2g::DBuf<double> geo_eps, mu, mass, inv_inertia, last, cur, fut, last_dt, bounding_radius;
+    // host copies of the constant body data the host-side stepper reads
+    std::vector<uint8_t> h_is_static;
+    std::vector<double> h_geo_eps, h_bounding_radius;
     d2g::Engine eng;
+    d2g::WorldState* world = nullptr;  // adaptive cluster stepper (d2g_world.cpp)
     int32_t* h_pinned = nullptr;  // small pinned scratch for counts
     const int32_t* validated_pairs = nullptr;  // device pair buffer last checked in range
     int validated_n = -1;
@@ -158,4 +198,28 @@ namespace d2g {
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
+// Time-step selection (d2g_step.cu).
+int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const int32_t* d_cl_pair_off,
+                     const int32_t* d_cl_part_off, const int32_t* d_cl_parts, int n_clusters, double opt_dt,
+                     double* d_out, int64_t* counters, int* n_ccd_contacts = nullptr);
+int run_outer_project(d2g_ctx* ctx, double opt_dt);
+int run_pde_prepare(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts,
+                    const double* d_step, const double* d_tmin, int32_t* d_err);
+int run_pde_finish(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts,
+                   const double* d_step, const int32_t* d_status, int32_t* d_will_sleep);
+int run_rollback(d2g_ctx* ctx, const double* d_t_body, int32_t* d_err);
+int run_sleep_apply(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts,
+                    const double* d_step);
+// stepRecursive bookkeeping ops (k_cluster_ops): int4 (code, frame slot, stash offset, 0).
+enum { D2G_OP_ENTER = 1, D2G_OP_SPLIT = 2, D2G_OP_SAVE = 3, D2G_OP_MID = 4, D2G_OP_RESTORE = 5, D2G_OP_EXIT = 6 };
+int run_cluster_ops(d2g_ctx* ctx, int n_active, const int32_t* d_cl_idx, const int32_t* d_op_off, const int4* d_ops,
+                    const int32_t* d_part_off, const int32_t* d_parts, double* d_cl_step, double* d_cl_tmin,
+                    double* d_frame_start, double* d_stash, int32_t* d_err);
+// Contact filtering and sequential impulses (d2g_solve.cu).
+int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pairs, int n_rec, double margin,
+               int* n_out);
+int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts, int n_parts,
+              const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
+              const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
+              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm);
 }  // namespace d2g

@@ -1,0 +1,604 @@
+// Contact filtering and the per-cluster sequential-impulse solve.
+//
+// filterContacts (collision_detection/contact.h:44-69): one thread per body
+// pair, stable insertion sort by (eps_a + eps_b, |A - B|) and the greedy
+// de-duplication of contact midpoints.
+//
+// SequentialImpulses::solve (strategies/contact_force/sequential_impulses.cpp:
+// 104-638): one block per cluster.  The reference's Gauss-Seidel sweep visits
+// the contacts in sorted order and integrates both bodies after each one; a
+// contact only reads and writes its own two bodies, so contacts are grouped
+// into waves: a contact's wave is one past the last wave that touched either
+// of its moving bodies.  Within a wave the bodies are disjoint and the
+// contacts run in parallel; every body still sees its contacts in sorted
+// order, so every floating-point operation happens in the reference's order
+// (static bodies are never integrated; the impulse sum the convergence test
+// reads for them is accumulated from per-contact deltas in sorted order).
+#include <cub/cub.cuh>
+
+#include "d2g_geom.cuh"
+#include "d2g_internal.hpp"
+
+namespace d2g {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kSolveBlock = 128;
+inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+// ------------------------------------------------------------ filtering ---
+__device__ __forceinline__ bool contact_less(const double* a, const double* b) {
+    const double a_eps = a[6] + a[7], b_eps = b[6] + b[7];
+    if (a_eps == b_eps) {
+        const V3 da = mk(a[0] - a[3], a[1] - a[4], a[2] - a[5]);
+        const V3 db = mk(b[0] - b[3], b[1] - b[4], b[2] - b[5]);
+        return norm(da) < norm(db);
+    }
+    return a_eps < b_eps;
+}
+
+// One thread per pair: order (stable) in idx, greedy keep flags in keep.
+__global__ void k_filter(int n_pairs, const int32_t* __restrict__ off, const double* __restrict__ rec,
+                         int32_t* __restrict__ idx, int32_t* __restrict__ keep, int32_t* __restrict__ kept_cnt,
+                         double margin) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs) return;
+    const int c0 = off[p], c1 = off[p + 1];
+    for (int i = c0; i < c1; i++) idx[i] = i;
+    for (int i = c0 + 1; i < c1; i++) {  // stable insertion sort
+        const int v = idx[i];
+        int j = i - 1;
+        while (j >= c0 && contact_less(rec + 14 * (size_t)v, rec + 14 * (size_t)idx[j])) {
+            idx[j + 1] = idx[j];
+            j--;
+        }
+        idx[j + 1] = v;
+    }
+    int kept = 0;
+    for (int i = c0; i < c1; i++) {
+        const double* ct = rec + 14 * (size_t)idx[i];
+        bool new_point = true;
+        for (int j = c0; j < i; j++) {
+            if (!keep[j]) continue;
+            const double* h = rec + 14 * (size_t)idx[j];
+            const V3 ht_mid = mk((ct[0] + ct[3]) / 2, (ct[1] + ct[4]) / 2, (ct[2] + ct[5]) / 2);
+            const V3 h_mid = mk((h[0] + h[3]) / 2, (h[1] + h[4]) / 2, (h[2] + h[5]) / 2);
+            const double dist = norm(ht_mid - h_mid);
+            const double search = (ct[6] + ct[7]) + margin;
+            if (dist < search) {
+                new_point = false;
+                break;
+            }
+        }
+        keep[i] = new_point ? 1 : 0;
+        kept += new_point ? 1 : 0;
+    }
+    kept_cnt[p] = kept;
+}
+
+__global__ void k_filter_write(int n_pairs, const int32_t* __restrict__ off, const int32_t* __restrict__ idx,
+                               const int32_t* __restrict__ keep, const int32_t* __restrict__ out_off,
+                               const double* __restrict__ rec, double* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs) return;
+    int o = out_off[p];
+    for (int i = off[p]; i < off[p + 1]; i++) {
+        if (!keep[i]) continue;
+        const double* s = rec + 14 * (size_t)idx[i];
+        double* d = out + 14 * (size_t)o;
+        for (int k = 0; k < 14; k++) d[k] = s[k];
+        o++;
+    }
+}
+
+// ---------------------------------------------------------------- solve ---
+// Per-body working state (indexed by global body id; moving bodies belong to
+// one cluster only).
+struct BodyWork {
+    double FS[14], FSf[14];
+    double T_FS[12], T_FSf[12], T_cur[12];
+    double Iinv[9];  // R(fut.q) * ii * R(fut.q)^T, constant during a solve
+    double imp[3], rimp[3], ioff[3], roff[3], last_imp[3];
+    int last_level;
+};
+
+// Per-contact working state (indexed by the contact's position in the call).
+struct ConWork {
+    double local_A[3], local_B[3], n[3];
+    double start_dist, mass_eff, outer, impulse, impulse_offset;
+    double last_fi[3], last_rot_A[3], last_rot_B[3], upd_total[3];
+    double static_delta[3];
+    int a, b, level, pair_cnt;
+};
+
+__device__ __forceinline__ V3 ld3(const double* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ void st3(double* p, V3 v) {
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+__device__ __forceinline__ void rigid12(const State& s, double* T12) {
+    double T[16];
+    transformation(s.q, s.x, T);
+    for (int k = 0; k < 12; k++) T12[k] = T[k];
+}
+__device__ __forceinline__ V3 calc_torque(V3 force, V3 point, V3 com) { return cross(-force, point - com); }
+
+// sequential_impulses.cpp:46-70 updateState and :72-96 updateStateImmediate,
+// with R(fut.q) * ii * R(fut.q)^T precomputed (it only depends on fut).
+__device__ void integrate_body(BodyWork& w, const double* fut, double mass, double t) {
+    const State f = load_state(fut);
+    const V3 imp = ld3(w.imp), ioff = ld3(w.ioff), rimp = ld3(w.rimp), roff = ld3(w.roff);
+    State u = f;
+    u.v = f.v + imp / mass;
+    u.x = f.x + (ioff / mass) * t;
+    u.L = f.L + rimp;
+    {
+        const V3 omega = m3_vec(w.Iinv, f.L + t * roff);
+        u.q = qmul(qexp((0.5 * omega) * t), f.q);
+    }
+    State ui = f;
+    ui.v = f.v + imp / mass;
+    ui.x = (f.x + (ioff / mass) * t) + (imp / mass) * t;
+    ui.L = f.L + rimp;
+    {
+        const V3 omega = m3_vec(w.Iinv, (f.L + t * roff) + t * rimp);
+        ui.q = qmul(qexp((0.5 * omega) * t), f.q);
+    }
+    store_state(w.FS, u);
+    store_state(w.FSf, ui);
+    rigid12(u, w.T_FS);
+    rigid12(ui, w.T_FSf);
+}
+
+__device__ __forceinline__ V3 xf12(V3 p, const double* T) {
+    return mk(((T[0] * p.x + T[1] * p.y) + T[2] * p.z) + T[3] * 1.0,
+              ((T[4] * p.x + T[5] * p.y) + T[6] * p.z) + T[7] * 1.0,
+              ((T[8] * p.x + T[9] * p.y) + T[10] * p.z) + T[11] * 1.0);
+}
+
+__device__ __forceinline__ bool block_any(bool v) { return __syncthreads_or(v ? 1 : 0) != 0; }
+
+// One block per cluster.
+__global__ void __launch_bounds__(kSolveBlock)
+    k_solve(int n_clusters, const int32_t* __restrict__ cl_part_off, const int32_t* __restrict__ cl_parts,
+            const int32_t* __restrict__ cl_con_off, const int32_t* __restrict__ order, const double* __restrict__ rec,
+            const int32_t* __restrict__ pair_cnt, const double* __restrict__ warm, const double* __restrict__ cl_step,
+            const uint8_t* __restrict__ is_static, const double* __restrict__ mass, const double* __restrict__ ii,
+            const double* __restrict__ mu, const double* __restrict__ cur, double* __restrict__ fut, double gravity_z,
+            BodyWork* __restrict__ bw, ConWork* __restrict__ cw, int32_t* __restrict__ wave_idx,
+            int32_t* __restrict__ wave_off, int32_t* __restrict__ wave_cursor, double* __restrict__ static_imp, int32_t* __restrict__ status,
+            int32_t* __restrict__ iters, double* __restrict__ out_impulse, int32_t* __restrict__ out_ab,
+            const int32_t* __restrict__ con_pair, double* __restrict__ pair_warm) {
+    const int k = blockIdx.x;
+    if (k >= n_clusters) return;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int p0 = cl_part_off[k], p1 = cl_part_off[k + 1];
+    const int c0 = cl_con_off[k], c1 = cl_con_off[k + 1];
+    const int nc = c1 - c0;
+    const double t = cl_step[k];
+    __shared__ int s_fail, s_levels;
+
+    // ---- contacts in sorted order: local frames, normal mass, failure test (:109-168)
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+    for (int i = tid; i < nc; i += nt) {
+        ConWork& C = cw[c0 + i];
+        const double* h = rec + 14 * (size_t)order[c0 + i];
+        const V3 A = ld3(h), B = ld3(h + 3);
+        C.a = (int)h[11];
+        C.b = (int)h[12];
+        C.pair_cnt = pair_cnt[order[c0 + i]];
+        C.start_dist = norm(A - B);
+        if (C.start_dist < 1e-6 && t > 1e-4) atomicExch(&s_fail, 1);
+        double T[16], Ti[16];
+        const State fa = load_state(fut + 14 * (size_t)C.a), fb = load_state(fut + 14 * (size_t)C.b);
+        transformation(fa.q, fa.x, T);
+        mat_inverse(T, Ti);
+        st3(C.local_A, xform_general(A, Ti));
+        transformation(fb.q, fb.x, T);
+        mat_inverse(T, Ti);
+        st3(C.local_B, xform_general(B, Ti));
+        const V3 gn = (B - A) / 2.0;
+        st3(C.n, normalized(gn));
+        const V3 rnA = cross(A - fa.x, gn), rnB = cross(B - fb.x, gn);
+        double kn = 0.0;
+        if (!is_static[C.a]) kn += 1.0 / mass[C.a] + quad_form(rnA, ii + 9 * (size_t)C.a);
+        if (!is_static[C.b]) kn += 1.0 / mass[C.b] + quad_form(rnB, ii + 9 * (size_t)C.b);
+        C.mass_eff = kn < 1e-6 ? 0.0 : 1.0 / kn;
+        C.outer = (h[6] + h[7]) * 0.25;
+        C.impulse = warm[order[c0 + i]] == warm[order[c0 + i]] ? warm[order[c0 + i]] * 0.75 : 0.0;
+        C.impulse_offset = 0.0;
+        for (int q = 0; q < 3; q++) C.last_fi[q] = C.last_rot_A[q] = C.last_rot_B[q] = 0.0;
+    }
+    __syncthreads();
+    if (s_fail) {
+        if (tid == 0) status[k] = 1;
+        return;
+    }
+    // ---- bodies: gravity impulse, states (:178-188)
+    for (int i = p0 + tid; i < p1; i += nt) {
+        const int g = cl_parts[i];
+        BodyWork& W = bw[g];
+        const double m = mass[g];
+        const V3 f = mk(m * 0.0, m * 0.0, m * gravity_z);
+        st3(W.imp, f * t);
+        for (int q = 0; q < 3; q++) W.rimp[q] = W.ioff[q] = W.roff[q] = 0.0;
+        for (int q = 0; q < 14; q++) W.FS[q] = W.FSf[q] = fut[14 * (size_t)g + q];
+        const State fs = load_state(fut + 14 * (size_t)g);
+        rigid12(fs, W.T_FS);
+        rigid12(fs, W.T_FSf);
+        rigid12(load_state(cur + 14 * (size_t)g), W.T_cur);
+        world_inv_inertia(fs.q, ii + 9 * (size_t)g, W.Iinv);
+        W.last_level = -1;
+        if (is_static[g]) st3(static_imp + 3 * (size_t)i, f * t);
+    }
+    __syncthreads();
+    // ---- wave schedule (sequential, integer work only)
+    if (tid == 0) {
+        int levels = 0;
+        for (int i = 0; i < nc; i++) {
+            ConWork& C = cw[c0 + i];
+            int lv = 0;
+            if (!is_static[C.a]) lv = max(lv, bw[C.a].last_level + 1);
+            if (!is_static[C.b]) lv = max(lv, bw[C.b].last_level + 1);
+            C.level = lv;
+            if (!is_static[C.a]) bw[C.a].last_level = lv;
+            if (!is_static[C.b]) bw[C.b].last_level = lv;
+            levels = max(levels, lv + 1);
+        }
+        for (int l = 0; l <= levels; l++) wave_off[c0 + k + l] = 0;
+        for (int i = 0; i < nc; i++) wave_off[c0 + k + cw[c0 + i].level + 1]++;
+        for (int l = 0; l < levels; l++) wave_off[c0 + k + l + 1] += wave_off[c0 + k + l];
+        // stable scatter: contacts of each wave in sorted order
+        int32_t* cursor = wave_cursor + c0 + k;
+        for (int l = 0; l < levels; l++) cursor[l] = wave_off[c0 + k + l];
+        for (int i = 0; i < nc; i++) wave_idx[c0 + cursor[cw[c0 + i].level]++] = i;
+        s_levels = levels;
+    }
+    __syncthreads();
+    const int levels = s_levels;
+    const int* woff = wave_off + c0 + k;
+    const int* widx = wave_idx + c0;
+
+    // Static impulse sums: add the contacts' deltas in sorted order.
+    auto static_sum = [&]() {
+        for (int i = p0 + tid; i < p1; i += nt) {
+            const int g = cl_parts[i];
+            if (!is_static[g]) continue;
+            V3 s = ld3(static_imp + 3 * (size_t)i);
+            for (int j = 0; j < nc; j++) {
+                const ConWork& C = cw[c0 + j];
+                if (C.a == g || C.b == g) s = s + ld3(C.static_delta);
+            }
+            st3(static_imp + 3 * (size_t)i, s);
+        }
+    };
+
+    // ---- warm-start impulses (:193-215), in waves
+    for (int l = 0; l < levels; l++) {
+        for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
+            ConWork& C = cw[c0 + widx[q]];
+            BodyWork &A = bw[C.a], &B = bw[C.b];
+            const V3 n = ld3(C.n);
+            const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
+            const V3 u = (-n) * C.impulse;
+            V3 sd = mk(0, 0, 0);
+            if (!is_static[C.a]) {
+                st3(A.imp, ld3(A.imp) + u);
+                st3(A.rimp, ld3(A.rimp) + calc_torque(u, p1A, ld3(A.FS + 8)));
+            } else {
+                sd = u;
+            }
+            if (!is_static[C.b]) {
+                st3(B.imp, ld3(B.imp) - u);
+                st3(B.rimp, ld3(B.rimp) + calc_torque(-u, p1B, ld3(B.FS + 8)));
+            } else {
+                sd = -u;
+            }
+            st3(C.static_delta, sd);
+        }
+        __syncthreads();
+    }
+    static_sum();
+    __syncthreads();
+    for (int i = p0 + tid; i < p1; i += nt) {
+        const int g = cl_parts[i];
+        if (!is_static[g]) integrate_body(bw[g], fut + 14 * (size_t)g, mass[g], t);
+    }
+    __syncthreads();
+
+    int it_n = 0, it_f = 0;
+    if (nc > 0) {
+        // ---- normal loop (:230-395)
+        bool converged = false;
+        while (!converged && it_n < 1000) {
+            for (int i = p0 + tid; i < p1; i += nt) {
+                const int g = cl_parts[i];
+                double* li = is_static[g] ? nullptr : bw[g].last_imp;
+                if (li)
+                    for (int q = 0; q < 3; q++) li[q] = bw[g].imp[q];
+            }
+            // static bodies keep their running sums in static_imp; remember them
+            __syncthreads();
+            for (int l = 0; l < levels; l++) {
+                for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
+                    ConWork& C = cw[c0 + widx[q]];
+                    BodyWork &A = bw[C.a], &B = bw[C.b];
+                    const bool sa = is_static[C.a], sb = is_static[C.b];
+                    const V3 n = ld3(C.n);
+                    const double outer = C.outer;
+                    const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
+                    const double d1 = dot(p1B, n) - dot(p1A, n);
+                    const V3 xA = ld3(A.FS + 8), xB = ld3(B.FS + 8);
+                    const V3 v1A = ld3(A.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.a, ld3(A.FS + 5)), p1A - xA);
+                    const V3 v1B = ld3(B.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.b, ld3(B.FS + 5)), p1B - xB);
+                    const double v1 = dot(v1A, n) - dot(v1B, n);
+                    const double m = C.mass_eff;
+                    const double damp = 0.1;
+                    const double dimp = d1 < outer ? (v1 * m) * damp : -C.impulse;
+                    const double last_mag = C.impulse;
+                    C.impulse = dmax(C.impulse + dimp, 0.0);
+                    const double upd = C.impulse - last_mag;
+                    const V3 u = (-n) * upd;
+                    V3 sd = mk(0, 0, 0);
+                    if (!sa) {
+                        st3(A.imp, ld3(A.imp) + u);
+                        st3(A.rimp, ld3(A.rimp) + calc_torque(u, p1A, xA));
+                    } else {
+                        sd = u;
+                    }
+                    if (!sb) {
+                        st3(B.imp, ld3(B.imp) - u);
+                        st3(B.rimp, ld3(B.rimp) + calc_torque(-u, p1B, xB));
+                    } else {
+                        sd = -u;
+                    }
+                    st3(C.static_delta, sd);
+                    const double lower_slop = dmax(outer * 0.2, outer - C.start_dist);
+                    const double slop = lerp1(lower_slop, outer * 0.2, 0.3);
+                    const double pen = outer - d1;
+                    const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -C.impulse_offset;
+                    const double last_off = C.impulse_offset;
+                    C.impulse_offset = dmax(C.impulse_offset + doff, 0.0);
+                    const V3 uo = (-n) * (C.impulse_offset - last_off);
+                    if (!sa) st3(A.ioff, ld3(A.ioff) + uo);
+                    if (!sb) st3(B.ioff, ld3(B.ioff) - uo);
+                    if (!sa) integrate_body(A, fut + 14 * (size_t)C.a, mass[C.a], t);
+                    if (!sb) integrate_body(B, fut + 14 * (size_t)C.b, mass[C.b], t);
+                }
+                __syncthreads();
+            }
+            // convergence over every particle of the cluster (:380-387)
+            bool moved = false;
+            for (int i = p0 + tid; i < p1; i += nt) {
+                const int g = cl_parts[i];
+                if (is_static[g]) {
+                    const V3 before = ld3(static_imp + 3 * (size_t)i);
+                    V3 s = before;
+                    for (int j = 0; j < nc; j++) {
+                        const ConWork& C = cw[c0 + j];
+                        if (C.a == g || C.b == g) s = s + ld3(C.static_delta);
+                    }
+                    st3(static_imp + 3 * (size_t)i, s);
+                    if (norm(s - before) > 1e-6) moved = true;
+                } else {
+                    if (norm(ld3(bw[g].imp) - ld3(bw[g].last_imp)) > 1e-6) moved = true;
+                }
+            }
+            converged = !block_any(moved);
+            it_n++;
+        }
+        // ---- friction loop (:397-607)
+        converged = false;
+        while (!converged && it_f < 100) {
+            for (int i = tid; i < nc; i += nt) {  // pass 1: every contact reads, none writes bodies
+                ConWork& C = cw[c0 + i];
+                const BodyWork &A = bw[C.a], &B = bw[C.b];
+                const bool sa = is_static[C.a], sb = is_static[C.b];
+                const double* h = rec + 14 * (size_t)order[c0 + i];
+                const V3 n = ld3(C.n);
+                const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
+                const V3 v1A = sa ? mk(0, 0, 0)
+                                  : ld3(A.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.a, ld3(A.FS + 5)), p1A - ld3(A.FS + 8));
+                const V3 v1B = sb ? mk(0, 0, 0)
+                                  : ld3(B.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.b, ld3(B.FS + 5)), p1B - ld3(B.FS + 8));
+                const V3 lpA = xf12(ld3(C.local_A), A.T_cur), fpA = xf12(ld3(C.local_A), A.T_FSf);
+                const V3 vdA = (fpA - lpA) / t;
+                const V3 lpB = xf12(ld3(C.local_B), B.T_cur), fpB = xf12(ld3(C.local_B), B.T_FSf);
+                const V3 vdB = (fpB - lpB) / t;
+                const V3 vAB = v1A - v1B;
+                const V3 vABd = vdA - vdB;
+                const V3 vt = vAB - dot(vAB, n) * n;
+                (void)vABd;
+                const double mu_ = dmin(mu[C.a], mu[C.b]);
+                const double max_force = (C.impulse * mu_) * 10;
+                const V3 rA = ld3(h) - ld3(fut + 14 * (size_t)C.a + 8);
+                const V3 rB = ld3(h + 3) - ld3(fut + 14 * (size_t)C.b + 8);
+                const V3 tan = normalized(vt);
+                double kt = 0.0;
+                if (!sa) kt += 1.0 / mass[C.a] + quad_form(cross(rA, tan), ii + 9 * (size_t)C.a);
+                if (!sb) kt += 1.0 / mass[C.b] + quad_form(cross(rB, tan), ii + 9 * (size_t)C.b);
+                const double mit = kt < 1e-6 ? 0.0 : 1.0 / kt;
+                const V3 dfi = ((-vt) * mit) * 0.9;
+                V3 total = ld3(C.last_fi) + dfi;
+                total = normalized(total) * dclamp(norm(total), 0.0, max_force);
+                st3(C.upd_total, total);
+            }
+            __syncthreads();
+            bool big = false;
+            for (int l = 0; l < levels; l++) {  // pass 2: ordered accumulation
+                for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
+                    ConWork& C = cw[c0 + widx[q]];
+                    BodyWork &A = bw[C.a], &B = bw[C.b];
+                    const bool sa = is_static[C.a], sb = is_static[C.b];
+                    const double cnt = (double)C.pair_cnt;
+                    const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
+                    const V3 u = (ld3(C.upd_total) - ld3(C.last_fi)) / cnt;
+                    st3(C.last_fi, ld3(C.upd_total));
+                    V3 sd = mk(0, 0, 0);
+                    if (!sa)
+                        st3(A.imp, ld3(A.imp) + u);
+                    else
+                        sd = u;
+                    if (!sb)
+                        st3(B.imp, ld3(B.imp) - u);
+                    else
+                        sd = -u;
+                    st3(C.static_delta, sd);
+                    if (norm(u) > 1e-4) big = true;
+                    const V3 rfA = calc_torque(ld3(C.last_fi), p1A, ld3(A.FS + 8));
+                    const V3 rfB = calc_torque(-ld3(C.last_fi), p1B, ld3(B.FS + 8));
+                    if (!sa) st3(A.rimp, ld3(A.rimp) - ld3(C.last_rot_A));
+                    if (!sb) st3(B.rimp, ld3(B.rimp) - ld3(C.last_rot_B));
+                    st3(C.last_rot_A, rfA);
+                    st3(C.last_rot_B, rfB);
+                    if (!sa) st3(A.rimp, ld3(A.rimp) + rfA);
+                    if (!sb) st3(B.rimp, ld3(B.rimp) + rfB);
+                    const V3 uo = (mk(0, 0, 0) - mk(0, 0, 0)) / cnt;
+                    if (!sa) st3(A.ioff, ld3(A.ioff) + uo);
+                    if (!sb) st3(B.ioff, ld3(B.ioff) - uo);
+                    if (norm(uo) > 1e-4) big = true;
+                    if (!sa) st3(A.roff, ld3(A.roff) + calc_torque(uo, p1A, ld3(A.FS + 8)));
+                    if (!sb) st3(B.roff, ld3(B.roff) + calc_torque(-uo, p1B, ld3(B.FS + 8)));
+                }
+                __syncthreads();
+            }
+            // (the static bodies' impulse sums are read only by the normal loop's test)
+            for (int i = p0 + tid; i < p1; i += nt) {
+                const int g = cl_parts[i];
+                if (!is_static[g]) integrate_body(bw[g], fut + 14 * (size_t)g, mass[g], t);
+            }
+            converged = !block_any(big);
+            it_f++;
+        }
+    }
+    __syncthreads();
+    // ---- write back (:622-624) and the contacts' impulses for the warm start
+    for (int i = p0 + tid; i < p1; i += nt) {
+        const int g = cl_parts[i];
+        if (!is_static[g])
+            for (int q = 0; q < 14; q++) fut[14 * (size_t)g + q] = bw[g].FS[q];
+    }
+    for (int i = tid; i < nc; i += nt) {
+        out_impulse[c0 + i] = cw[c0 + i].impulse;
+        out_ab[2 * (c0 + i)] = cw[c0 + i].a;
+        out_ab[2 * (c0 + i) + 1] = cw[c0 + i].b;
+    }
+    if (tid == 0) {
+        status[k] = 0;
+        iters[2 * k] = it_n;
+        iters[2 * k + 1] = it_f;
+        // Warm-start store (sequential_impulses_warm_start.cpp:28-54): each
+        // body pair keeps the impulse of its last contact in sorted order;
+        // a pair's first contact enters as 0.0 + impulse.
+        if (pair_warm)
+            for (int i = 0; i < nc; i++) {
+                const int oi = order[c0 + i];
+                pair_warm[con_pair[oi]] = pair_cnt[oi] == 1 ? 0.0 + cw[c0 + i].impulse : cw[c0 + i].impulse;
+            }
+    }
+}
+
+// Sort key of Contact::operator< (contact.h:17-21) as orderable bits
+// (proportions are >= +0).
+__global__ void k_prop_keys(int n, const double* __restrict__ rec, unsigned long long* __restrict__ keys,
+                            int32_t* __restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* h = rec + 14 * (size_t)i;
+    const double prop = norm(mk(h[0] - h[3], h[1] - h[4], h[2] - h[5])) / (h[6] + h[7]);
+    keys[i] = (unsigned long long)__double_as_longlong(prop);
+    vals[i] = i;
+}
+
+#define VLAUNCH(kern, n, ...)                                        \
+    do {                                                             \
+        kern<<<nblocks(n), kBlock, 0, ctx->stream>>>(__VA_ARGS__);   \
+        ctx->eng.launches++;                                         \
+    } while (0)
+#define RC(x)                          \
+    do {                               \
+        if (int rc_ = (x)) return rc_; \
+    } while (0)
+
+}  // namespace
+
+// Per-pair filterContacts of contact records grouped by pair (d_rec /
+// d_off over n_pairs), into flt (records) / flt_off / flt_cnt (kept per pair).
+int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pairs, int n_rec, double margin,
+               int* n_out) {
+    Engine& E = ctx->eng;
+    RC(E.flt_idx.ensure(n_rec + 1));
+    RC(E.flt_keep.ensure(n_rec + 1));
+    RC(E.flt_cnt.ensure(n_pairs + 1));
+    RC(E.flt_off.ensure(n_pairs + 1));
+    if (n_pairs > 0)
+        VLAUNCH(k_filter, n_pairs, n_pairs, d_off, d_rec, E.flt_idx.p, E.flt_keep.p, E.flt_cnt.p, margin);
+    // exclusive scan of the kept counts
+    D2G_CUDA(cudaMemsetAsync(E.flt_off.p, 0, sizeof(int32_t), ctx->stream));
+    if (n_pairs > 0) {
+        size_t bytes = 0;
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, E.flt_cnt.p, E.flt_off.p + 1, n_pairs, ctx->stream));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, E.flt_cnt.p, E.flt_off.p + 1, n_pairs, ctx->stream));
+    }
+    D2G_CUDA(cudaMemcpyAsync(ctx->h_pinned, E.flt_off.p + n_pairs, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    D2G_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int n = ctx->h_pinned[0];
+    RC(E.flt.ensure(14 * (size_t)n + 14));
+    if (n_pairs > 0)
+        VLAUNCH(k_filter_write, n_pairs, n_pairs, d_off, E.flt_idx.p, E.flt_keep.p, E.flt_off.p, d_rec, E.flt.p);
+    *n_out = n;
+    D2G_CUDA(cudaGetLastError());
+    return D2G_OK;
+}
+
+// Solve clusters.  Contacts (14-double records in the reference's hit order,
+// clusters contiguous per d_con_off) with per-contact pair counts and warm
+// values (NaN = none).  Outputs: status / iteration counts per cluster, the
+// final impulse and body pair of each contact in sorted order.
+int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts, int n_parts,
+              const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
+              const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
+              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm) {
+    Engine& E = ctx->eng;
+    cudaStream_t s = ctx->stream;
+    RC(E.sv_keys.ensure(n_con + 1));
+    RC(E.sv_keys_out.ensure(n_con + 1));
+    RC(E.sv_vals.ensure(n_con + 1));
+    RC(E.sv_order.ensure(n_con + 1));
+    RC(E.sv_bw_raw.ensure(sizeof(BodyWork) * ((size_t)ctx->n_bodies + 1)));
+    RC(E.sv_cw_raw.ensure(sizeof(ConWork) * ((size_t)n_con + 1)));
+    BodyWork* bw = (BodyWork*)E.sv_bw_raw.p;
+    ConWork* cw = (ConWork*)E.sv_cw_raw.p;
+    RC(E.sv_wave_idx.ensure(n_con + 1));
+    RC(E.sv_wave_off.ensure(n_con + n_clusters + 2));
+    RC(E.sv_wave_cursor.ensure(n_con + n_clusters + 2));
+    RC(E.sv_static_imp.ensure(3 * (size_t)n_parts + 3));
+    if (n_con > 0) {
+        VLAUNCH(k_prop_keys, n_con, n_con, d_rec, E.sv_keys.p, E.sv_vals.p);
+        size_t bytes = 0;
+        D2G_CUDA(cub::DeviceSegmentedRadixSort::SortPairs(nullptr, bytes, E.sv_keys.p, E.sv_keys_out.p, E.sv_vals.p,
+                                                          E.sv_order.p, n_con, n_clusters, d_con_off, d_con_off + 1,
+                                                          0, 64, s));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceSegmentedRadixSort::SortPairs(E.cub_tmp.p, bytes, E.sv_keys.p, E.sv_keys_out.p,
+                                                          E.sv_vals.p, E.sv_order.p, n_con, n_clusters, d_con_off,
+                                                          d_con_off + 1, 0, 64, s));
+    }
+    if (n_clusters > 0) {
+        k_solve<<<n_clusters, kSolveBlock, 0, s>>>(
+            n_clusters, d_part_off, d_parts, d_con_off, E.sv_order.p, d_rec, d_pair_cnt, d_warm, d_step,
+            ctx->is_static.p, ctx->mass.p, ctx->inv_inertia.p, ctx->mu.p, ctx->cur.p, ctx->fut.p, gravity_z,
+            bw, cw, E.sv_wave_idx.p, E.sv_wave_off.p, E.sv_wave_cursor.p, E.sv_static_imp.p, d_status, d_iters,
+            d_out_impulse, d_out_ab, d_con_pair, d_pair_warm);
+        ctx->eng.launches++;
+    }
+    D2G_CUDA(cudaGetLastError());
+    return D2G_OK;
+}
+
+}  // namespace d2g

@@ -1,0 +1,707 @@
+// The adaptive cluster stepper with every cluster's work batched on the GPU.
+//
+// Restates BroadPhaseEmbreeCluster::step and stepRecursive
+// (strategies/broad_phase/broad_phase_embree_cluster.cpp:16-257),
+// separateCollisionClusters (collision_detection/separate_clusters.cpp:
+// 355-459), PDEExplicit::step (strategies/PDE/PDE_explicit.cpp:30-142) and
+// PDEStrategy::stepSleeping (PDE_strategy.cpp:11-15).
+//
+// The reference steps clusters one after another.  Clusters share no moving
+// body, and the warm-start store is keyed by body pair, so their steps are
+// independent; here every cluster advances in the same launches:
+//   * the host runs the broad phase over the states copied back once per
+//     outer step, labels the clusters and schedules;
+//   * one CCD launch sequence selects every cluster's step
+//     (d2g_step.cu run_select_steps);
+//   * stepRecursive runs as one state machine per cluster on the host; each
+//     round batches the PDE steps of all clusters that need one (narrow
+//     phase, contact filter, sequential-impulse solve, state shift) and the
+//     bookkeeping between steps runs as per-cluster op lists on the device.
+// Static bodies are the one state clusters share.  The reference's
+// sequential order decides three of their fields, reproduced here on the
+// host: last_dt and sleeping come from the last PDE step (in cluster order)
+// of a cluster holding the body, and the current time advances once per
+// sleeping cluster holding it, in cluster order.
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "d2g_geom.cuh"
+#include "d2g_internal.hpp"
+
+namespace d2g {
+
+int broad_phase_pairs(const d2g_bodies* b, const float* local_aabb, std::vector<int32_t>& out);
+int run_gather_f64(d2g_ctx* ctx, int n, const int32_t* d_idx, const double* d_src, double* d_dst);
+int run_con_off(d2g_ctx* ctx, int n, const int32_t* d_pair_off, const int32_t* d_flt_off, int32_t* d_con_off);
+int run_expand_contacts(d2g_ctx* ctx, int n_pairs, const int32_t* d_off, const double* d_pwarm,
+                        const int32_t* d_pcnt, double* d_warm, int32_t* d_cnt, int32_t* d_pair);
+
+namespace {
+
+#define RC(x)                          \
+    do {                               \
+        if (int rc_ = (x)) return rc_; \
+    } while (0)
+
+constexpr int kMaxDepth = 60;  // stepRecursive's depth guard (the reference has none)
+
+template <class T>
+struct Pinned {
+    T* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n) {
+        if (n <= cap) return D2G_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        const size_t c = n + n / 2 + 64;
+        cudaError_t e = cudaMallocHost((void**)&p, c * sizeof(T));
+        if (e != cudaSuccess) {
+            cap = 0;
+            set_error(std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+            return D2G_ERR_CUDA;
+        }
+        cap = c;
+        return D2G_OK;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// Packs host arrays into one pinned staging area and one device buffer with
+// a single copy.  The staging area is rewritten only after the stream has
+// been synchronised past the previous copy (the callers sync once per round).
+template <class T>
+struct Packer {
+    Pinned<T> stage;
+    DBuf<T> dev;
+    std::vector<T> host;
+    std::vector<size_t> offs;
+    void clear() {
+        host.clear();
+        offs.clear();
+    }
+    int add(const T* v, size_t n) {
+        offs.push_back(host.size());
+        host.insert(host.end(), v, v + n);
+        // keep each array 16-byte aligned on the device
+        while ((host.size() * sizeof(T)) % 16) host.push_back(T());
+        return (int)offs.size() - 1;
+    }
+    int add(const std::vector<T>& v) { return add(v.data(), v.size()); }
+    int upload(cudaStream_t s) {
+        const size_t n = host.size() + 1;
+        RC(stage.ensure(n));
+        RC(dev.ensure(n));
+        if (!host.empty()) memcpy(stage.p, host.data(), host.size() * sizeof(T));
+        D2G_CUDA(cudaMemcpyAsync(dev.p, stage.p, host.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        return D2G_OK;
+    }
+    T* ptr(int id) { return dev.p + offs[id]; }
+    void release() {
+        stage.release();
+        dev.release();
+    }
+};
+
+struct HostCluster {
+    std::vector<int32_t> parts;  // component members ascending, then static bodies by first interaction
+    std::vector<int32_t> pairs;  // interactions (a, b), broad-phase order
+    double mct = 0.0, step = 0.0;
+    bool sleeping = true;
+    int n_dyn = 0;
+};
+
+struct Frame {
+    int depth = 0, phase = 0;
+};
+
+struct Machine {
+    std::vector<Frame> stack;
+    std::vector<int4> ops;
+    bool need_pde = false;
+    double last_step = 0.0;  // step of its latest PDE step
+    int last_sleep = 0;      // will_sleep of its latest successful PDE step
+};
+
+}  // namespace
+
+struct WorldState {
+    std::vector<float> local_aabb;
+    float opt_dt = 0.01f;
+    double gravity_z = -9.8;
+    std::map<std::pair<int, int>, double> warm;
+    int64_t stats[13] = {0};
+    // host mirrors of the device states, refreshed once per outer step
+    Pinned<double> h_last, h_cur, h_fut, h_last_dt;
+    Pinned<uint8_t> h_sleeping;
+    Pinned<double> h_rd;
+    Pinned<int32_t> h_ri;
+    Packer<int32_t> pk_round, pk_batch, pk_cl;
+    Packer<double> pk_round_d, pk_warm;
+    Packer<int4> pk_ops;
+    DBuf<double> cl_step, cl_tmin, frame_start, stash, step_a, tmin_a, con_warm, pair_warm, con_imp, sel_out;
+    DBuf<int32_t> err, status, iters, will_sleep, con_cnt, con_pair, con_off, con_ab;
+    size_t stash_used = 0;
+};
+
+void world_free(WorldState* w) {
+    if (!w) return;
+    w->h_last.release();
+    w->h_cur.release();
+    w->h_fut.release();
+    w->h_last_dt.release();
+    w->h_sleeping.release();
+    w->h_rd.release();
+    w->h_ri.release();
+    w->pk_round.release();
+    w->pk_batch.release();
+    w->pk_cl.release();
+    w->pk_round_d.release();
+    w->pk_warm.release();
+    w->pk_ops.release();
+    for (DBuf<double>* b : {&w->cl_step, &w->cl_tmin, &w->frame_start, &w->stash, &w->step_a, &w->tmin_a,
+                            &w->con_warm, &w->pair_warm, &w->con_imp, &w->sel_out})
+        b->release();
+    for (DBuf<int32_t>* b : {&w->err, &w->status, &w->iters, &w->will_sleep, &w->con_cnt, &w->con_pair,
+                             &w->con_off, &w->con_ab})
+        b->release();
+    delete w;
+}
+
+namespace {
+
+// Reads the device error flag (after the stream has been synchronised).
+int check_err(d2g_ctx* c, WorldState& W, const char* where) {
+    D2G_CUDA(cudaMemcpyAsync(W.h_ri.p, W.err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    if (W.h_ri.p[0]) {
+        set_error(std::string("invalid state interpolation in ") + where + " (the reference throws here)");
+        return D2G_ERR_STATE;
+    }
+    return D2G_OK;
+}
+
+// One batched PDEExplicit::step over the clusters R[a] for a in `act`.
+int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, const std::vector<int>& R,
+              const std::vector<int>& act, std::vector<Machine>& M, std::vector<int>& ok_out) {
+    cudaStream_t s = c->stream;
+    Engine& E = c->eng;
+    const int nA = (int)act.size();
+    std::vector<int32_t> a_idx(nA), part_off(nA + 1, 0), parts, pairs, pair_off(nA + 1, 0);
+    for (int b = 0; b < nA; b++) {
+        const HostCluster& h = cls[R[act[b]]];
+        a_idx[b] = act[b];
+        parts.insert(parts.end(), h.parts.begin(), h.parts.end());
+        pairs.insert(pairs.end(), h.pairs.begin(), h.pairs.end());
+        part_off[b + 1] = (int32_t)parts.size();
+        pair_off[b + 1] = (int32_t)(pairs.size() / 2);
+    }
+    const int n_pairs = (int)(pairs.size() / 2);
+    W.pk_batch.clear();
+    const int i_idx = W.pk_batch.add(a_idx), i_poff = W.pk_batch.add(part_off), i_parts = W.pk_batch.add(parts),
+              i_pairs = W.pk_batch.add(pairs), i_pairoff = W.pk_batch.add(pair_off);
+    RC(W.pk_batch.upload(s));
+    RC(W.step_a.ensure(nA + 1));
+    RC(W.tmin_a.ensure(nA + 1));
+    RC(run_gather_f64(c, nA, W.pk_batch.ptr(i_idx), W.cl_step.p, W.step_a.p));
+    RC(run_gather_f64(c, nA, W.pk_batch.ptr(i_idx), W.cl_tmin.p, W.tmin_a.p));
+    RC(run_pde_prepare(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), W.step_a.p, W.tmin_a.p, W.err.p));
+    int n_rec = 0;
+    int64_t cnt[4] = {0, 0, 0, 0};
+    RC(run_narrowphase(c, W.pk_batch.ptr(i_pairs), n_pairs, &n_rec, cnt));
+    int n_kept = 0;
+    RC(run_filter(c, E.out_off.p, E.rec_sorted.p, n_pairs, n_rec, 0.0, &n_kept));
+    // warm-start values per interaction (sequential_impulses_warm_start.cpp:11-26)
+    std::vector<double> pwarm(n_pairs + 1, std::numeric_limits<double>::quiet_NaN());
+    for (int p = 0; p < n_pairs; p++) {
+        auto f = W.warm.find(std::make_pair(pairs[2 * p], pairs[2 * p + 1]));
+        if (f != W.warm.end()) pwarm[p] = f->second;
+    }
+    W.pk_warm.clear();
+    const int i_w = W.pk_warm.add(pwarm);
+    RC(W.pk_warm.upload(s));
+    RC(W.con_warm.ensure(n_kept + 1));
+    RC(W.con_cnt.ensure(n_kept + 1));
+    RC(W.con_pair.ensure(n_kept + 1));
+    RC(W.con_off.ensure(nA + 1));
+    RC(W.con_imp.ensure(n_kept + 1));
+    RC(W.con_ab.ensure(2 * (size_t)n_kept + 2));
+    RC(W.pair_warm.ensure(n_pairs + 1));
+    RC(W.status.ensure(nA + 1));
+    RC(W.iters.ensure(2 * (size_t)nA + 2));
+    RC(W.will_sleep.ensure(nA + 1));
+    RC(run_expand_contacts(c, n_pairs, E.flt_off.p, W.pk_warm.ptr(i_w), E.flt_cnt.p, W.con_warm.p, W.con_cnt.p,
+                           W.con_pair.p));
+    RC(run_con_off(c, nA, W.pk_batch.ptr(i_pairoff), E.flt_off.p, W.con_off.p));
+    RC(run_solve(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), (int)parts.size(), W.con_off.p, n_kept,
+                 E.flt.p, W.con_cnt.p, W.con_warm.p, W.step_a.p, W.gravity_z, W.status.p, W.iters.p, W.con_imp.p,
+                 W.con_ab.p, W.con_pair.p, W.pair_warm.p));
+    RC(run_pde_finish(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), W.step_a.p, W.status.p,
+                      W.will_sleep.p));
+    // results back: status, iterations, will_sleep, kept counts (int); step, pair warm (double)
+    const size_t ni = (size_t)nA * 4 + n_pairs + 1;
+    RC(W.h_ri.ensure(ni + 1));
+    RC(W.h_rd.ensure((size_t)nA + n_pairs + 1));
+    int32_t* hi = W.h_ri.p + 1;
+    D2G_CUDA(cudaMemcpyAsync(hi, W.status.p, nA * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(hi + nA, W.iters.p, 2 * nA * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(hi + 3 * nA, W.will_sleep.p, nA * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (n_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(hi + 4 * nA, E.flt_cnt.p, n_pairs * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(W.h_rd.p, W.step_a.p, nA * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (n_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(W.h_rd.p + nA, W.pair_warm.p, n_pairs * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RC(check_err(c, W, "PDEExplicit::step"));
+    hi = W.h_ri.p + 1;
+    // statistics (PDE_explicit.cpp:77-101)
+    W.stats[2] += n_pairs;
+    W.stats[3] += n_kept;
+    W.stats[4] += nA;
+    W.stats[11] += cnt[0];
+    W.stats[12] += cnt[1];
+    ok_out.assign(nA, 0);
+    for (int b = 0; b < nA; b++) {
+        Machine& m = M[act[b]];
+        m.last_step = W.h_rd.p[b];
+        const bool ok = hi[b] == 0;
+        ok_out[b] = ok ? 1 : 0;
+        if (!ok) {
+            W.stats[5]++;
+            continue;
+        }
+        W.stats[6] += hi[nA + 2 * b];
+        W.stats[7] += hi[nA + 2 * b + 1];
+        m.last_sleep = hi[3 * nA + b];
+        for (int p = pair_off[b]; p < pair_off[b + 1]; p++)
+            if (hi[4 * nA + p] > 0) W.warm[std::make_pair(pairs[2 * p], pairs[2 * p + 1])] = W.h_rd.p[nA + p];
+    }
+    return D2G_OK;
+}
+
+// stepRecursive as a state machine.  Frame slots: frame_start[depth * nR + r];
+// stash of a frame: depth * total_dyn + dyn_base[r] (in states).
+struct Recursion {
+    int nR = 0, total_dyn = 0;
+    std::vector<int> dyn_base;
+    int slot(int r, int depth) const { return depth * nR + r; }
+    int stash_off(int r, int depth) const { return depth * total_dyn + dyn_base[r]; }
+};
+
+int enter_frame(Machine& m, const Recursion& Rc, int r, int depth) {
+    if (depth > kMaxDepth) {
+        set_error("stepRecursive exceeded depth " + std::to_string(kMaxDepth));
+        return D2G_ERR_STATE;
+    }
+    Frame f;
+    f.depth = depth;
+    f.phase = 0;
+    m.stack.push_back(f);
+    m.ops.push_back(make_int4(D2G_OP_ENTER, Rc.slot(r, depth), 0, 0));
+    m.need_pde = true;
+    return D2G_OK;
+}
+
+int ensure_stash(d2g_ctx* c, WorldState& W, const Recursion& Rc, int depth) {
+    const size_t need = 14 * (size_t)(depth + 1) * Rc.total_dyn;
+    if (need > W.stash_used) {
+        RC(W.stash.ensure_keep(need, W.stash_used, c->stream));
+        W.stash_used = need;
+    }
+    return D2G_OK;
+}
+
+// Advances cluster r after its PDE step (ok) until it needs another or ends.
+int advance(d2g_ctx* c, WorldState& W, const Recursion& Rc, Machine& m, int r, bool ok) {
+    m.need_pde = false;
+    if (!ok) {  // :42-65 roll back to the midpoint and recurse
+        const int d = m.stack.back().depth;
+        m.ops.push_back(make_int4(D2G_OP_SPLIT, 0, 0, 0));
+        return enter_frame(m, Rc, r, d + 1);
+    }
+    for (;;) {  // the frame on top has finished
+        const Frame f = m.stack.back();
+        m.ops.push_back(make_int4(D2G_OP_EXIT, Rc.slot(r, f.depth), 0, 0));
+        m.stack.pop_back();
+        if (m.stack.empty()) return D2G_OK;
+        Frame& p = m.stack.back();
+        p.phase++;
+        if (p.phase == 1) {  // :67-85 second half, first part
+            RC(ensure_stash(c, W, Rc, p.depth));
+            m.ops.push_back(make_int4(D2G_OP_SAVE, Rc.slot(r, p.depth), Rc.stash_off(r, p.depth), 0));
+            return enter_frame(m, Rc, r, p.depth + 1);
+        }
+        if (p.phase == 2) {  // :87-93 second half, second part
+            m.ops.push_back(make_int4(D2G_OP_MID, Rc.slot(r, p.depth), 0, 0));
+            return enter_frame(m, Rc, r, p.depth + 1);
+        }
+        // :95-107 restore the first half's end as the last state
+        m.ops.push_back(make_int4(D2G_OP_RESTORE, Rc.slot(r, p.depth), Rc.stash_off(r, p.depth), 0));
+    }
+}
+
+int flush_ops(d2g_ctx* c, WorldState& W, std::vector<Machine>& M, const int32_t* d_part_off,
+              const int32_t* d_parts) {
+    std::vector<int32_t> idx, off(1, 0);
+    std::vector<int4> ops;
+    for (int r = 0; r < (int)M.size(); r++) {
+        if (M[r].ops.empty()) continue;
+        idx.push_back(r);
+        ops.insert(ops.end(), M[r].ops.begin(), M[r].ops.end());
+        off.push_back((int32_t)ops.size());
+        M[r].ops.clear();
+    }
+    if (idx.empty()) return D2G_OK;
+    W.pk_cl.clear();
+    const int i_idx = W.pk_cl.add(idx), i_off = W.pk_cl.add(off);
+    RC(W.pk_cl.upload(c->stream));
+    W.pk_ops.clear();
+    const int i_ops = W.pk_ops.add(ops);
+    RC(W.pk_ops.upload(c->stream));
+    return run_cluster_ops(c, (int)idx.size(), W.pk_cl.ptr(i_idx), W.pk_cl.ptr(i_off), W.pk_ops.ptr(i_ops), d_part_off,
+                           d_parts, W.cl_step.p, W.cl_tmin.p, W.frame_start.p, W.stash.p, W.err.p);
+}
+
+int world_step_once(d2g_ctx* c, WorldState& W) {
+    const int n = c->n_bodies;
+    cudaStream_t s = c->stream;
+    const double opt_dt = (double)W.opt_dt;
+    D2G_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int32_t), s));
+    // :126-132 every body: last_dt doubles (capped), future projected
+    RC(run_outer_project(c, opt_dt));
+    D2G_CUDA(cudaMemcpyAsync(W.h_last.p, c->last.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(W.h_cur.p, c->cur.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(W.h_fut.p, c->fut.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(W.h_last_dt.p, c->last_dt.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(W.h_sleeping.p, c->sleeping.p, (size_t)n, cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaStreamSynchronize(s));
+    const uint8_t* is_static = c->h_is_static.data();
+    // :134 broad phase
+    d2g_bodies hb;
+    memset(&hb, 0, sizeof(hb));
+    hb.n = n;
+    hb.is_static = is_static;
+    hb.geo_eps = c->h_geo_eps.data();
+    hb.last = W.h_last.p;
+    hb.cur = W.h_cur.p;
+    hb.fut = W.h_fut.p;
+    hb.last_dt = W.h_last_dt.p;
+    hb.bounding_radius = c->h_bounding_radius.data();
+    std::vector<int32_t> B;
+    RC(broad_phase_pairs(&hb, W.local_aabb.data(), B));
+    const int nb = (int)(B.size() / 2);
+    // :136 separateCollisionClusters: components over moving-moving pairs
+    std::vector<int32_t> deg(n + 1, 0), adj;
+    for (int e = 0; e < nb; e++)
+        if (!is_static[B[2 * e]] && !is_static[B[2 * e + 1]]) {
+            deg[B[2 * e] + 1]++;
+            deg[B[2 * e + 1] + 1]++;
+        }
+    for (int i = 0; i < n; i++) deg[i + 1] += deg[i];
+    adj.assign(deg[n], 0);
+    {
+        std::vector<int32_t> fill(deg.begin(), deg.end() - 1);
+        for (int e = 0; e < nb; e++) {
+            const int a = B[2 * e], b = B[2 * e + 1];
+            if (is_static[a] || is_static[b]) continue;
+            adj[fill[a]++] = b;
+            adj[fill[b]++] = a;
+        }
+    }
+    std::vector<int32_t> comp(n, -1), queue;
+    queue.reserve(n);
+    int n_comp = 0;
+    for (int st = 0; st < n; st++) {
+        if (comp[st] >= 0) continue;
+        comp[st] = n_comp;
+        queue.clear();
+        queue.push_back(st);
+        for (size_t h = 0; h < queue.size(); h++)
+            for (int q = deg[queue[h]]; q < deg[queue[h] + 1]; q++)
+                if (comp[adj[q]] < 0) {
+                    comp[adj[q]] = n_comp;
+                    queue.push_back(adj[q]);
+                }
+        n_comp++;
+    }
+    // clusters with a moving body, in label order (static singletons dropped)
+    std::vector<int32_t> cl_of(n_comp, -1);
+    std::vector<HostCluster> cls;
+    for (int p = 0; p < n; p++) {
+        if (is_static[p]) continue;
+        if (cl_of[comp[p]] < 0) {
+            cl_of[comp[p]] = 0;  // mark
+        }
+    }
+    {
+        int k = 0;
+        for (int q = 0; q < n_comp; q++)
+            if (cl_of[q] == 0) cl_of[q] = k++;
+        cls.resize(k);
+    }
+    for (HostCluster& h : cls) {
+        h.mct = std::numeric_limits<double>::infinity();
+        h.step = std::numeric_limits<double>::infinity();
+        h.sleeping = true;
+    }
+    for (int p = 0; p < n; p++) {
+        if (is_static[p]) continue;
+        HostCluster& h = cls[cl_of[comp[p]]];
+        h.parts.push_back(p);
+        h.n_dyn++;
+        h.mct = dmin(h.mct, W.h_cur.p[14 * (size_t)p]);
+        h.step = dmin(h.step, W.h_last_dt.p[p]);
+        if (!W.h_sleeping.p[p]) h.sleeping = false;
+    }
+    for (int e = 0; e < nb; e++) {
+        const int a = B[2 * e], b = B[2 * e + 1];
+        if (is_static[a] && is_static[b]) continue;
+        const int dyn = is_static[a] ? b : a;
+        HostCluster& h = cls[cl_of[comp[dyn]]];
+        if (is_static[a] || is_static[b]) {
+            const int st = is_static[a] ? a : b;
+            bool in = false;
+            for (size_t q = h.n_dyn; q < h.parts.size(); q++) in = in || h.parts[q] == st;
+            if (!in) h.parts.push_back(st);
+        }
+        h.pairs.push_back(a);
+        h.pairs.push_back(b);
+    }
+    // :445-456 roll every moving body back to its cluster's minimum time
+    {
+        std::vector<double> t_body(n, -1.0);
+        for (const HostCluster& h : cls)
+            for (int q = 0; q < h.n_dyn; q++) t_body[h.parts[q]] = h.mct;
+        W.pk_round_d.clear();
+        const int i_t = W.pk_round_d.add(t_body);
+        RC(W.pk_round_d.upload(s));
+        RC(run_rollback(c, W.pk_round_d.ptr(i_t), W.err.p));
+        RC(check_err(c, W, "separateCollisionClusters"));
+    }
+    const int nc = (int)cls.size();
+    // :139-147 the earliest end of any cluster's step
+    double min_final = std::numeric_limits<double>::infinity();
+    for (const HostCluster& h : cls) min_final = dmin(min_final, h.mct + h.step);
+    // :149-170 time-step selection for the awake clusters that start in time
+    std::vector<int> sel;
+    for (int k = 0; k < nc; k++)
+        if (!(cls[k].mct > min_final) && !cls[k].sleeping) sel.push_back(k);
+    if (!sel.empty()) {
+        std::vector<int32_t> pairs, pair_off(1, 0), part_off(1, 0), parts;
+        for (int k : sel) {
+            pairs.insert(pairs.end(), cls[k].pairs.begin(), cls[k].pairs.end());
+            parts.insert(parts.end(), cls[k].parts.begin(), cls[k].parts.end());
+            pair_off.push_back((int32_t)(pairs.size() / 2));
+            part_off.push_back((int32_t)parts.size());
+        }
+        W.pk_round.clear();
+        const int i_pairs = W.pk_round.add(pairs), i_pairoff = W.pk_round.add(pair_off),
+                  i_partoff = W.pk_round.add(part_off), i_parts = W.pk_round.add(parts);
+        RC(W.pk_round.upload(s));
+        RC(W.sel_out.ensure(sel.size() + 1));
+        int64_t cnt[4] = {0, 0, 0, 0};
+        int n_ccd = 0;
+        RC(run_select_steps(c, W.pk_round.ptr(i_pairs), (int)(pairs.size() / 2), W.pk_round.ptr(i_pairoff),
+                            W.pk_round.ptr(i_partoff), W.pk_round.ptr(i_parts), (int)sel.size(), opt_dt, W.sel_out.p,
+                            cnt, &n_ccd));
+        RC(W.h_rd.ensure(sel.size() + 1));
+        D2G_CUDA(cudaMemcpyAsync(W.h_rd.p, W.sel_out.p, sel.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        D2G_CUDA(cudaStreamSynchronize(s));
+        for (size_t q = 0; q < sel.size(); q++) cls[sel[q]].step = W.h_rd.p[q];
+        W.stats[0] += (int64_t)(pairs.size() / 2);
+        W.stats[1] += n_ccd;
+        W.stats[8] += cnt[0];
+        W.stats[9] += cnt[1];
+        W.stats[10] += cnt[2];
+    }
+    double fine_min_final = std::numeric_limits<double>::infinity();
+    for (int k = 0; k < nc; k++) {
+        if (cls[k].mct > min_final) continue;
+        fine_min_final = dmin(fine_min_final, cls[k].mct + (cls[k].sleeping ? opt_dt : cls[k].step));
+    }
+    // :172-255 the clusters that start before the earliest end step
+    std::vector<int> sleepers, R;
+    for (int k = 0; k < nc; k++) {
+        if (cls[k].mct > fine_min_final) continue;
+        (cls[k].sleeping ? sleepers : R).push_back(k);
+    }
+    std::vector<double> static_time(n, 0.0);
+    std::vector<uint8_t> static_touched(n, 0);
+    if (!sleepers.empty()) {
+        std::vector<int32_t> part_off(1, 0), parts;
+        std::vector<double> steps;
+        for (int k : sleepers) {
+            parts.insert(parts.end(), cls[k].parts.begin(), cls[k].parts.end());
+            part_off.push_back((int32_t)parts.size());
+            steps.push_back(cls[k].step);
+            for (size_t q = cls[k].n_dyn; q < cls[k].parts.size(); q++) {
+                const int st = cls[k].parts[q];
+                if (!static_touched[st]) static_time[st] = W.h_cur.p[14 * (size_t)st];
+                static_touched[st] = 1;
+                static_time[st] = static_time[st] + cls[k].step;
+            }
+        }
+        W.pk_round.clear();
+        const int i_off = W.pk_round.add(part_off), i_parts = W.pk_round.add(parts);
+        RC(W.pk_round.upload(s));
+        W.pk_round_d.clear();
+        const int i_st = W.pk_round_d.add(steps);
+        RC(W.pk_round_d.upload(s));
+        RC(run_sleep_apply(c, (int)sleepers.size(), W.pk_round.ptr(i_off), W.pk_round.ptr(i_parts),
+                           W.pk_round_d.ptr(i_st)));
+        D2G_CUDA(cudaStreamSynchronize(s));
+    }
+    if (!R.empty()) {
+        const int nR = (int)R.size();
+        Recursion Rc;
+        Rc.nR = nR;
+        Rc.dyn_base.resize(nR);
+        std::vector<int32_t> part_off(1, 0), parts;
+        std::vector<double> step0(nR), tmin0(nR);
+        for (int r = 0; r < nR; r++) {
+            const HostCluster& h = cls[R[r]];
+            Rc.dyn_base[r] = Rc.total_dyn;
+            Rc.total_dyn += h.n_dyn;
+            parts.insert(parts.end(), h.parts.begin(), h.parts.end());
+            part_off.push_back((int32_t)parts.size());
+            step0[r] = h.step;
+            tmin0[r] = h.mct;
+        }
+        W.pk_round.clear();
+        const int i_off = W.pk_round.add(part_off), i_parts = W.pk_round.add(parts);
+        RC(W.pk_round.upload(s));
+        RC(W.cl_step.ensure(nR + 1));
+        RC(W.cl_tmin.ensure(nR + 1));
+        RC(W.frame_start.ensure((size_t)(kMaxDepth + 2) * nR + 1));
+        D2G_CUDA(cudaMemcpyAsync(W.cl_step.p, step0.data(), nR * sizeof(double), cudaMemcpyHostToDevice, s));
+        D2G_CUDA(cudaMemcpyAsync(W.cl_tmin.p, tmin0.data(), nR * sizeof(double), cudaMemcpyHostToDevice, s));
+        W.stash_used = 0;
+        std::vector<Machine> M(nR);
+        for (int r = 0; r < nR; r++) RC(enter_frame(M[r], Rc, r, 0));
+        std::vector<int> act, ok;
+        for (;;) {
+            act.clear();
+            for (int r = 0; r < nR; r++)
+                if (M[r].need_pde) act.push_back(r);
+            if (act.empty()) break;
+            RC(flush_ops(c, W, M, W.pk_round.ptr(i_off), W.pk_round.ptr(i_parts)));
+            RC(pde_round(c, W, cls, R, act, M, ok));
+            for (size_t q = 0; q < act.size(); q++) RC(advance(c, W, Rc, M[act[q]], act[q], ok[q] != 0));
+        }
+        RC(flush_ops(c, W, M, W.pk_round.ptr(i_off), W.pk_round.ptr(i_parts)));
+        RC(check_err(c, W, "stepRecursive"));
+        // static bodies: last_dt and sleeping of the last stepped cluster holding them
+        std::vector<int> last_r(n, -1);
+        for (int r = 0; r < nR; r++) {
+            const HostCluster& h = cls[R[r]];
+            for (size_t q = h.n_dyn; q < h.parts.size(); q++) last_r[h.parts[q]] = r;
+        }
+        for (int g = 0; g < n; g++) {
+            if (last_r[g] < 0) continue;
+            W.h_last_dt.p[g] = M[last_r[g]].last_step;
+            W.h_sleeping.p[g] = (uint8_t)(M[last_r[g]].last_sleep ? 1 : 0);
+            D2G_CUDA(cudaMemcpyAsync(c->last_dt.p + g, W.h_last_dt.p + g, sizeof(double), cudaMemcpyHostToDevice, s));
+            D2G_CUDA(cudaMemcpyAsync(c->sleeping.p + g, W.h_sleeping.p + g, 1, cudaMemcpyHostToDevice, s));
+        }
+    }
+    // static bodies of sleeping clusters: the clock advanced, future = current
+    for (int g = 0; g < n; g++) {
+        if (!static_touched[g]) continue;
+        double* cur = W.h_cur.p + 14 * (size_t)g;
+        cur[0] = static_time[g];
+        D2G_CUDA(cudaMemcpyAsync(c->cur.p + 14 * (size_t)g, cur, 14 * sizeof(double), cudaMemcpyHostToDevice, s));
+        D2G_CUDA(cudaMemcpyAsync(c->fut.p + 14 * (size_t)g, cur, 14 * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    D2G_CUDA(cudaStreamSynchronize(s));
+    return D2G_OK;
+}
+
+}  // namespace
+}  // namespace d2g
+
+using namespace d2g;
+
+extern "C" int d2g_world_configure(d2g_ctx* c, const float* local_aabb, float opt_dt, double gravity_z) {
+    if (!c || !local_aabb || !(opt_dt > 0.0f)) {
+        set_error("invalid world configuration");
+        return D2G_ERR_INVALID;
+    }
+    if (c->n_bodies <= 0 || c->n_meshes <= 0) {
+        set_error("set trees and bodies before configuring the world");
+        return D2G_ERR_STATE;
+    }
+    if ((int)c->h_bounding_radius.size() != c->n_bodies) {
+        set_error("the world stepper needs the bodies' bounding radii");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    if (!c->world) c->world = new WorldState();
+    WorldState& W = *c->world;
+    const int n = c->n_bodies;
+    W.local_aabb.assign(local_aabb, local_aabb + 6 * (size_t)n);
+    W.opt_dt = opt_dt;
+    W.gravity_z = gravity_z;
+    W.warm.clear();
+    for (int64_t& v : W.stats) v = 0;
+    RC(W.h_last.ensure(14 * (size_t)n));
+    RC(W.h_cur.ensure(14 * (size_t)n));
+    RC(W.h_fut.ensure(14 * (size_t)n));
+    RC(W.h_last_dt.ensure(n));
+    RC(W.h_sleeping.ensure(n));
+    RC(W.h_ri.ensure(64));
+    RC(W.h_rd.ensure(64));
+    RC(W.err.ensure(4));
+    return D2G_OK;
+}
+
+extern "C" int d2g_world_step(d2g_ctx* c, int32_t n_steps) {
+    if (!c || n_steps < 0) {
+        set_error("invalid arguments");
+        return D2G_ERR_INVALID;
+    }
+    if (!c->world || (int)(c->world->local_aabb.size() / 6) != c->n_bodies) {
+        set_error("configure the world (d2g_world_configure) after setting the bodies");
+        return D2G_ERR_STATE;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    for (int i = 0; i < n_steps; i++) RC(world_step_once(c, *c->world));
+    return D2G_OK;
+}
+
+extern "C" int d2g_world_stats(d2g_ctx* c, int64_t* out13) {
+    if (!c || !out13 || !c->world) {
+        set_error("no world configured");
+        return D2G_ERR_STATE;
+    }
+    for (int i = 0; i < 13; i++) out13[i] = c->world->stats[i];
+    return D2G_OK;
+}
+
+extern "C" int d2g_world_warm(d2g_ctx* c, int32_t* keys, double* vals, int32_t capacity, int32_t* n) {
+    if (!c || !n || !c->world) {
+        set_error("no world configured");
+        return D2G_ERR_STATE;
+    }
+    const auto& m = c->world->warm;
+    *n = (int32_t)m.size();
+    int i = 0;
+    if (keys && vals)
+        for (const auto& kv : m) {
+            if (i >= capacity) break;
+            keys[2 * i] = kv.first.first;
+            keys[2 * i + 1] = kv.first.second;
+            vals[i] = kv.second;
+            i++;
+        }
+    if (keys && vals && (int)m.size() > capacity) {
+        set_error("warm-start capacity too small");
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
+}

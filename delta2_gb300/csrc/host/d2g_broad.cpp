@@ -8,7 +8,6 @@
 // both grown by geo_eps), an inclusive overlap test, then the swept
 // bounding-sphere first-contact time within max(last_dt).  Embree reports
 // pairs in a thread-dependent order; here they come in ascending (i, j).
-// All-pairs box tests: scenes of the benchmark sizes take a few ms.
 #include <algorithm>
 #include <limits>
 #include <string>
@@ -73,6 +72,72 @@ FBox bounds(const d2g_bodies* b, const float* aabb, int i) {
     return r;
 }
 }  // namespace
+
+// Candidate pairs as (i, j), i < j, ascending.  Boxes are swept along x in
+// order of their lower x bound (ties by index); every pair whose boxes
+// overlap on all three axes is then filtered exactly as the all-pairs loop
+// does, so the pair set is the same.  Returns D2G_ERR_STATE when a state
+// interpolation is invalid (the reference throws there).
+int broad_phase_pairs(const d2g_bodies* b, const float* local_aabb, std::vector<int32_t>& out) {
+    out.clear();
+    const int n = b->n;
+    std::vector<FBox> box(n);
+    std::vector<int32_t> order;
+    order.reserve(n);
+    for (int i = 0; i < n; i++) {
+        box[i] = bounds(b, local_aabb, i);
+        bool finite = true;
+        for (int k = 0; k < 3; k++) finite = finite && box[i].lo[k] == box[i].lo[k] && box[i].hi[k] == box[i].hi[k];
+        if (finite) order.push_back(i);  // a NaN box overlaps nothing
+    }
+    std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return box[x].lo[0] < box[y].lo[0] || (box[x].lo[0] == box[y].lo[0] && x < y);
+    });
+    std::vector<std::pair<int32_t, int32_t>> cand;
+    for (size_t u = 0; u < order.size(); u++) {
+        const int p = order[u];
+        for (size_t v = u + 1; v < order.size(); v++) {
+            const int q = order[v];
+            if (box[q].lo[0] > box[p].hi[0]) break;
+            const int i = p < q ? p : q, j = p < q ? q : p;
+            if (b->is_static[i] && b->is_static[j]) continue;
+            bool ov = true;
+            for (int k = 0; k < 3; k++) ov = ov && box[i].lo[k] <= box[j].hi[k] && box[j].lo[k] <= box[i].hi[k];
+            if (ov) cand.emplace_back(i, j);
+        }
+    }
+    std::sort(cand.begin(), cand.end());
+    for (const auto& c : cand) {
+        const int i = c.first, j = c.second;
+        State as = load_state(b->cur + 14 * (size_t)i), bs = load_state(b->cur + 14 * (size_t)j);
+        if (!b->is_static[i] && !b->is_static[j]) {
+            const State al = load_state(b->last + 14 * (size_t)i), bl = load_state(b->last + 14 * (size_t)j);
+            State o;
+            if (as.time < bs.time) {
+                if (!interpolate(bs, bl, as.time, o)) {
+                    set_error("invalid state interpolation in the broad phase (bodies " + std::to_string(i) + ", " +
+                              std::to_string(j) + ")");
+                    return D2G_ERR_STATE;
+                }
+                bs = o;
+            } else {
+                if (!interpolate(as, al, bs.time, o)) {
+                    set_error("invalid state interpolation in the broad phase (bodies " + std::to_string(i) + ", " +
+                              std::to_string(j) + ")");
+                    return D2G_ERR_STATE;
+                }
+                as = o;
+            }
+        }
+        const double t = sphere_sphere_first_intersect(as.x, as.v, b->bounding_radius[i] + b->geo_eps[i], bs.x, bs.v,
+                                                       b->bounding_radius[j] + b->geo_eps[j]);
+        if (t >= 0.0 && t < dmax(b->last_dt[i], b->last_dt[j])) {
+            out.push_back(i);
+            out.push_back(j);
+        }
+    }
+    return D2G_OK;
+}
 }  // namespace d2g
 
 extern "C" int d2g_broad_phase(const d2g_bodies* b, const float* local_aabb, int32_t* pairs, int32_t capacity,
@@ -82,46 +147,16 @@ extern "C" int d2g_broad_phase(const d2g_bodies* b, const float* local_aabb, int
         set_error("invalid broad-phase arguments");
         return D2G_ERR_INVALID;
     }
-    const int n = b->n;
-    std::vector<FBox> box(n);
-    for (int i = 0; i < n; i++) box[i] = bounds(b, local_aabb, i);
-    int cnt = 0;
-    for (int i = 0; i < n; i++) {
-        for (int j = i + 1; j < n; j++) {
-            if (b->is_static[i] && b->is_static[j]) continue;
-            bool ov = true;
-            for (int k = 0; k < 3; k++) ov = ov && box[i].lo[k] <= box[j].hi[k] && box[j].lo[k] <= box[i].hi[k];
-            if (!ov) continue;
-            State as = load_state(b->cur + 14 * (size_t)i), bs = load_state(b->cur + 14 * (size_t)j);
-            if (!b->is_static[i] && !b->is_static[j]) {
-                const State al = load_state(b->last + 14 * (size_t)i), bl = load_state(b->last + 14 * (size_t)j);
-                State o;
-                if (as.time < bs.time) {
-                    if (!interpolate(bs, bl, as.time, o)) {
-                        set_error("invalid interpolation in the broad phase");
-                        return D2G_ERR_INVALID;
-                    }
-                    bs = o;
-                } else {
-                    if (!interpolate(as, al, bs.time, o)) {
-                        set_error("invalid interpolation in the broad phase");
-                        return D2G_ERR_INVALID;
-                    }
-                    as = o;
-                }
-            }
-            const double t = sphere_sphere_first_intersect(as.x, as.v, b->bounding_radius[i] + b->geo_eps[i], bs.x,
-                                                           bs.v, b->bounding_radius[j] + b->geo_eps[j]);
-            if (t >= 0.0 && t < dmax(b->last_dt[i], b->last_dt[j])) {
-                if (pairs && cnt < capacity) {
-                    pairs[2 * cnt] = i;
-                    pairs[2 * cnt + 1] = j;
-                }
-                cnt++;
-            }
-        }
-    }
+    std::vector<int32_t> out;
+    const int rc = broad_phase_pairs(b, local_aabb, out);
+    if (rc) return rc;
+    const int cnt = (int)(out.size() / 2);
     *n_pairs = cnt;
+    if (pairs)
+        for (int k = 0; k < cnt && k < capacity; k++) {
+            pairs[2 * k] = out[2 * k];
+            pairs[2 * k + 1] = out[2 * k + 1];
+        }
     if (pairs && cnt > capacity) {
         set_error("broad-phase pair capacity too small");
         return D2G_CAPACITY;

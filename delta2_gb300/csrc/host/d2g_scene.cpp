@@ -751,6 +751,19 @@ void random_quat(Pcg32& rng, double* q) {
     q[3] = b * m_sin(t3);
 }
 
+// Largest |coordinate| of the mesh's vertices rotated by q (w, x, y, z).
+double max_axis_extent(const Mesh& m, const double* q) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z),     2 * (x * z + w * y),
+                         2 * (x * y + w * z),     1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y),     2 * (y * z + w * x),     1 - 2 * (x * x + y * y)};
+    double e = 0.0;
+    for (size_t v = 0; v + 2 < m.V.size(); v += 3)
+        for (int r = 0; r < 3; r++)
+            e = std::max(e, std::fabs(R[3 * r] * m.V[v] + R[3 * r + 1] * m.V[v + 1] + R[3 * r + 2] * m.V[v + 2]));
+    return e;
+}
+
 // Standard normal by Marsaglia's polar method.
 double normal(Pcg32& rng) {
     for (;;) {
@@ -843,8 +856,15 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
                     mp = shared_mp;
                 }
                 double x[3] = {ix * spacing - cx, iy * spacing - cy, z0 + iz * spacing};
+                // Orientations are uniform, redrawn while the rotated mesh
+                // reaches past half the spacing along a grid axis, where it
+                // could start interpenetrating a neighbour (unit cubes at
+                // 1.5 m spacing can: their half-diagonal is 0.87 m).
                 double q[4];
-                random_quat(rng, q);
+                for (int attempt = 0;; attempt++) {
+                    random_quat(rng, q);
+                    if (attempt >= 1000 || max_axis_extent(m, q) <= 0.5 * spacing) break;
+                }
                 double v[3];
                 for (int k = 0; k < 3; k++) v[k] = sigma * normal(rng);
                 add_body(s, mesh_id, m, mp, false, density, geo_eps, mu, x, q, v, dt);

@@ -169,6 +169,69 @@ int d2g_compare_trees_full_continuous_device(d2g_ctx* ctx, const int32_t* d_pair
                                              int32_t n_pairs, int32_t* n_contacts, const double** d_contacts,
                                              const int32_t** d_offsets, int64_t* counters);
 
+/* --------------------------------------------------- time-step selection --
+ * fineCollisionClustersWithTimeStepSelection followed by the clamp of
+ * TimeStepSelectionDynamicContinuous::selectTimeStep, for many clusters in one
+ * call (collision_detection/separate_clusters.cpp:462-599,
+ * strategies/time_step_size/time_step_selection_dynamic_continuous.cpp:17-21).
+ * Cluster k owns interactions pairs[cluster_pair_off[k] .. cluster_pair_off[k+1])
+ * in the reference's order and particles cluster_particles[cluster_particle_off[k]
+ * .. +1) (its first particle gives the fallback step).  Every interaction runs
+ * a CCD query over min(last_dt_a, last_dt_b) of the device bodies; the device
+ * future states are left as the reference leaves them (each body's last
+ * query).  step_out[k] receives the clamped step in [1e-3, opt_dt].
+ * counters (optional, 4 int64) as for the CCD entry points. */
+int d2g_select_time_steps(d2g_ctx* ctx, const int32_t* pairs, int32_t n_pairs, const int32_t* cluster_pair_off,
+                          const int32_t* cluster_particle_off, const int32_t* cluster_particles, int32_t n_clusters,
+                          float opt_dt, double* step_out, int64_t* counters);
+
+/* ------------------------------------------------------ contact filter --
+ * filterContacts(contacts, margin) for each group of contacts
+ * (collision_detection/contact.h:44-69; called per interaction with margin 0
+ * at strategies/PDE/PDE_explicit.cpp:85): a stable sort by (eps_a + eps_b,
+ * |A - B|), then a contact is kept unless its midpoint lies within
+ * eps_a + eps_b + margin of an already kept contact's midpoint.  Group g is
+ * contacts[offsets[g] .. offsets[g+1]); its kept contacts are
+ * out[out_offsets[g] .. out_offsets[g+1]).  D2G_CAPACITY when more than
+ * capacity contacts are kept (out_offsets still written). */
+int d2g_filter_contacts(d2g_ctx* ctx, const double* contacts, const int32_t* offsets, int32_t n_groups, double margin,
+                        double* out, int32_t capacity, int32_t* out_offsets);
+/* ------------------------------------------------- sequential impulses --
+ * SequentialImpulses::solve (strategies/contact_force/sequential_impulses.cpp:
+ * 104-638) for many clusters in one call, one block per cluster.  Cluster k
+ * has particles particles[particle_off[k] .. +1) (a moving body in one cluster
+ * only), step step[k] and hits contacts[contact_off[k] .. +1) in the
+ * reference's hit order; pair_count[i] is the number of hits of contact i's
+ * body pair in its cluster (the friction split) and warm[i] the warm-start
+ * impulse stored for that pair (NaN when none;
+ * sequential_impulses_warm_start.cpp:11-26).  The device future states of the
+ * cluster's moving bodies are replaced by the solved ones.  Outputs: status[k]
+ * (0 ok, 1 rejected: a hit closer than 1e-6 with step > 1e-4),
+ * iterations[2k..2k+1] (normal, friction), and per hit in the solver's sorted
+ * order its final normal impulse and body pair.  Returns D2G_SOLVE_FAILED when
+ * any cluster was rejected. */
+int d2g_solve_clusters(d2g_ctx* ctx, int32_t n_clusters, const int32_t* particle_off, const int32_t* particles,
+                       const double* step, const double* contacts, const int32_t* contact_off,
+                       const int32_t* pair_count, const double* warm, double gravity_z, int32_t* status,
+                       int32_t* iterations, double* impulse_out, int32_t* pair_out);
+/* ----------------------------------------------- adaptive cluster stepper --
+ * BroadPhaseEmbreeCluster::step (strategies/broad_phase/
+ * broad_phase_embree_cluster.cpp:125-257) with stepRecursive, PDEExplicit::step
+ * and SequentialImpulses over the context's device bodies: the broad phase
+ * and scheduling run on the host, every cluster's time-step selection, narrow
+ * phase, contact filter, solve and state updates run batched on the GPU.
+ * d2g_world_configure takes each body's local mesh box (6 floats: min, max;
+ * Mesh::getAABB) for the static bodies' broad-phase bounds, the option time
+ * step and gravity; it clears the warm-start store and the statistics.
+ * d2g_world_stats: ccd_pairs, ccd_contacts, np_pairs, np_contacts, solves,
+ * failures, normal_iters, friction_iters, ccd_node_pairs, ccd_tri_pairs,
+ * ccd_leaf_pairs, np_node_pairs, np_tri_pairs.  d2g_world_warm lists the
+ * warm-start store in ascending body-pair order.  An invalid state
+ * interpolation (where the reference throws) returns D2G_ERR_STATE. */
+int d2g_world_configure(d2g_ctx* ctx, const float* local_aabb, float opt_dt, double gravity_z);
+int d2g_world_step(d2g_ctx* ctx, int32_t n_steps);
+int d2g_world_stats(d2g_ctx* ctx, int64_t* stats13);
+int d2g_world_warm(d2g_ctx* ctx, int32_t* keys, double* values, int32_t capacity, int32_t* n);
 /* ------------------------------------ allocation-free discrete narrow phase
  * No counterpart in the reference.  The same compareTreesFull traversal and
  * contacts as d2g_compare_trees_full, for callers that may not allocate

@@ -463,7 +463,10 @@ inline FBox body_bounds(const Body& p, const float* local_aabb6) {
     return b;
 }
 
-inline std::vector<std::pair<int, int>> broad_phase(const std::vector<Body>& bodies, const float* local_aabbs) {
+// `ok` (optional) turns false on an invalid interpolation, where the
+// reference's State::interpolate throws (model/state.cpp:56-58).
+inline std::vector<std::pair<int, int>> broad_phase(const std::vector<Body>& bodies, const float* local_aabbs,
+                                                    bool* ok = nullptr) {
     const int n = (int)bodies.size();
     std::vector<FBox> boxes(n);
     for (int i = 0; i < n; i++) boxes[i] = body_bounds(bodies[i], local_aabbs + 6 * (size_t)i);
@@ -478,10 +481,9 @@ inline std::vector<std::pair<int, int>> broad_phase(const std::vector<Body>& bod
             if (!ov) continue;
             State as = a.cur, bs = b.cur;
             if (!a.is_static && !b.is_static) {
-                if (a.cur.time < b.cur.time)
-                    state_interpolate(b.cur, b.last, a.cur.time, bs);
-                else
-                    state_interpolate(a.cur, a.last, b.cur.time, as);
+                const bool good = a.cur.time < b.cur.time ? state_interpolate(b.cur, b.last, a.cur.time, bs)
+                                                          : state_interpolate(a.cur, a.last, b.cur.time, as);
+                if (!good && ok) *ok = false;
             }
             const double t = sphere_sphere_first_intersect(as.x, as.v, a.bounding_radius + a.geo_eps, bs.x, bs.v,
                                                            b.bounding_radius + b.geo_eps);
@@ -697,7 +699,12 @@ inline void world_step(World& w) {
         p.last_dt = dmin(p.last_dt, (double)w.opt_dt);
         p.fut = state_extrapolate(p.cur, p.last_dt, p.ii);
     }
-    const auto B = broad_phase(w.bodies, w.local_aabb.data());
+    bool bp_ok = true;
+    const auto B = broad_phase(w.bodies, w.local_aabb.data(), &bp_ok);
+    if (!bp_ok) {
+        w.error = true;
+        return;
+    }
     std::vector<Cluster> cls;
     if (!separate_clusters(B, w.bodies, cls)) {
         w.error = true;

@@ -1,0 +1,151 @@
+"""The GPU contact filter, sequential-impulse solve and adaptive cluster
+stepper against the oracle, bit for bit: every body state after every outer
+step, the statistics and the warm-start store."""
+import numpy as np
+import pytest
+
+import delta2_gb300 as D
+from oracle import oracle as O
+from tests.clusters import separate
+
+pytestmark = pytest.mark.gpu
+
+BODY_FIELDS = ["last", "cur", "fut", "last_dt", "sleep_steps", "sleeping"]
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_required):
+    from delta2_gb300 import build as B
+    B.build()
+    c = D.Context(0)
+    yield c
+    c.close()
+
+
+def bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint64) if a.dtype == np.float64 else a
+
+
+def assert_bodies_equal(got, ref, where):
+    for f in BODY_FIELDS:
+        g, r = bits(getattr(got, f)), bits(getattr(ref, f))
+        if not np.array_equal(g, r):
+            bad = np.nonzero((g != r).reshape(len(g), -1).any(axis=1))[0]
+            raise AssertionError(f"{where}: field {f} differs for bodies {bad[:10].tolist()}: "
+                                 f"gpu {getattr(got, f)[bad[0]]} oracle {getattr(ref, f)[bad[0]]}")
+
+
+def run_world(ctx, scene, steps):
+    ref = O.World(scene.copy(), scene.opt_dt, scene.gravity_z)
+    gs = scene.copy()
+    ctx.set_scene(gs)
+    ctx.world_configure(gs)
+    for i in range(steps):
+        assert ref.step(1) == 0
+        ctx.world_step(1)
+        assert_bodies_equal(ctx.get_bodies(gs), ref.get_bodies(), f"after step {i + 1}")
+    ref_stats = ref.stats()
+    got_stats = ctx.world_stats()
+    assert got_stats == ref_stats
+    assert {k: np.float64(v).view(np.uint64) for k, v in ctx.world_warm().items()} == \
+        {k: np.float64(v).view(np.uint64) for k, v in ref.warm().items()}
+    return got_stats
+
+
+def test_world_cubes_with_rollbacks(ctx):
+    # 8 cubes falling onto the ground and each other; the solver rejects
+    # steps (rollback and step halving in stepRecursive) from about step 90
+    s = D.make_scene(1, nx=2, ny=2, nz=2)
+    st = run_world(ctx, s, 140)
+    assert st["np_contacts"] > 0 and st["failures"] > 0
+
+
+def test_world_hulls(ctx):
+    s = D.make_scene(2, nx=2, ny=2, nz=1)
+    st = run_world(ctx, s, 110)
+    assert st["np_contacts"] > 0
+
+
+def test_world_sleeping_clusters_share_the_ground(ctx):
+    # Weightless, motionless cubes hovering 0.4 m over the ground: each is a
+    # cluster with the ground (broad-phase pair, no contact), and after 20
+    # stationary steps every cluster sleeps, so the ground's clock advances
+    # once per sleeping cluster.
+    s = D.make_scene(1, nx=2, ny=2, nz=1, spacing=3.0, speed_sigma=0.0, gravity_z=0.0)
+    for arr in (s.last, s.cur, s.fut):
+        arr[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
+        arr[1:, 10] = 0.9
+        arr[1:, 11:14] = 0.0
+        arr[1:, 5:8] = 0.0
+    st = run_world(ctx, s, 30)
+    got = ctx.get_bodies(s.copy())
+    assert got.sleeping[1:].all()
+    assert st["np_contacts"] == 0
+
+
+def test_filter_matches_oracle(ctx):
+    s = D.make_scene(2, nx=3, ny=3, nz=1, spacing=1.25, speed_sigma=0.0)
+    pairs = D.broad_phase(s)
+    ctx.set_scene(s.copy())
+    con, off, _ = ctx.compare_trees_full(pairs)
+    assert len(con) > 0
+    kept, koff = ctx.filter_contacts(con, off)
+    for p in range(len(pairs)):
+        ref = O.filter_contacts(con[off[p]:off[p + 1]])
+        got = kept[koff[p]:koff[p + 1]]
+        assert np.array_equal(bits(got), bits(np.asarray(ref).reshape(-1, 14))), p
+
+
+def test_solve_matches_oracle(ctx):
+    # a state with many contacts: the cube scene after 120 oracle steps
+    s = D.make_scene(1, nx=2, ny=2, nz=2)
+    w = O.World(s.copy(), s.opt_dt, s.gravity_z)
+    w.step(120)
+    base = w.get_bodies().copy()
+    pairs = D.broad_phase(base)
+    clusters = separate(pairs, base.is_static, base.n_bodies)
+    flat = np.array([p for _, inter in clusters for p in inter], dtype=np.int32).reshape(-1, 2)
+    raw, off = O.narrowphase(base, flat)[:2]
+    hits, k = [], 0
+    for parts, inter in clusters:
+        cl = []
+        for _ in inter:
+            f = np.asarray(O.filter_contacts(raw[off[k]:off[k + 1]])).reshape(-1, 14)
+            cl.append(f)
+            k += 1
+        hits.append(np.concatenate(cl) if cl else np.zeros((0, 14)))
+    assert sum(len(h) for h in hits) > 0
+    step = float(np.float32(s.opt_dt))
+    # oracle: one cluster after another, its warm store empty
+    ref_world = O.World(base.copy(), s.opt_dt, s.gravity_z)
+    ref_res = [ref_world.solve(parts, step, h) for (parts, _), h in zip(clusters, hits)]
+    ref_b = ref_world.get_bodies()
+    # GPU: all clusters in one call
+    gs = base.copy()
+    ctx.set_scene(gs)
+    inputs = []
+    for (parts, _), h in zip(clusters, hits):
+        keys = [tuple(sorted((int(r[11]), int(r[12])))) for r in h]
+        cnt = [keys.count(kk) for kk in keys]
+        inputs.append((parts, step, h, cnt, np.full(len(h), np.nan)))
+    status, iters, imps, abs_ = ctx.solve_clusters(inputs, s.gravity_z)
+    got = ctx.get_bodies(gs)
+    for i, (ok, it) in enumerate(ref_res):
+        assert status[i] == (0 if ok else 1)
+        if ok:
+            assert tuple(iters[i]) == tuple(it)
+    assert np.array_equal(bits(got.fut), bits(ref_b.fut))
+    # the warm-start store: last contact of each pair in sorted order
+    warm = {}
+    for imp, ab, ok in zip(imps, abs_, status):
+        if ok != 0:
+            continue
+        seen = {}
+        for x, (a, b) in zip(imp, ab):
+            key = (min(a, b), max(a, b))
+            seen[key] = (x if key in seen else 0.0 + x)
+        warm.update(seen)
+    ref_warm = ref_world.warm()
+    assert {k: np.float64(v).view(np.uint64) for k, v in warm.items()} == \
+        {k: np.float64(v).view(np.uint64) for k, v in ref_warm.items()}
