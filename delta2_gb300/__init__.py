@@ -120,6 +120,10 @@ WORLD_STATS = ["ccd_pairs", "ccd_contacts", "np_pairs", "np_contacts", "solves",
                "friction_iters", "ccd_node_pairs", "ccd_tri_pairs", "ccd_leaf_pairs", "np_node_pairs", "np_tri_pairs"]
 
 
+WORLD_PHASES = ["project", "broad_phase", "clusters", "select", "sleeping", "narrowphase", "filter", "solve",
+                "bookkeeping", "reserved"]
+
+
 class Scene:
     """Flattened trees and bodies (numpy arrays in the C ABI layout)."""
 
@@ -412,6 +416,12 @@ class Context:
         out = np.zeros(13, dtype=np.int64)
         _check(lib().d2g_world_stats(self.h, _p(out, I64P)))
         return dict(zip(WORLD_STATS, out.tolist()))
+
+    def world_timing(self):
+        """Cumulative host wall time (ms) per stepper phase (instrumentation)."""
+        out = np.zeros(10)
+        _check(lib().d2g_world_timing(self.h, _p(out, F64P), 10))
+        return dict(zip(WORLD_PHASES, out.tolist()))
 
     def world_warm(self):
         n = C.c_int32()

@@ -687,6 +687,11 @@ int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
 
 }  // namespace
 
+// Profiling marks for kernels launched outside this file.
+int prof_mark_begin(d2g_ctx* ctx, int kind, long long items) { return prof_begin(ctx, kind, items); }
+void prof_mark_end(d2g_ctx* ctx, int idx) { prof_end(ctx, idx); }
+void prof_mark_collect(d2g_ctx* ctx) { prof_collect(ctx); }
+
 // Launch with an explicit block size.
 #define LAUNCHB(kern, n, block, ...)                                                  \
     do {                                                                              \

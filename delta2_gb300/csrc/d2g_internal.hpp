@@ -194,6 +194,11 @@ struct d2g_ctx {
 };
 
 namespace d2g {
+// Profiling-mode event marks around a kernel (d2g_engine.cu); collect after a
+// stream synchronisation.
+int prof_mark_begin(d2g_ctx* ctx, int kind, long long items);
+void prof_mark_end(d2g_ctx* ctx, int idx);
+void prof_mark_collect(d2g_ctx* ctx);
 // Engine entry points (d2g_engine.cu).
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters);

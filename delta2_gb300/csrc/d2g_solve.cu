@@ -590,11 +590,13 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
                                                           d_con_off + 1, 0, 64, s));
     }
     if (n_clusters > 0) {
+        const int pf = prof_mark_begin(ctx, PROF_SOLVE, n_con);
         k_solve<<<n_clusters, kSolveBlock, 0, s>>>(
             n_clusters, d_part_off, d_parts, d_con_off, E.sv_order.p, d_rec, d_pair_cnt, d_warm, d_step,
             ctx->is_static.p, ctx->mass.p, ctx->inv_inertia.p, ctx->mu.p, ctx->cur.p, ctx->fut.p, gravity_z,
             bw, cw, E.sv_wave_idx.p, E.sv_wave_off.p, E.sv_wave_cursor.p, E.sv_static_imp.p, d_status, d_iters,
             d_out_impulse, d_out_ab, d_con_pair, d_pair_warm);
+        prof_mark_end(ctx, pf);
         ctx->eng.launches++;
     }
     D2G_CUDA(cudaGetLastError());

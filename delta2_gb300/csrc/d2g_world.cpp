@@ -22,6 +22,7 @@
 // host: last_dt and sleeping come from the last PDE step (in cluster order)
 // of a cluster holding the body, and the current time advances once per
 // sleeping cluster holding it, in cluster order.
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -149,6 +150,14 @@ struct WorldState {
     DBuf<double> cl_step, cl_tmin, frame_start, stash, step_a, tmin_a, con_warm, pair_warm, con_imp, sel_out;
     DBuf<int32_t> err, status, iters, will_sleep, con_cnt, con_pair, con_off, con_ab;
     size_t stash_used = 0;
+    // host wall time per phase (instrumentation): see d2g_world_timing
+    double phase_ms[D2G_WORLD_PHASES] = {0};
+    std::chrono::steady_clock::time_point t_mark;
+    void mark(int phase) {
+        const auto now = std::chrono::steady_clock::now();
+        if (phase >= 0) phase_ms[phase] += std::chrono::duration<double, std::milli>(now - t_mark).count();
+        t_mark = now;
+    }
 };
 
 void world_free(WorldState* w) {
@@ -181,6 +190,7 @@ namespace {
 int check_err(d2g_ctx* c, WorldState& W, const char* where) {
     D2G_CUDA(cudaMemcpyAsync(W.h_ri.p, W.err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
     D2G_CUDA(cudaStreamSynchronize(c->stream));
+    prof_mark_collect(c);
     if (W.h_ri.p[0]) {
         set_error(std::string("invalid state interpolation in ") + where + " (the reference throws here)");
         return D2G_ERR_STATE;
@@ -216,6 +226,7 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
     int n_rec = 0;
     int64_t cnt[4] = {0, 0, 0, 0};
     RC(run_narrowphase(c, W.pk_batch.ptr(i_pairs), n_pairs, &n_rec, cnt));
+    W.mark(5);
     int n_kept = 0;
     RC(run_filter(c, E.out_off.p, E.rec_sorted.p, n_pairs, n_rec, 0.0, &n_kept));
     // warm-start values per interaction (sequential_impulses_warm_start.cpp:11-26)
@@ -239,6 +250,7 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
     RC(W.will_sleep.ensure(nA + 1));
     RC(run_expand_contacts(c, n_pairs, E.flt_off.p, W.pk_warm.ptr(i_w), E.flt_cnt.p, W.con_warm.p, W.con_cnt.p,
                            W.con_pair.p));
+    W.mark(6);
     RC(run_con_off(c, nA, W.pk_batch.ptr(i_pairoff), E.flt_off.p, W.con_off.p));
     RC(run_solve(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), (int)parts.size(), W.con_off.p, n_kept,
                  E.flt.p, W.con_cnt.p, W.con_warm.p, W.step_a.p, W.gravity_z, W.status.p, W.iters.p, W.con_imp.p,
@@ -282,6 +294,7 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
         for (int p = pair_off[b]; p < pair_off[b + 1]; p++)
             if (hi[4 * nA + p] > 0) W.warm[std::make_pair(pairs[2 * p], pairs[2 * p + 1])] = W.h_rd.p[nA + p];
     }
+    W.mark(7);
     return D2G_OK;
 }
 
@@ -372,6 +385,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
     const int n = c->n_bodies;
     cudaStream_t s = c->stream;
     const double opt_dt = (double)W.opt_dt;
+    W.mark(-1);
     D2G_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int32_t), s));
     // :126-132 every body: last_dt doubles (capped), future projected
     RC(run_outer_project(c, opt_dt));
@@ -382,6 +396,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
     D2G_CUDA(cudaMemcpyAsync(W.h_sleeping.p, c->sleeping.p, (size_t)n, cudaMemcpyDeviceToHost, s));
     D2G_CUDA(cudaStreamSynchronize(s));
     const uint8_t* is_static = c->h_is_static.data();
+    W.mark(0);
     // :134 broad phase
     d2g_bodies hb;
     memset(&hb, 0, sizeof(hb));
@@ -396,6 +411,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
     std::vector<int32_t> B;
     RC(broad_phase_pairs(&hb, W.local_aabb.data(), B));
     const int nb = (int)(B.size() / 2);
+    W.mark(1);
     // :136 separateCollisionClusters: components over moving-moving pairs
     std::vector<int32_t> deg(n + 1, 0), adj;
     for (int e = 0; e < nb; e++)
@@ -485,6 +501,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         RC(check_err(c, W, "separateCollisionClusters"));
     }
     const int nc = (int)cls.size();
+    W.mark(2);
     // :139-147 the earliest end of any cluster's step
     double min_final = std::numeric_limits<double>::infinity();
     for (const HostCluster& h : cls) min_final = dmin(min_final, h.mct + h.step);
@@ -520,6 +537,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         W.stats[9] += cnt[1];
         W.stats[10] += cnt[2];
     }
+    W.mark(3);
     double fine_min_final = std::numeric_limits<double>::infinity();
     for (int k = 0; k < nc; k++) {
         if (cls[k].mct > min_final) continue;
@@ -557,6 +575,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
                            W.pk_round_d.ptr(i_st)));
         D2G_CUDA(cudaStreamSynchronize(s));
     }
+    W.mark(4);
     if (!R.empty()) {
         const int nR = (int)R.size();
         Recursion Rc;
@@ -590,6 +609,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
             for (int r = 0; r < nR; r++)
                 if (M[r].need_pde) act.push_back(r);
             if (act.empty()) break;
+            W.mark(8);
             RC(flush_ops(c, W, M, W.pk_round.ptr(i_off), W.pk_round.ptr(i_parts)));
             RC(pde_round(c, W, cls, R, act, M, ok));
             for (size_t q = 0; q < act.size(); q++) RC(advance(c, W, Rc, M[act[q]], act[q], ok[q] != 0));
@@ -619,6 +639,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         D2G_CUDA(cudaMemcpyAsync(c->fut.p + 14 * (size_t)g, cur, 14 * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     D2G_CUDA(cudaStreamSynchronize(s));
+    W.mark(8);
     return D2G_OK;
 }
 
@@ -649,6 +670,7 @@ extern "C" int d2g_world_configure(d2g_ctx* c, const float* local_aabb, float op
     W.gravity_z = gravity_z;
     W.warm.clear();
     for (int64_t& v : W.stats) v = 0;
+    for (double& v : W.phase_ms) v = 0.0;
     RC(W.h_last.ensure(14 * (size_t)n));
     RC(W.h_cur.ensure(14 * (size_t)n));
     RC(W.h_fut.ensure(14 * (size_t)n));
@@ -680,6 +702,15 @@ extern "C" int d2g_world_stats(d2g_ctx* c, int64_t* out13) {
         return D2G_ERR_STATE;
     }
     for (int i = 0; i < 13; i++) out13[i] = c->world->stats[i];
+    return D2G_OK;
+}
+
+extern "C" int d2g_world_timing(d2g_ctx* c, double* ms, int32_t n) {
+    if (!c || !ms || !c->world || n < 0) {
+        set_error("no world configured");
+        return D2G_ERR_STATE;
+    }
+    for (int i = 0; i < n && i < D2G_WORLD_PHASES; i++) ms[i] = c->world->phase_ms[i];
     return D2G_OK;
 }
 

@@ -232,6 +232,13 @@ int d2g_world_configure(d2g_ctx* ctx, const float* local_aabb, float opt_dt, dou
 int d2g_world_step(d2g_ctx* ctx, int32_t n_steps);
 int d2g_world_stats(d2g_ctx* ctx, int64_t* stats13);
 int d2g_world_warm(d2g_ctx* ctx, int32_t* keys, double* values, int32_t capacity, int32_t* n);
+/* Instrumentation (no reference counterpart): cumulative host wall time in ms
+ * of the stepper's phases since d2g_world_configure: 0 state projection and
+ * copy back, 1 broad phase, 2 cluster labelling and rollback, 3 time-step
+ * selection (CCD), 4 sleeping clusters, 5 narrow phase, 6 contact filter,
+ * 7 solve and state shift, 8 recursion bookkeeping and static bodies. */
+#define D2G_WORLD_PHASES 10
+int d2g_world_timing(d2g_ctx* ctx, double* ms, int32_t n);
 /* ------------------------------------ allocation-free discrete narrow phase
  * No counterpart in the reference.  The same compareTreesFull traversal and
  * contacts as d2g_compare_trees_full, for callers that may not allocate
