@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -357,6 +359,29 @@ int d2g_ctx_set_trees(d2g_ctx* c, const d2g_trees* t) {
     RC(upload(c, c->tris, t->tris, 72 * (size_t)N));
     RC(upload(c, c->eps, t->eps, 8 * (size_t)N));
     RC(upload(c, c->inner_eps, t->inner_eps, 8 * (size_t)N));
+    {
+        // FP32 bounding spheres of the bucket triangles and eps rounded up,
+        // for the discrete narrow phase's candidate prefilter.
+        std::vector<float4> sph(8 * (size_t)N, make_float4(0.f, 0.f, 0.f, 0.f));
+        std::vector<float> eu(8 * (size_t)N, 0.f);
+        for (size_t k = 0; k < 8 * (size_t)N; k++) {
+            const double* v = t->tris + 9 * k;
+            const double cx = (v[0] + v[3] + v[6]) / 3.0, cy = (v[1] + v[4] + v[7]) / 3.0,
+                         cz = (v[2] + v[5] + v[8]) / 3.0;
+            double r = 0.0;
+            for (int j = 0; j < 3; j++) {
+                const double dx = v[3 * j] - cx, dy = v[3 * j + 1] - cy, dz = v[3 * j + 2] - cz;
+                r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            const float fx = (float)cx, fy = (float)cy, fz = (float)cz;
+            // the FP32 centre moved by at most |c - fc|: add it to the radius
+            const double moved = std::sqrt((cx - fx) * (cx - fx) + (cy - fy) * (cy - fy) + (cz - fz) * (cz - fz));
+            sph[k] = make_float4(fx, fy, fz, std::nextafter((float)(r + moved), INFINITY));
+            eu[k] = std::nextafter((float)t->eps[k], INFINITY);
+        }
+        RC(upload(c, c->tri_sph, sph.data(), sph.size()));
+        RC(upload(c, c->eps_up, eu.data(), eu.size()));
+    }
     D2G_CUDA(cudaStreamSynchronize(c->stream));
     c->n_meshes = t->n_meshes;
     c->n_nodes = N;

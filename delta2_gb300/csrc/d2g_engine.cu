@@ -66,14 +66,20 @@ __global__ void k_ccd_prep(int n, const int32_t* __restrict__ pairs, const doubl
 __global__ void k_np_prep(int n, const int32_t* __restrict__ pairs, const double* __restrict__ fut,
                           const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
                           const double* __restrict__ geo_eps, double* __restrict__ pm, float* __restrict__ search,
-                          Entry* __restrict__ front) {
+                          Entry* __restrict__ front, float* __restrict__ pm32) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int a = pairs[2 * p], b = pairs[2 * p + 1];
     const State fa = load_state(fut + 14 * (size_t)a);
     const State fb = load_state(fut + 14 * (size_t)b);
-    transformation(fa.q, fa.x, pm + 32 * (size_t)p);
-    transformation(fb.q, fb.x, pm + 32 * (size_t)p + 16);
+    double* M = pm + 32 * (size_t)p;
+    transformation(fa.q, fa.x, M);
+    transformation(fb.q, fb.x, M + 16);
+    if (pm32)  // rows 0-2 of both poses in FP32, for the candidate prefilter
+        for (int k = 0; k < 12; k++) {
+            pm32[24 * (size_t)p + k] = (float)M[k];
+            pm32[24 * (size_t)p + 12 + k] = (float)M[16 + k];
+        }
     search[p] = (float)(geo_eps[a] + geo_eps[b]);
     Entry e;
     e.pair = p;
@@ -344,6 +350,65 @@ __global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entr
 // ----------------------------------------------------------- discrete -----
 // All 64 slots of a node pair: triangle distance at the future poses and the
 // hit test dist < float(search) + eps_a + eps_b (comparison_dist.h:223-236).
+// Candidate slots of the discrete narrow phase.  A (node pair, ta, tb) slot
+// can only hit (comparison_dist.h:231-233) when the triangles are closer than
+// thr = search + eps_a + eps_b; their bounding spheres (centroid, radius
+// rounded up) give the lower bound |c_a - c_b| - r_a - r_b on that distance.
+// It is evaluated in FP32 and a slot is dropped only when the bound exceeds
+// thr by a margin (1 mm plus 4e-6 of the magnitudes involved) far above the
+// FP32 rounding of the bound and the FP64 rounding of the exact test, so every
+// slot that hits survives.  Dropped slots produce nothing in the reference
+// either.  One thread per slot; per warp a survivor mask and count.  The valid
+// slots (ta < ntris_a, tb < ntris_b) are counted for the statistics.
+__global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __restrict__ front,
+                                                    const float* __restrict__ pm32, const int32_t* __restrict__ ntris,
+                                                    const float4* __restrict__ sph, const float* __restrict__ eps_up,
+                                                    const float* __restrict__ search, uint32_t* __restrict__ mask,
+                                                    int32_t* __restrict__ cnt, int32_t* __restrict__ tri_pairs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = false, keep = false;
+    if (i < n_slots) {
+        const Entry e = front[i >> 6];
+        const int ta = (i >> 3) & 7, tb = i & 7;
+        valid = ta < ntris[e.na] && tb < ntris[e.nb];
+        if (valid) {
+            const float* A = pm32 + 24 * (size_t)e.pair;
+            const float* B = A + 12;
+            const float4 sa = sph[(size_t)e.na * 8 + ta], sb = sph[(size_t)e.nb * 8 + tb];
+            const float dx = (A[0] * sa.x + A[1] * sa.y + A[2] * sa.z + A[3]) -
+                             (B[0] * sb.x + B[1] * sb.y + B[2] * sb.z + B[3]);
+            const float dy = (A[4] * sa.x + A[5] * sa.y + A[6] * sa.z + A[7]) -
+                             (B[4] * sb.x + B[5] * sb.y + B[6] * sb.z + B[7]);
+            const float dz = (A[8] * sa.x + A[9] * sa.y + A[10] * sa.z + A[11]) -
+                             (B[8] * sb.x + B[9] * sb.y + B[10] * sb.z + B[11]);
+            const float thr = search[e.pair] + eps_up[(size_t)e.na * 8 + ta] + eps_up[(size_t)e.nb * 8 + tb];
+            const float mag = fabsf(A[3]) + fabsf(A[7]) + fabsf(A[11]) + fabsf(B[3]) + fabsf(B[7]) + fabsf(B[11]) +
+                              fabsf(sa.x) + fabsf(sa.y) + fabsf(sa.z) + fabsf(sb.x) + fabsf(sb.y) + fabsf(sb.z) +
+                              sa.w + sb.w + thr;
+            const float lb = sqrtf(dx * dx + dy * dy + dz * dz) - sa.w - sb.w;
+            keep = !(lb > thr + (1e-3f + 4e-6f * mag));  // NaN keeps the slot
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const unsigned v = __ballot_sync(0xffffffffu, valid);
+    if ((threadIdx.x & 31) == 0 && i < n_slots) {
+        mask[i >> 5] = m;
+        cnt[i >> 5] = __popc(m);
+        if (tri_pairs && v) atomicAdd(tri_pairs, __popc(v));  // statistics only
+    }
+}
+
+// Ordered compaction of the surviving slots (slot order = the reference's
+// triangle-pair order within each node pair).
+__global__ void k_np_items(int n_slots, const uint32_t* __restrict__ mask, const int32_t* __restrict__ off,
+                           int32_t* __restrict__ items) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_slots) return;
+    const unsigned m = mask[i >> 5];
+    const int lane = i & 31;
+    if ((m >> lane) & 1u) items[off[i >> 5] + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
 __global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restrict__ front,
                                                const int32_t* __restrict__ pairs, const double* __restrict__ pm,
                                                const int32_t* __restrict__ ntris, const double* __restrict__ tris,
@@ -351,12 +416,19 @@ __global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restr
                                                const double* __restrict__ geo_eps,
                                                const float* __restrict__ search, PrimResult* __restrict__ res,
                                                double* __restrict__ res_eps, int32_t* __restrict__ hit,
-                                               int32_t* __restrict__ entry_hits, int32_t* __restrict__ tri_pairs) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_slots) return;
+                                               int32_t* __restrict__ entry_hits, const int32_t* __restrict__ items,
+                                               const int32_t* __restrict__ n_items) {
+    // Work item k tests slot items[k] (all slots when items is null); results
+    // are stored per item.
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_slots) return;
+    if (n_items && k >= *n_items) {
+        hit[k] = 0;
+        return;
+    }
+    const int i = items ? items[k] : k;
     const Entry e = front[i >> 6];
     const int ta = (i >> 3) & 7, tb = i & 7;
-    if (tri_pairs && (i & 63) == 0) atomicAdd(tri_pairs, ntris[e.na] * ntris[e.nb]);  // statistics only
     int h = 0;
     if (ta < ntris[e.na] && tb < ntris[e.nb]) {
         const double* M = pm + 32 * (size_t)e.pair;
@@ -368,15 +440,15 @@ __global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restr
         h = d < ((double)search[e.pair] + ea) + eb ? 1 : 0;
         if (h) {
             const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
-            put_result(res[i], d, P, Q, 0.0);
-            res_eps[4 * (size_t)i + 0] = geo_eps[a] + ea;
-            res_eps[4 * (size_t)i + 1] = geo_eps[b] + eb;
-            res_eps[4 * (size_t)i + 2] = inner_eps[(size_t)e.na * 8 + ta];
-            res_eps[4 * (size_t)i + 3] = inner_eps[(size_t)e.nb * 8 + tb];
+            put_result(res[k], d, P, Q, 0.0);
+            res_eps[4 * (size_t)k + 0] = geo_eps[a] + ea;
+            res_eps[4 * (size_t)k + 1] = geo_eps[b] + eb;
+            res_eps[4 * (size_t)k + 2] = inner_eps[(size_t)e.na * 8 + ta];
+            res_eps[4 * (size_t)k + 3] = inner_eps[(size_t)e.nb * 8 + tb];
             atomicAdd(&entry_hits[i >> 6], 1);
         }
     }
-    hit[i] = h;
+    hit[k] = h;
 }
 
 // --------------------------------------------------- finals / expansion ----
@@ -838,9 +910,10 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     RC(E.soup.ensure(n_pairs + 1));
     RC(E.np_tri.ensure(1));
     D2G_CUDA(cudaMemsetAsync(E.np_tri.p, 0, sizeof(int32_t), s));
+    RC(E.pm32.ensure(24 * (size_t)n_pairs + 1));
     if (n_pairs > 0)
         LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, ctx->fut.p, ctx->mesh.p, ctx->mesh_node_off.p,
-                                                     ctx->geo_eps.p, E.pm.p, E.search.p, E.soup.p);
+                                                     ctx->geo_eps.p, E.pm.p, E.search.p, E.soup.p, E.pm32.p);
     int n = n_pairs, n_rec = 0;
     DBuf<double>& res_eps = E.pfut;  // reused as the per-slot eps record buffer
     while (n > 0) {
@@ -853,14 +926,23 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
         RC(E.flags.ensure(n_slots));
         RC(E.entry_hits.ensure(n));
         D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n, s));
+        const int n_words = n_slots / 32;
+        RC(E.np_mask.ensure(n_words + 1));
+        RC(E.np_cnt.ensure(n_words + 1));
+        RC(E.np_off.ensure(n_words + 1));
+        RC(E.items.ensure(n_slots + 1));
+        LAUNCH(k_np_mask, n_slots, n_slots, E.soup.p, E.pm32.p, ctx->ntris.p, ctx->tri_sph.p, ctx->eps_up.p,
+               E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p);
+        RC(scan(ctx, E.np_cnt.p, E.np_off.p, n_words));
+        LAUNCH(k_np_items, n_slots, n_slots, E.np_mask.p, E.np_off.p, E.items.p);
         const int pf = prof_begin(ctx, PROF_NP, n_slots);
         LAUNCH(k_np, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
                                                  ctx->eps.p, ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p,
-                                                 res_eps.p, E.hit.p, E.entry_hits.p, E.np_tri.p);
+                                                 res_eps.p, E.hit.p, E.entry_hits.p, E.items.p, E.np_off.p + n_words);
         prof_end(ctx, pf);
-        LAUNCH(k_final_flags, n_slots, n_slots, nullptr, E.soup.p, ctx->nodes.p, E.hit.p,
+        LAUNCH(k_final_flags, n_slots, n_slots, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p,
                                                           E.flags.p);
-        RC(append_records(ctx, n_slots, E.flags.p, nullptr, 6, E.soup.p, nullptr, 0, d_pairs, res_eps.p, n_rec));
+        RC(append_records(ctx, n_slots, E.flags.p, E.items.p, 6, E.soup.p, nullptr, 0, d_pairs, res_eps.p, n_rec));
         RC(E.cnt_a.ensure(n));
         RC(E.cnt_b.ensure(n));
         RC(E.off_a.ensure(n + 1));
@@ -1072,7 +1154,7 @@ extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const 
     }
     if (n_pairs > 0)
         NA_LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, sc->fut, sc->mesh, sc->mesh_node_off, sc->geo_eps, pm, search,
-                  front);
+                  front, nullptr);
     int n = n_pairs, n_rec = 0, level = 0;
     while (n > 0) {
         if (n > MN) {
@@ -1083,7 +1165,7 @@ extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const 
         const int n_slots = 64 * n;
         D2G_CUDA(cudaMemsetAsync(entry_hits, 0, sizeof(int32_t) * n, s));
         NA_LAUNCH(k_np, n_slots, n_slots, front, d_pairs, pm, sc->ntris, sc->tris, sc->eps, sc->inner_eps,
-                  sc->geo_eps, search, res, res_eps, hit, entry_hits, nullptr);
+                  sc->geo_eps, search, res, res_eps, hit, entry_hits, nullptr, nullptr);
         NA_LAUNCH(k_final_flags, n_slots, n_slots, nullptr, front, nodes, hit, flags);
         if (int rc = noalloc_scan(s, tmp, tmp_bytes, flags, flag_off, n_slots)) return rc;
         int32_t tot = 0;

@@ -131,7 +131,13 @@ struct Engine {
     DBuf<double> st_mt, st_new_dt, st_step, st_out;
     DBuf<int32_t> st_has, st_cl_pair_off, st_cl_part_off, st_cl_parts;
     // contact filtering
-    DBuf<int32_t> flt_idx, flt_keep, flt_cnt, flt_off, np_tri;
+    DBuf<int32_t> flt_idx, flt_order, flt_keep, flt_pos, flt_cnt, flt_off, np_tri;
+    DBuf<unsigned long long> flt_keys, flt_keys_s;
+    DBuf<double> flt_mid;
+    // discrete narrow-phase candidates: FP32 poses, survivor masks and offsets
+    DBuf<float> pm32;
+    DBuf<uint32_t> np_mask;
+    DBuf<int32_t> np_cnt, np_off;
     DBuf<double> flt;
     // sequential-impulse solve
     DBuf<unsigned long long> sv_keys, sv_keys_out;
@@ -178,6 +184,8 @@ struct d2g_ctx {
     d2g::DBuf<int32_t> mesh_node_off, ntris;
     d2g::DBuf<int4> nodes;
     d2g::DBuf<double> tris, eps, inner_eps;
+    d2g::DBuf<float4> tri_sph;  // per tree triangle: centroid, bounding radius (rounded up), FP32
+    d2g::DBuf<float> eps_up;    // eps rounded up to FP32
     // bodies
     int n_bodies = 0;
     d2g::DBuf<int32_t> mesh, sleep_steps;

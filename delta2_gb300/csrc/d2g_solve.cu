@@ -28,68 +28,95 @@ constexpr int kSolveBlock = 128;
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
-__device__ __forceinline__ bool contact_less(const double* a, const double* b) {
-    const double a_eps = a[6] + a[7], b_eps = b[6] + b[7];
-    if (a_eps == b_eps) {
-        const V3 da = mk(a[0] - a[3], a[1] - a[4], a[2] - a[5]);
-        const V3 db = mk(b[0] - b[3], b[1] - b[4], b[2] - b[5]);
-        return norm(da) < norm(db);
-    }
-    return a_eps < b_eps;
+// Sort keys of compareContacts (contact.h:32-40): (eps_a + eps_b, |A - B|),
+// both non-negative doubles, whose bit patterns order like the values.
+__global__ void k_filter_keys(int n, const double* __restrict__ rec, unsigned long long* __restrict__ key_norm,
+                              int32_t* __restrict__ idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* c = rec + 14 * (size_t)i;
+    key_norm[i] = (unsigned long long)__double_as_longlong(norm(mk(c[0] - c[3], c[1] - c[4], c[2] - c[5])));
+    idx[i] = i;
 }
 
-// One thread per pair: order (stable) in idx, greedy keep flags in keep.
-__global__ void k_filter(int n_pairs, const int32_t* __restrict__ off, const double* __restrict__ rec,
-                         int32_t* __restrict__ idx, int32_t* __restrict__ keep, int32_t* __restrict__ kept_cnt,
-                         double margin) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs) return;
-    const int c0 = off[p], c1 = off[p + 1];
-    for (int i = c0; i < c1; i++) idx[i] = i;
-    for (int i = c0 + 1; i < c1; i++) {  // stable insertion sort
-        const int v = idx[i];
-        int j = i - 1;
-        while (j >= c0 && contact_less(rec + 14 * (size_t)v, rec + 14 * (size_t)idx[j])) {
-            idx[j + 1] = idx[j];
-            j--;
-        }
-        idx[j + 1] = v;
-    }
-    int kept = 0;
-    for (int i = c0; i < c1; i++) {
-        const double* ct = rec + 14 * (size_t)idx[i];
-        bool new_point = true;
-        for (int j = c0; j < i; j++) {
-            if (!keep[j]) continue;
-            const double* h = rec + 14 * (size_t)idx[j];
-            const V3 ht_mid = mk((ct[0] + ct[3]) / 2, (ct[1] + ct[4]) / 2, (ct[2] + ct[5]) / 2);
-            const V3 h_mid = mk((h[0] + h[3]) / 2, (h[1] + h[4]) / 2, (h[2] + h[5]) / 2);
-            const double dist = norm(ht_mid - h_mid);
-            const double search = (ct[6] + ct[7]) + margin;
-            if (dist < search) {
-                new_point = false;
-                break;
-            }
-        }
-        keep[i] = new_point ? 1 : 0;
-        kept += new_point ? 1 : 0;
-    }
-    kept_cnt[p] = kept;
+__global__ void k_filter_eps_keys(int n, const double* __restrict__ rec, const int32_t* __restrict__ idx,
+                                  unsigned long long* __restrict__ key_eps) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* c = rec + 14 * (size_t)idx[i];
+    key_eps[i] = (unsigned long long)__double_as_longlong(c[6] + c[7]);
 }
 
-__global__ void k_filter_write(int n_pairs, const int32_t* __restrict__ off, const int32_t* __restrict__ idx,
-                               const int32_t* __restrict__ keep, const int32_t* __restrict__ out_off,
-                               const double* __restrict__ rec, double* __restrict__ out) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs) return;
-    int o = out_off[p];
-    for (int i = off[p]; i < off[p + 1]; i++) {
-        if (!keep[i]) continue;
-        const double* s = rec + 14 * (size_t)idx[i];
-        double* d = out + 14 * (size_t)o;
-        for (int k = 0; k < 14; k++) d[k] = s[k];
-        o++;
+// The greedy pass of filterContacts (contact.h:49-66), one warp per body
+// pair over its contacts in sorted order: a contact is kept unless its
+// midpoint lies within eps_a + eps_b + margin (its own) of an already kept
+// contact's midpoint.  Contacts are taken 32 at a time: each lane tests its
+// contact against the pair's kept midpoints, then the chunk is resolved in
+// order (the lowest surviving lane is kept and eliminates the later lanes
+// near it).  kept_mid holds each pair's kept midpoints (from its first slot).
+__global__ void k_filter_dedupe(int n_pairs, const int32_t* __restrict__ off, const int32_t* __restrict__ order,
+                                const double* __restrict__ rec, double margin, int32_t* __restrict__ keep,
+                                int32_t* __restrict__ kept_cnt, double* __restrict__ kept_mid) {
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (warp >= n_pairs) return;  // uniform per warp
+    const int c0 = off[warp], c1 = off[warp + 1];
+    int nk = 0;
+    for (int base = c0; base < c1; base += 32) {
+        const int j = base + lane;
+        const bool in = j < c1;
+        V3 mid = mk(0, 0, 0);
+        double search = 0.0;
+        if (in) {
+            const double* ct = rec + 14 * (size_t)order[j];
+            mid = mk((ct[0] + ct[3]) / 2, (ct[1] + ct[4]) / 2, (ct[2] + ct[5]) / 2);
+            search = (ct[6] + ct[7]) + margin;
+        }
+        bool alive = in;
+        for (int t = 0; t < nk && alive; t++) {
+            const double* h = kept_mid + 3 * (size_t)(c0 + t);
+            if (norm(mid - mk(h[0], h[1], h[2])) < search) alive = false;
+        }
+        unsigned kept = 0;
+        unsigned live = __ballot_sync(0xffffffffu, alive);
+        while (live) {
+            const int src = __ffs(live) - 1;
+            kept |= 1u << src;
+            const V3 h = mk(__shfl_sync(0xffffffffu, mid.x, src), __shfl_sync(0xffffffffu, mid.y, src),
+                            __shfl_sync(0xffffffffu, mid.z, src));
+            if (alive && lane > src && norm(mid - h) < search) alive = false;
+            live = __ballot_sync(0xffffffffu, alive) & ~((2u << src) - 1u);
+        }
+        const bool k = (kept >> lane) & 1u;
+        if (in) keep[j] = k ? 1 : 0;
+        if (k) {
+            double* o = kept_mid + 3 * (size_t)(c0 + nk + __popc(kept & ((1u << lane) - 1u)));
+            o[0] = mid.x;
+            o[1] = mid.y;
+            o[2] = mid.z;
+        }
+        nk += __popc(kept);
+        __syncwarp();
     }
+    if (lane == 0) kept_cnt[warp] = nk;
+}
+
+// Kept contacts, in sorted order per pair, to their scanned positions.
+__global__ void k_filter_write(int n, const int32_t* __restrict__ order, const int32_t* __restrict__ keep,
+                               const int32_t* __restrict__ pos, const double* __restrict__ rec,
+                               double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || !keep[j]) return;
+    const double* s = rec + 14 * (size_t)order[j];
+    double* d = out + 14 * (size_t)pos[j];
+    for (int k = 0; k < 14; k++) d[k] = s[k];
+}
+
+// flt_off[p] = pos[off[p]] for p in [0, n].
+__global__ void k_filter_offsets(int n, const int32_t* __restrict__ off, const int32_t* __restrict__ pos,
+                                 int32_t* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p <= n) out[p] = pos[off[p]];
 }
 
 // ---------------------------------------------------------------- solve ---
@@ -530,28 +557,61 @@ __global__ void k_prop_keys(int n, const double* __restrict__ rec, unsigned long
 int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pairs, int n_rec, double margin,
                int* n_out) {
     Engine& E = ctx->eng;
-    RC(E.flt_idx.ensure(n_rec + 1));
-    RC(E.flt_keep.ensure(n_rec + 1));
+    cudaStream_t s = ctx->stream;
+    const size_t n = (size_t)n_rec;
+    RC(E.flt_keys.ensure(n + 1));
+    RC(E.flt_keys_s.ensure(n + 1));
+    RC(E.flt_idx.ensure(n + 1));
+    RC(E.flt_order.ensure(n + 1));
+    RC(E.flt_keep.ensure(n + 1));
+    RC(E.flt_pos.ensure(n + 1));
+    RC(E.flt_mid.ensure(3 * n + 3));
     RC(E.flt_cnt.ensure(n_pairs + 1));
     RC(E.flt_off.ensure(n_pairs + 1));
-    if (n_pairs > 0)
-        VLAUNCH(k_filter, n_pairs, n_pairs, d_off, d_rec, E.flt_idx.p, E.flt_keep.p, E.flt_cnt.p, margin);
-    // exclusive scan of the kept counts
-    D2G_CUDA(cudaMemsetAsync(E.flt_off.p, 0, sizeof(int32_t), ctx->stream));
-    if (n_pairs > 0) {
+    if (n_rec > 0 && n_pairs > 0) {
+        // stable sort by |A - B|, then stable by eps_a + eps_b: lexicographic, ties in input order
+        VLAUNCH(k_filter_keys, n_rec, n_rec, d_rec, E.flt_keys.p, E.flt_idx.p);
         size_t bytes = 0;
-        D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, E.flt_cnt.p, E.flt_off.p + 1, n_pairs, ctx->stream));
+        D2G_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, E.flt_keys.p, E.flt_keys_s.p, E.flt_idx.p,
+                                                          E.flt_order.p, n_rec, n_pairs, d_off, d_off + 1, s));
         RC(E.cub_tmp.ensure(bytes + 16));
-        D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, E.flt_cnt.p, E.flt_off.p + 1, n_pairs, ctx->stream));
+        D2G_CUDA(cub::DeviceSegmentedSort::StableSortPairs(E.cub_tmp.p, bytes, E.flt_keys.p, E.flt_keys_s.p,
+                                                          E.flt_idx.p, E.flt_order.p, n_rec, n_pairs, d_off,
+                                                          d_off + 1, s));
+        VLAUNCH(k_filter_eps_keys, n_rec, n_rec, d_rec, E.flt_order.p, E.flt_keys.p);
+        bytes = 0;
+        D2G_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, E.flt_keys.p, E.flt_keys_s.p,
+                                                          E.flt_order.p, E.flt_idx.p, n_rec, n_pairs, d_off,
+                                                          d_off + 1, s));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceSegmentedSort::StableSortPairs(E.cub_tmp.p, bytes, E.flt_keys.p, E.flt_keys_s.p,
+                                                          E.flt_order.p, E.flt_idx.p, n_rec, n_pairs, d_off,
+                                                          d_off + 1, s));
+        // E.flt_idx now holds the sorted order
+        k_filter_dedupe<<<nblocks(32LL * n_pairs), kBlock, 0, s>>>(n_pairs, d_off, E.flt_idx.p, d_rec, margin,
+                                                                    E.flt_keep.p, E.flt_cnt.p, E.flt_mid.p);
+        ctx->eng.launches++;
+    } else if (n_pairs > 0) {
+        D2G_CUDA(cudaMemsetAsync(E.flt_cnt.p, 0, sizeof(int32_t) * n_pairs, s));
     }
-    D2G_CUDA(cudaMemcpyAsync(ctx->h_pinned, E.flt_off.p + n_pairs, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                             ctx->stream));
-    D2G_CUDA(cudaStreamSynchronize(ctx->stream));
-    const int n = ctx->h_pinned[0];
-    RC(E.flt.ensure(14 * (size_t)n + 14));
-    if (n_pairs > 0)
-        VLAUNCH(k_filter_write, n_pairs, n_pairs, d_off, E.flt_idx.p, E.flt_keep.p, E.flt_off.p, d_rec, E.flt.p);
-    *n_out = n;
+    RC(E.flt_keep.ensure(n + 1));
+    if (n_rec > 0) {
+        size_t bytes = 0;
+        D2G_CUDA(cudaMemsetAsync(E.flt_pos.p, 0, sizeof(int32_t), s));
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, E.flt_keep.p, E.flt_pos.p + 1, n_rec, s));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, E.flt_keep.p, E.flt_pos.p + 1, n_rec, s));
+        VLAUNCH(k_filter_offsets, n_pairs + 1, n_pairs, d_off, E.flt_pos.p, E.flt_off.p);
+    } else {
+        D2G_CUDA(cudaMemsetAsync(E.flt_off.p, 0, sizeof(int32_t) * (n_pairs + 1), s));
+    }
+    D2G_CUDA(cudaMemcpyAsync(ctx->h_pinned, E.flt_off.p + n_pairs, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaStreamSynchronize(s));
+    prof_mark_collect(ctx);
+    const int kept = ctx->h_pinned[0];
+    RC(E.flt.ensure(14 * (size_t)kept + 14));
+    if (n_rec > 0) VLAUNCH(k_filter_write, n_rec, n_rec, E.flt_idx.p, E.flt_keep.p, E.flt_pos.p, d_rec, E.flt.p);
+    *n_out = kept;
     D2G_CUDA(cudaGetLastError());
     return D2G_OK;
 }
