@@ -24,7 +24,7 @@ namespace d2g {
 namespace {
 
 constexpr int kBlock = 128;
-constexpr int kSolveBlock = 128;
+constexpr int kSolveBlock = 256;
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -152,32 +152,30 @@ __device__ __forceinline__ void rigid12(const State& s, double* T12) {
 }
 __device__ __forceinline__ V3 calc_torque(V3 force, V3 point, V3 com) { return cross(-force, point - com); }
 
-// sequential_impulses.cpp:46-70 updateState and :72-96 updateStateImmediate,
-// with R(fut.q) * ii * R(fut.q)^T precomputed (it only depends on fut).
-__device__ void integrate_body(BodyWork& w, const double* fut, double mass, double t) {
+// sequential_impulses.cpp:46-70 updateState (variant 0, FS) or :72-96
+// updateStateImmediate (variant 1, FSf) of one body, with R(fut.q) * ii *
+// R(fut.q)^T precomputed (it only depends on fut).  Both forms are evaluated
+// and the variant's selected, so lanes integrating different variants do
+// not diverge.
+__device__ void integrate_one(BodyWork& w, const double* fut, double mass, double t, int variant) {
     const State f = load_state(fut);
     const V3 imp = ld3(w.imp), ioff = ld3(w.ioff), rimp = ld3(w.rimp), roff = ld3(w.roff);
     State u = f;
     u.v = f.v + imp / mass;
-    u.x = f.x + (ioff / mass) * t;
+    const V3 xa = f.x + (ioff / mass) * t;
+    const V3 xb = xa + (imp / mass) * t;
+    u.x = variant ? xb : xa;
     u.L = f.L + rimp;
-    {
-        const V3 omega = m3_vec(w.Iinv, f.L + t * roff);
-        u.q = qmul(qexp((0.5 * omega) * t), f.q);
-    }
-    State ui = f;
-    ui.v = f.v + imp / mass;
-    ui.x = (f.x + (ioff / mass) * t) + (imp / mass) * t;
-    ui.L = f.L + rimp;
-    {
-        const V3 omega = m3_vec(w.Iinv, (f.L + t * roff) + t * rimp);
-        ui.q = qmul(qexp((0.5 * omega) * t), f.q);
-    }
-    store_state(w.FS, u);
-    store_state(w.FSf, ui);
-    rigid12(u, w.T_FS);
-    rigid12(ui, w.T_FSf);
+    const V3 La = f.L + t * roff;
+    const V3 Lb = La + t * rimp;
+    const V3 omega = m3_vec(w.Iinv, variant ? Lb : La);
+    u.q = qmul(qexp((0.5 * omega) * t), f.q);
+    store_state(variant ? w.FSf : w.FS, u);
+    rigid12(u, variant ? w.T_FSf : w.T_FS);
 }
+
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ V3 shfl3(V3 v, int src) { return mk(shfl_d(v.x, src), shfl_d(v.y, src), shfl_d(v.z, src)); }
 
 __device__ __forceinline__ V3 xf12(V3 p, const double* T) {
     return mk(((T[0] * p.x + T[1] * p.y) + T[2] * p.z) + T[3] * 1.0,
@@ -330,9 +328,9 @@ __global__ void __launch_bounds__(kSolveBlock)
     }
     static_sum();
     __syncthreads();
-    for (int i = p0 + tid; i < p1; i += nt) {
-        const int g = cl_parts[i];
-        if (!is_static[g]) integrate_body(bw[g], fut + 14 * (size_t)g, mass[g], t);
+    for (int k2 = tid; k2 < 2 * (p1 - p0); k2 += nt) {  // two lanes per body: FS, FSf
+        const int g = cl_parts[p0 + (k2 >> 1)];
+        if (!is_static[g]) integrate_one(bw[g], fut + 14 * (size_t)g, mass[g], t, k2 & 1);
     }
     __syncthreads();
 
@@ -350,50 +348,58 @@ __global__ void __launch_bounds__(kSolveBlock)
             // static bodies keep their running sums in static_imp; remember them
             __syncthreads();
             for (int l = 0; l < levels; l++) {
-                for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
-                    ConWork& C = cw[c0 + widx[q]];
-                    BodyWork &A = bw[C.a], &B = bw[C.b];
+                // Four lanes per contact, one warp instruction stream: lane bit 0
+                // picks the body side (A, B), bit 1 the integrated state (FS,
+                // FSf).  FP64 latency, not lane count, bounds a wave, so the
+                // sides and the four integrations run side by side.
+                const int end4 = 4 * woff[l + 1];
+                for (int base = 4 * woff[l] + (tid & ~31); base < end4; base += nt) {
+                    const int lane = tid & 31, quad = lane & ~3, side = lane & 1, variant = (lane >> 1) & 1;
+                    const int qq = base + lane;
+                    const bool act = qq < end4;
+                    ConWork& C = cw[c0 + widx[act ? (qq >> 2) : woff[l]]];
+                    const int g = side ? C.b : C.a;
+                    BodyWork& W = bw[g];
+                    const bool st = is_static[g];
+                    // this side's contact point and its velocity (State::pointVelocity)
+                    const V3 p1 = xf12(ld3(side ? C.local_B : C.local_A), W.T_FS);
+                    const V3 x = ld3(W.FS + 8);
+                    const V3 v1s = ld3(W.FS + 11) + cross(m3_vec(ii + 9 * (size_t)g, ld3(W.FS + 5)), p1 - x);
+                    const V3 p1A = shfl3(p1, quad), p1B = shfl3(p1, quad + 1);
+                    const V3 v1A = shfl3(v1s, quad), v1B = shfl3(v1s, quad + 1);
                     const bool sa = is_static[C.a], sb = is_static[C.b];
                     const V3 n = ld3(C.n);
                     const double outer = C.outer;
-                    const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
                     const double d1 = dot(p1B, n) - dot(p1A, n);
-                    const V3 xA = ld3(A.FS + 8), xB = ld3(B.FS + 8);
-                    const V3 v1A = ld3(A.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.a, ld3(A.FS + 5)), p1A - xA);
-                    const V3 v1B = ld3(B.FS + 11) + cross(m3_vec(ii + 9 * (size_t)C.b, ld3(B.FS + 5)), p1B - xB);
                     const double v1 = dot(v1A, n) - dot(v1B, n);
                     const double m = C.mass_eff;
                     const double damp = 0.1;
-                    const double dimp = d1 < outer ? (v1 * m) * damp : -C.impulse;
-                    const double last_mag = C.impulse;
-                    C.impulse = dmax(C.impulse + dimp, 0.0);
-                    const double upd = C.impulse - last_mag;
-                    const V3 u = (-n) * upd;
-                    V3 sd = mk(0, 0, 0);
-                    if (!sa) {
-                        st3(A.imp, ld3(A.imp) + u);
-                        st3(A.rimp, ld3(A.rimp) + calc_torque(u, p1A, xA));
-                    } else {
-                        sd = u;
-                    }
-                    if (!sb) {
-                        st3(B.imp, ld3(B.imp) - u);
-                        st3(B.rimp, ld3(B.rimp) + calc_torque(-u, p1B, xB));
-                    } else {
-                        sd = -u;
-                    }
-                    st3(C.static_delta, sd);
+                    const double imp0 = C.impulse, off0 = C.impulse_offset;
+                    const double dimp = d1 < outer ? (v1 * m) * damp : -imp0;
+                    const double imp1 = dmax(imp0 + dimp, 0.0);
+                    const V3 u = (-n) * (imp1 - imp0);
                     const double lower_slop = dmax(outer * 0.2, outer - C.start_dist);
                     const double slop = lerp1(lower_slop, outer * 0.2, 0.3);
                     const double pen = outer - d1;
-                    const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -C.impulse_offset;
-                    const double last_off = C.impulse_offset;
-                    C.impulse_offset = dmax(C.impulse_offset + doff, 0.0);
-                    const V3 uo = (-n) * (C.impulse_offset - last_off);
-                    if (!sa) st3(A.ioff, ld3(A.ioff) + uo);
-                    if (!sb) st3(B.ioff, ld3(B.ioff) - uo);
-                    if (!sa) integrate_body(A, fut + 14 * (size_t)C.a, mass[C.a], t);
-                    if (!sb) integrate_body(B, fut + 14 * (size_t)C.b, mass[C.b], t);
+                    const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -off0;
+                    const double off1 = dmax(off0 + doff, 0.0);
+                    const V3 uo = (-n) * (off1 - off0);
+                    __syncwarp();
+                    if (act && variant == 0) {
+                        if (!st) {  // imp[b] - u is imp[b] + (-u) in IEEE arithmetic
+                            const V3 us = side ? -u : u;
+                            st3(W.imp, ld3(W.imp) + us);
+                            st3(W.rimp, ld3(W.rimp) + calc_torque(us, p1, x));
+                            st3(W.ioff, ld3(W.ioff) + (side ? -uo : uo));
+                        }
+                        if (side == 0) {
+                            C.impulse = imp1;
+                            C.impulse_offset = off1;
+                            st3(C.static_delta, sa ? u : (sb ? -u : mk(0, 0, 0)));
+                        }
+                    }
+                    __syncwarp();
+                    if (act && !st) integrate_one(W, fut + 14 * (size_t)g, mass[g], t, variant);
                 }
                 __syncthreads();
             }
@@ -493,9 +499,9 @@ __global__ void __launch_bounds__(kSolveBlock)
                 __syncthreads();
             }
             // (the static bodies' impulse sums are read only by the normal loop's test)
-            for (int i = p0 + tid; i < p1; i += nt) {
-                const int g = cl_parts[i];
-                if (!is_static[g]) integrate_body(bw[g], fut + 14 * (size_t)g, mass[g], t);
+            for (int k2 = tid; k2 < 2 * (p1 - p0); k2 += nt) {  // two lanes per body: FS, FSf
+                const int g = cl_parts[p0 + (k2 >> 1)];
+                if (!is_static[g]) integrate_one(bw[g], fut + 14 * (size_t)g, mass[g], t, k2 & 1);
             }
             converged = !block_any(big);
             it_f++;
