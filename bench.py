@@ -16,6 +16,11 @@ A pair-query is one compareTreesFullContinuous call.
   --impl reference : the reference algorithm on the host cores (the CPU
            restatement in oracle/, all host threads, spawn pool); the
            reference itself cannot be built here (Eigen, Embree, libigl).
+  world_steps : the second half of the metric, outer steps/s of the adaptive
+           cluster stepper (BroadPhaseEmbreeCluster::step) on the same
+           scene from its initial state, through d2g_world_step; e2e also
+           reads every body state back each step.  Its cpu_baseline is the
+           oracle stepper over the first steps of the same trajectory.
 Multi-GPU: the path does not shard across GPUs in this workload; every rank
 runs an independent replica and `value` sums them (weak scaling).
 """
@@ -48,6 +53,8 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget (single thread)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--world-steps", type=int, default=24, help="outer steps timed for steps/s")
+    p.add_argument("--cpu-step-seconds", type=float, default=20.0, help="oracle stepper sample budget")
     p.add_argument("--seed", type=int, default=0)
     return p.parse_args()
 
@@ -82,14 +89,14 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic_per_test():
-    """DRAM bytes per primitive test of the dominant kernel from the committed
-    ncu summary (profiles/ccd_kernels_c2.md), or None."""
+def profile_figures(key):
+    """Per-kernel figures from the committed ncu summary
+    (profiles/ccd_kernels_c2.md): lines '<key> <kernel>: <value>'."""
     path = os.path.join(ROOT, "profiles", "ccd_kernels_c2.md")
     out = {}
     try:
         for line in open(path):
-            if line.strip().startswith("dram_bytes_per_test"):
+            if line.strip().startswith(key + " "):
                 k, v = line.split(":", 1)
                 kind = k.strip().split()[-1]
                 out[kind] = float(v.strip().split()[0])
@@ -237,6 +244,12 @@ def run_ours(args):
 
     # ---- end to end through the host C-ABI entry points (pinned host buffers)
     e2e = e2e_host(ctx, scene, pairs, mt, args)
+    steps_line, steps_scene, steps_per = world_steps(local_rank, args)
+    t = torch.tensor([steps_line["ms_per_step"]], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    steps_line["value"] = world * 1e3 / float(t.item())
 
     if rank != 0:
         ctx.close()
@@ -250,17 +263,21 @@ def run_ours(args):
     dom = max((D.PROF_SOUP_CCD, D.PROF_CONN), key=lambda k: prof[k][0])
     ms, nl, items = prof[dom]
     achieved = (items * BYTES_PER_TEST) / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    tr = profile_traffic_per_test().get(kinds[dom])
+    tr = profile_figures("dram_bytes_per_test").get(kinds[dom])
+    fp64 = profile_figures("fp64_pipe_pct_active").get(kinds[dom])
     traffic = tr * items / nl if (tr is not None and nl) else None
     roofline = {"bound": "hbm", "kernel": kinds[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "kernel_ms_per_launch": ms / max(nl, 1), "launches": nl, "tests_per_launch": items / max(nl, 1),
-                "note": "FP64 arithmetic bound: the kernel's bytes are small next to its FP64 work"}
+                "note": "FP64 arithmetic bound: the kernel's bytes are small next to its FP64 work",
+                "fp64_pipe": {"frac_of_peak_active": fp64 / 100.0 if fp64 is not None else None,
+                              "source": "ncu sm__inst_executed_pipe_fp64, profiles/ccd_kernels_c2.md"}}
     kernel_share = {kinds[k]: prof[k][0] / max(1e-9, sum(v[0] for v in prof.values())) for k in prof}
 
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, pairs, mt, args.cpu_seconds)
+        steps_line["cpu_baseline"] = cpu_world_steps(steps_scene, steps_per, args.cpu_step_seconds)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -270,7 +287,7 @@ def run_ours(args):
                    "dt": scene.opt_dt, "l2": "flushed before every timed step (512 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
-        "kernel_time_share": kernel_share,
+        "kernel_time_share": kernel_share, "world_steps": steps_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
     }
@@ -347,6 +364,93 @@ def e2e_host(ctx, scene, pairs, mt, args):
     return {"value": len(pairs) * len(times) / sum(times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * sum(times) / len(times),
             "path": "d2g_ctx_set_bodies + d2g_compare_trees_full_continuous (host buffers)"}
+
+
+def world_steps(local_rank, args):
+    """Outer steps/s of the GPU stepper on the benchmark scene from its initial
+    state (warm-up on a discarded run), per-step wall times, kernel shares."""
+    import numpy as np
+
+    import delta2_gb300 as D
+
+    s0 = D.make_scene(2, seed=args.seed)
+    ctx = D.Context(local_rank)
+    ctx.set_scene(s0.copy())
+    ctx.world_configure(s0)
+    ctx.world_step(max(1, args.warmup))
+    # timed run from the initial state
+    sc = s0.copy()
+    ctx.set_bodies(sc)
+    ctx.world_configure(sc)
+    ctx.set_profiling(True)
+    l0 = ctx.launches()
+    per_step = []
+    for _ in range(args.world_steps):
+        t0 = time.perf_counter()
+        ctx.world_step(1)
+        per_step.append(time.perf_counter() - t0)
+    launches = ctx.launches() - l0
+    prof = {name: ctx.profile(k)[0] for name, k in (("swept_box_filter", D.PROF_SOUP_FILTER),
+                                                   ("point_tri_ccd", D.PROF_SOUP_CCD),
+                                                   ("edge_edge_ccd", D.PROF_CONN), ("np_tri_dist", D.PROF_NP),
+                                                   ("solve", D.PROF_SOLVE))}
+    ctx.set_profiling(False)
+    phases = ctx.world_timing()
+    stats = ctx.world_stats()
+    end = ctx.get_bodies(s0.copy())
+    moving = s0.is_static == 0
+    sim_s = float(end.cur[moving, 0].min() - s0.cur[moving, 0].min())
+    wall = sum(per_step)
+    # end to end: every step also copies every body state back to pinned host memory
+    import torch
+    sc2 = s0.copy()
+    ctx.set_bodies(sc2)
+    ctx.world_configure(sc2)
+    host = s0.copy()
+    keep = []
+    for k in ["last", "cur", "fut", "last_dt"]:
+        t = torch.empty(getattr(host, k).shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = getattr(host, k)
+        setattr(host, k, t.numpy())
+        keep.append(t)
+    e2e_t = []
+    for _ in range(args.world_steps):
+        t0 = time.perf_counter()
+        ctx.world_step(1)
+        ctx.get_bodies(host)
+        e2e_t.append(time.perf_counter() - t0)
+    d2h = sum(getattr(host, k).nbytes for k in ["last", "cur", "fut", "last_dt", "sleep_steps", "sleeping"])
+    ctx.close()
+    out = {"metric": "steps/s", "value": len(per_step) / wall, "unit": "steps/s", "steps": len(per_step),
+           "ms_per_step": 1e3 * wall / len(per_step), "per_step_ms": [round(1e3 * x, 3) for x in per_step],
+           "sim_seconds_per_wall_second": sim_s / wall, "sim_seconds": sim_s, "gpu_launches": launches,
+           "phase_ms_per_step": {k: v / len(per_step) for k, v in phases.items() if k != "reserved"},
+           "kernel_ms_per_step": {k: v / len(per_step) for k, v in prof.items()},
+           "stats_per_step": {k: v / len(per_step) for k, v in stats.items()},
+           "e2e": {"value": len(e2e_t) / sum(e2e_t), "unit": "steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": int(d2h),
+                   "path": "d2g_world_step + d2g_ctx_get_bodies into pinned host memory every step"}}
+    return out, s0, per_step
+
+
+def cpu_world_steps(scene, per_step_gpu, budget_s):
+    """The oracle stepper (single thread) from the same initial state for
+    about budget_s seconds; the GPU's time over the same first steps."""
+    from oracle import oracle as O
+
+    w = O.World(scene.copy(), scene.opt_dt, scene.gravity_z)
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and done < len(per_step_gpu):
+        if w.step(1) != 0:
+            break
+        done += 1
+    dt = time.perf_counter() - t0
+    if done == 0:
+        return None
+    return {"value": done / dt, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"the first {done} outer steps from the initial state, {dt:.1f} s single-threaded, "
+                      f"CPU oracle g++ -O2",
+            "gpu_same_steps_per_s": done / sum(per_step_gpu[:done])}
 
 
 # ------------------------------------------------------------- reference ---
