@@ -693,6 +693,29 @@ int d2g_select_time_steps(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, con
             set_error("cluster particle index out of range");
             return D2G_ERR_INVALID;
         }
+    // a moving body belongs to one cluster, and every interaction's bodies to its cluster
+    int max_parts = 0;
+    {
+        std::vector<int32_t> owner(c->n_bodies, -1), mark(c->n_bodies, -1);
+        for (int k = 0; k < n_clusters; k++) {
+            max_parts = std::max(max_parts, cluster_particle_off[k + 1] - cluster_particle_off[k]);
+            for (int i = cluster_particle_off[k]; i < cluster_particle_off[k + 1]; i++) {
+                const int g = cluster_particles[i];
+                mark[g] = k;
+                if (c->h_is_static[g]) continue;
+                if (owner[g] >= 0) {
+                    set_error("moving body " + std::to_string(g) + " is in more than one cluster or listed twice");
+                    return D2G_ERR_INVALID;
+                }
+                owner[g] = k;
+            }
+            for (int i = cluster_pair_off[k]; i < cluster_pair_off[k + 1]; i++)
+                if (mark[pairs[2 * i]] != k || mark[pairs[2 * i + 1]] != k) {
+                    set_error("interaction " + std::to_string(i) + " names a body outside its cluster");
+                    return D2G_ERR_INVALID;
+                }
+        }
+    }
     D2G_CUDA(cudaSetDevice(c->device));
     d2g::Engine& E = c->eng;
     RC(upload(c, E.d_pairs, pairs, 2 * (size_t)n_pairs));
@@ -701,7 +724,7 @@ int d2g_select_time_steps(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, con
     RC(upload(c, E.st_cl_parts, cluster_particles, (size_t)np));
     RC(E.st_out.ensure(n_clusters + 1));
     RC(d2g::run_select_steps(c, E.d_pairs.p, n_pairs, E.st_cl_pair_off.p, E.st_cl_part_off.p, E.st_cl_parts.p,
-                             n_clusters, (double)opt_dt, E.st_out.p, counters));
+                             n_clusters, np, max_parts, (double)opt_dt, E.st_out.p, counters));
     RC(download(c, step_out, E.st_out, (size_t)n_clusters));
     D2G_CUDA(cudaStreamSynchronize(c->stream));
     return D2G_OK;

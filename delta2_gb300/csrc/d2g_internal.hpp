@@ -129,7 +129,7 @@ struct Engine {
     DBuf<int32_t> chit, cflag_off, nn_cnt, nn_off, citem_off;
     // time-step selection
     DBuf<double> st_mt, st_new_dt, st_step, st_out;
-    DBuf<int32_t> st_has, st_cl_pair_off, st_cl_part_off, st_cl_parts;
+    DBuf<int32_t> st_has, st_cl_pair_off, st_cl_part_off, st_cl_parts, st_loc;
     // contact filtering
     DBuf<int32_t> flt_idx, flt_order, flt_keep, flt_pos, flt_cnt, flt_off, np_tri;
     DBuf<unsigned long long> flt_keys, flt_keys_s;
@@ -212,9 +212,11 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             int64_t* counters);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
 // Time-step selection (d2g_step.cu).
+// n_parts: particles of all clusters; max_cluster_parts: of the largest.
 int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const int32_t* d_cl_pair_off,
-                     const int32_t* d_cl_part_off, const int32_t* d_cl_parts, int n_clusters, double opt_dt,
-                     double* d_out, int64_t* counters, int* n_ccd_contacts = nullptr);
+                     const int32_t* d_cl_part_off, const int32_t* d_cl_parts, int n_clusters, int n_parts,
+                     int max_cluster_parts, double opt_dt, double* d_out, int64_t* counters,
+                     int* n_ccd_contacts = nullptr);
 int run_outer_project(d2g_ctx* ctx, double opt_dt);
 int run_pde_prepare(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts,
                     const double* d_step, const double* d_tmin, int32_t* d_err);

@@ -21,17 +21,15 @@ namespace {
 constexpr int kBlock = 128;
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
-// separate_clusters.cpp:497-554: the scale one continuous contact asks for.
-__device__ double contact_step_scale(const double* c, const State& fa, const double* iia, const State& fb,
-                                     const double* iib, double max_dt) {
+// separate_clusters.cpp:497-554: the scale one continuous contact asks for
+// (Ia, Ib: the future world inverse inertias, Particle::futurePointVelocity).
+__device__ double contact_step_scale(const double* c, const State& fa, const double* Ia, const State& fb,
+                                     const double* Ib, double max_dt) {
     double scale = 1.0;
     const V3 A = mk(c[0], c[1], c[2]), B = mk(c[3], c[4], c[5]);
     const double toc = c[10];
     const V3 hit_normal = A - B;
     const double interaction_dist = c[6] + c[7];
-    double Ia[9], Ib[9];
-    world_inv_inertia(fa.q, iia, Ia);
-    world_inv_inertia(fb.q, iib, Ib);
     const V3 a_vel = fa.v + cross(m3_vec(Ia, fa.L), A - fa.x);
     const V3 b_vel = fb.v + cross(m3_vec(Ib, fb.L), B - fb.x);
     const V3 rel = a_vel - b_vel;
@@ -57,42 +55,92 @@ __device__ double contact_step_scale(const double* c, const State& fa, const dou
     return scale;
 }
 
+// min(b, a) as (b < a) ? b : a, through an integer compare when both are
+// finite and non-negative (their bit patterns order like the values, and
+// equal values have equal bits); the FP64 compare otherwise.
+__device__ __forceinline__ double dmin_fast(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    if ((ia | ib) >= 0 && ia < 0x7ff0000000000000LL && ib < 0x7ff0000000000000LL) return ib < ia ? b : a;
+    return b < a ? b : a;
+}
+
+// One warp per interaction (separate_clusters.cpp:494-562): every contact's
+// scale in parallel, then the reference's running minimum from 1.0, which
+// keeps the first of equal values and never takes a NaN, as a leftmost-
+// minimum reduction over (value, contact index).
 __global__ void k_pair_new_dt(int n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ max_time,
                               const int32_t* __restrict__ off, const double* __restrict__ rec,
                               const double* __restrict__ pfut, const double* __restrict__ ii,
                               double* __restrict__ new_dt, int32_t* __restrict__ has) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs) return;
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= n_pairs) return;  // uniform per warp
     const int a = pairs[2 * p], b = pairs[2 * p + 1];
     const int c0 = off[p], c1 = off[p + 1];
-    has[p] = c1 > c0 ? 1 : 0;
     if (c1 <= c0) {
-        new_dt[p] = 0.0;
+        if (lane == 0) {
+            has[p] = 0;
+            new_dt[p] = 0.0;
+        }
         return;
     }
     const State fa = load_state(pfut + 28 * (size_t)p), fb = load_state(pfut + 28 * (size_t)p + 14);
     const double mt = max_time[p];
-    double min_scaling = 1.0;
-    for (int c = c0; c < c1; c++)
-        min_scaling = dmin(min_scaling, contact_step_scale(rec + 14 * (size_t)c, fa, ii + 9 * (size_t)a, fb,
-                                                           ii + 9 * (size_t)b, mt));
-    new_dt[p] = mt * min_scaling;
+    double Ia[9], Ib[9];
+    world_inv_inertia(fa.q, ii + 9 * (size_t)a, Ia);
+    world_inv_inertia(fb.q, ii + 9 * (size_t)b, Ib);
+    double best = 1.0;
+    int best_i = -1;  // the running minimum's start value comes first
+    for (int c = c0 + lane; c < c1; c += 32) {
+        const double sc = contact_step_scale(rec + 14 * (size_t)c, fa, Ia, fb, Ib, mt);
+        if (sc < best) {
+            best = sc;
+            best_i = c;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, best_i, o);
+        if (ob < best || (ob == best && oi < best_i)) {
+            best = ob;
+            best_i = oi;
+        }
+    }
+    if (lane == 0) {
+        has[p] = 1;
+        new_dt[p] = mt * best;
+    }
 }
 
+// The reference's order-dependent propagation over a cluster's interactions
+// (separate_clusters.cpp:555-598), one block per cluster: the moving bodies'
+// steps live in shared memory (loc maps a moving body to its slot), thread 0
+// walks the interactions in order.
 __global__ void k_cluster_steps(int n_clusters, const int32_t* __restrict__ cl_pair_off,
                                 const int32_t* __restrict__ cl_part_off, const int32_t* __restrict__ cl_parts,
                                 const int32_t* __restrict__ pairs, const double* __restrict__ new_dt,
                                 const int32_t* __restrict__ has, const uint8_t* __restrict__ is_static,
-                                const double* __restrict__ last_dt, double* __restrict__ step, double opt_dt,
-                                double* __restrict__ out) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+                                const double* __restrict__ last_dt, int32_t* __restrict__ loc, double opt_dt,
+                                double* __restrict__ out, double* __restrict__ gstep) {
+    extern __shared__ double s_dyn[];
+    const int c = blockIdx.x;
     if (c >= n_clusters) return;
+    const int p0 = cl_part_off[c], p1 = cl_part_off[c + 1];
+    double* s_step = gstep ? gstep + p0 : s_dyn;  // global scratch for clusters too large for shared memory
+    for (int i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+        const int g = cl_parts[i];
+        s_step[i - p0] = last_dt[g];
+        if (!is_static[g]) loc[g] = i - p0;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    auto step_of = [&](int g) { return is_static[g] ? last_dt[g] : s_step[loc[g]]; };
     for (int i = cl_pair_off[c]; i < cl_pair_off[c + 1]; i++) {
         if (!has[i]) continue;
         const int a = pairs[2 * i], b = pairs[2 * i + 1];
-        const double use = dmin(new_dt[i], dmin(step[a], step[b]));
-        if (!is_static[a]) step[a] = use;
-        if (!is_static[b]) step[b] = use;
+        const double use = dmin_fast(new_dt[i], dmin_fast(step_of(a), step_of(b)));
+        if (!is_static[a]) s_step[loc[a]] = use;
+        if (!is_static[b]) s_step[loc[b]] = use;
     }
     double cs = -1.0;
     for (int i = cl_pair_off[c]; i < cl_pair_off[c + 1]; i++) {
@@ -106,9 +154,9 @@ __global__ void k_cluster_steps(int n_clusters, const int32_t* __restrict__ cl_p
             id = b;
         else
             id = a;
-        cs = cs < 0.0 ? step[a] : dmin(cs, step[id]);
+        cs = cs < 0.0 ? step_of(a) : dmin_fast(cs, step_of(id));
     }
-    if (cs < 0.0) cs = last_dt[cl_parts[cl_part_off[c]]];
+    if (cs < 0.0) cs = last_dt[cl_parts[p0]];
     out[c] = dmax(1e-3, dmin(cs, opt_dt));
 }
 
@@ -118,10 +166,6 @@ __global__ void k_max_time(int n, const int32_t* __restrict__ pairs, const doubl
     if (p < n) mt[p] = dmin(last_dt[pairs[2 * p]], last_dt[pairs[2 * p + 1]]);
 }
 
-__global__ void k_copy(int n, const double* __restrict__ in, double* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = in[i];
-}
 
 #define SLAUNCH(kern, n, ...)                                          \
     do {                                                               \
@@ -456,24 +500,37 @@ int run_con_off(d2g_ctx* ctx, int n, const int32_t* d_pair_off, const int32_t* d
 
 // Device-side driver: pairs/cluster arrays already in HBM.
 int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const int32_t* d_cl_pair_off,
-                     const int32_t* d_cl_part_off, const int32_t* d_cl_parts, int n_clusters, double opt_dt,
-                     double* d_out, int64_t* counters, int* n_ccd_contacts) {
+                     const int32_t* d_cl_part_off, const int32_t* d_cl_parts, int n_clusters, int n_parts,
+                     int max_cluster_parts, double opt_dt, double* d_out, int64_t* counters, int* n_ccd_contacts) {
     Engine& E = ctx->eng;
     RC(E.st_mt.ensure(n_pairs + 1));
     RC(E.st_new_dt.ensure(n_pairs + 1));
     RC(E.st_has.ensure(n_pairs + 1));
-    RC(E.st_step.ensure(ctx->n_bodies + 1));
     if (n_pairs > 0) SLAUNCH(k_max_time, n_pairs, n_pairs, d_pairs, ctx->last_dt.p, E.st_mt.p);
     int n_rec = 0;
     RC(run_ccd(ctx, d_pairs, E.st_mt.p, n_pairs, &n_rec, counters));
     if (n_ccd_contacts) *n_ccd_contacts = n_rec;
     if (n_pairs > 0)
-        SLAUNCH(k_pair_new_dt, n_pairs, n_pairs, d_pairs, E.st_mt.p, E.out_off.p, E.rec_sorted.p, E.pfut.p,
+        SLAUNCH(k_pair_new_dt, 32LL * n_pairs, n_pairs, d_pairs, E.st_mt.p, E.out_off.p, E.rec_sorted.p, E.pfut.p,
                 ctx->inv_inertia.p, E.st_new_dt.p, E.st_has.p);
-    SLAUNCH(k_copy, ctx->n_bodies, ctx->n_bodies, ctx->last_dt.p, E.st_step.p);
-    if (n_clusters > 0)
-        SLAUNCH(k_cluster_steps, n_clusters, n_clusters, d_cl_pair_off, d_cl_part_off, d_cl_parts, d_pairs,
-                E.st_new_dt.p, E.st_has.p, ctx->is_static.p, ctx->last_dt.p, E.st_step.p, opt_dt, d_out);
+    if (n_clusters > 0) {
+        RC(E.st_loc.ensure(ctx->n_bodies + 1));
+        constexpr int kMaxSmemParts = 24 * 1024;  // 192 KB of steps
+        double* gstep = nullptr;
+        size_t smem = (size_t)max_cluster_parts * sizeof(double);
+        if (max_cluster_parts > kMaxSmemParts) {
+            RC(E.st_step.ensure((size_t)n_parts + 1));
+            gstep = E.st_step.p;
+            smem = 0;
+        } else if (smem > 48 * 1024) {
+            D2G_CUDA(cudaFuncSetAttribute(k_cluster_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(kMaxSmemParts * sizeof(double))));
+        }
+        k_cluster_steps<<<n_clusters, kBlock, smem, ctx->stream>>>(
+            n_clusters, d_cl_pair_off, d_cl_part_off, d_cl_parts, d_pairs, E.st_new_dt.p, E.st_has.p,
+            ctx->is_static.p, ctx->last_dt.p, E.st_loc.p, opt_dt, d_out, gstep);
+        ctx->eng.launches++;
+    }
     D2G_CUDA(cudaGetLastError());
     return D2G_OK;
 }

@@ -22,6 +22,7 @@
 // host: last_dt and sleeping come from the last PDE step (in cluster order)
 // of a cluster holding the body, and the current time advances once per
 // sleeping cluster holding it, in cluster order.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -524,9 +525,11 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         RC(W.sel_out.ensure(sel.size() + 1));
         int64_t cnt[4] = {0, 0, 0, 0};
         int n_ccd = 0;
+        int max_parts = 0;
+        for (int k : sel) max_parts = std::max(max_parts, (int)cls[k].parts.size());
         RC(run_select_steps(c, W.pk_round.ptr(i_pairs), (int)(pairs.size() / 2), W.pk_round.ptr(i_pairoff),
-                            W.pk_round.ptr(i_partoff), W.pk_round.ptr(i_parts), (int)sel.size(), opt_dt, W.sel_out.p,
-                            cnt, &n_ccd));
+                            W.pk_round.ptr(i_partoff), W.pk_round.ptr(i_parts), (int)sel.size(), (int)parts.size(),
+                            max_parts, opt_dt, W.sel_out.p, cnt, &n_ccd));
         RC(W.h_rd.ensure(sel.size() + 1));
         D2G_CUDA(cudaMemcpyAsync(W.h_rd.p, W.sel_out.p, sel.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         D2G_CUDA(cudaStreamSynchronize(s));
