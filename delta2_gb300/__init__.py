@@ -350,6 +350,35 @@ class Context:
                                            _p(out, F64P), _p(cnt, I64P)))
         return out[:len(clusters)].copy(), cnt
 
+    def broad_phase_device(self, scene=None):
+        """broadPhaseEmbree over the device bodies -> pairs [n, 2] (ascending)."""
+        scene = scene or self.scene
+        aabb = np.ascontiguousarray(scene.local_aabb, dtype=np.float32)
+        n = C.c_int32()
+        _check(lib().d2g_ctx_broad_phase(self.h, _p(aabb, F32P), None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 2), np.int32)
+        _check(lib().d2g_ctx_broad_phase(self.h, _p(aabb, F32P), _p(out, I32P), n.value, C.byref(n)))
+        return out[:n.value].copy()
+
+    def separate_clusters(self, pairs):
+        """separateCollisionClusters on the device (rolls the device states back)
+        -> list of (particles, interactions [m, 2], min_current_time, step, sleeping)."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        nb = self.scene.n_bodies
+        ncl = C.c_int32()
+        poff = np.zeros(nb + 1, np.int32)
+        parts = np.zeros(nb + len(pairs) + 1, np.int32)
+        qoff = np.zeros(nb + 1, np.int32)
+        cp = np.zeros((max(1, len(pairs)), 2), np.int32)
+        mct = np.zeros(nb)
+        step = np.zeros(nb)
+        sl = np.zeros(nb, np.uint8)
+        _check(lib().d2g_ctx_separate_clusters(self.h, _p(pairs, I32P), len(pairs), C.byref(ncl), _p(poff, I32P),
+                                               _p(parts, I32P), _p(qoff, I32P), _p(cp, I32P), _p(mct, F64P),
+                                               _p(step, F64P), _p(sl, U8P)))
+        return [(parts[poff[k]:poff[k + 1]].tolist(), cp[qoff[k]:qoff[k + 1]].copy(), float(mct[k]), float(step[k]),
+                 bool(sl[k])) for k in range(ncl.value)]
+
     def filter_contacts(self, contacts, offsets, margin=0.0):
         """filterContacts per group -> (kept contacts [m,14], out_offsets [n_groups+1])."""
         c = np.ascontiguousarray(contacts, dtype=np.float64).reshape(-1, CONTACT_LEN)

@@ -667,6 +667,80 @@ int d2g_solve_clusters(d2g_ctx* c, int32_t n_clusters, const int32_t* particle_o
     return D2G_OK;
 }
 
+int d2g_ctx_broad_phase(d2g_ctx* c, const float* local_aabb, int32_t* pairs, int32_t capacity, int32_t* n_pairs) {
+    RC(check_ready(c));
+    if (!local_aabb || !n_pairs || (int)c->h_bounding_radius.size() != c->n_bodies) {
+        set_error("the device broad phase needs local boxes and the bodies' bounding radii");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.up_aabb, local_aabb, 6 * (size_t)c->n_bodies));
+    RC(E.up_err.ensure(2));
+    D2G_CUDA(cudaMemsetAsync(E.up_err.p, 0, sizeof(int32_t), c->stream));
+    int n = 0;
+    RC(d2g::run_broad_phase(c, E.up_aabb.p, &n, E.up_err.p));
+    *n_pairs = n;
+    if (pairs && n <= capacity) RC(download(c, pairs, E.bp_pairs, 2 * (size_t)n));
+    int32_t err = 0;
+    D2G_CUDA(cudaMemcpyAsync(&err, E.up_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    if (err) {
+        set_error("invalid state interpolation in the broad phase (the reference throws here)");
+        return D2G_ERR_STATE;
+    }
+    if (pairs && n > capacity) {
+        set_error("broad-phase pair capacity too small");
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
+}
+
+int d2g_ctx_separate_clusters(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, int32_t* n_clusters,
+                              int32_t* particle_off, int32_t* particles, int32_t* pair_off, int32_t* cluster_pairs,
+                              double* min_current_time, double* step, uint8_t* sleeping) {
+    RC(check_ready(c));
+    RC(check_pairs(c, pairs, n_pairs));
+    if (!n_clusters || !particle_off || !particles || !pair_off || !min_current_time || !step || !sleeping ||
+        (n_pairs > 0 && !cluster_pairs)) {
+        set_error("null output");
+        return D2G_ERR_INVALID;
+    }
+    for (int k = 0; k < n_pairs; k++)
+        if (c->h_is_static[pairs[2 * k]] && c->h_is_static[pairs[2 * k + 1]]) {
+            set_error("pair " + std::to_string(k) + " joins two static bodies");
+            return D2G_ERR_INVALID;
+        }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.d_pairs, pairs, 2 * (size_t)n_pairs));
+    RC(E.up_err.ensure(2));
+    D2G_CUDA(cudaMemsetAsync(E.up_err.p, 0, sizeof(int32_t), c->stream));
+    int n_dyn = 0;
+    for (int g = 0; g < c->n_bodies; g++) n_dyn += c->h_is_static[g] ? 0 : 1;
+    int nc = 0, np = 0;
+    RC(d2g::run_clusters(c, E.d_pairs.p, n_pairs, n_dyn, &nc, &np, E.up_err.p));
+    RC(d2g::run_cluster_rollback(c, E.up_err.p));
+    *n_clusters = nc;
+    RC(download(c, particle_off, E.cl_part_off, (size_t)nc + 1));
+    RC(download(c, particles, E.cl_parts, (size_t)np));
+    RC(download(c, pair_off, E.cl_pair_off, (size_t)nc + 1));
+    RC(download(c, cluster_pairs, E.cl_pairs, 2 * (size_t)n_pairs));
+    RC(download(c, min_current_time, E.cl_mct, (size_t)nc));
+    RC(download(c, step, E.cl_step, (size_t)nc));
+    std::vector<int32_t> sl(nc + 1);
+    if (nc) RC(download(c, sl.data(), E.cl_sleep, (size_t)nc));
+    int32_t err = 0;
+    D2G_CUDA(cudaMemcpyAsync(&err, E.up_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < nc; k++) sleeping[k] = sl[k] ? 1 : 0;
+    if (err) {
+        set_error("invalid state interpolation in separateCollisionClusters (the reference throws here)");
+        return D2G_ERR_STATE;
+    }
+    return D2G_OK;
+}
+
 int d2g_select_time_steps(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, const int32_t* cluster_pair_off,
                           const int32_t* cluster_particle_off, const int32_t* cluster_particles, int32_t n_clusters,
                           float opt_dt, double* step_out, int64_t* counters) {

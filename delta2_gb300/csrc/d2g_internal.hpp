@@ -144,8 +144,22 @@ struct Engine {
     DBuf<int32_t> sv_vals, sv_order, sv_wave_idx, sv_wave_off, sv_wave_cursor;
     DBuf<double> sv_static_imp;
     DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
+    // GPU broad phase (d2g_broadphase.cu)
+    DBuf<float> bp_box;
+    DBuf<uint32_t> bp_key, bp_key_s;
+    DBuf<int32_t> bp_idx, bp_order, bp_cnt, bp_off, bp_cand, bp_flag, bp_foff, bp_pairs;
+    DBuf<unsigned long long> bp_pkey, bp_pkey2;
+    // GPU cluster separation (d2g_broadphase.cu)
+    DBuf<int32_t> uf_parent, uf_root, uf_roff, cl_cid, cl_uidx, cl_member, cl_pair_cid, cl_piota, cl_porder,
+        cl_pairs, cl_st_pos, cl_st_pos_s, cl_st_flag, cl_st_off, cl_st_body, cl_st_body3, cl_st_body4, cl_n_dyn,
+        cl_n_stat, cl_n_all, cl_dyn_off, cl_stat_off, cl_part_off, cl_pair_cnt, cl_pair_off, cl_sleep, cl_parts;
+    DBuf<uint32_t> cl_ukey, cl_ukey_s, cl_pkey_s;
+    DBuf<unsigned long long> cl_st_key, cl_st_key_s, cl_st_key2, cl_st_key3, cl_st_key4;
+    DBuf<double> cl_mct, cl_step;
     // inputs / outputs of the host filter and solve entry points
     DBuf<double> up_rec, up_warm, up_step, up_imp;
+    DBuf<float> up_aabb;
+    DBuf<int32_t> up_err;
     DBuf<int32_t> up_off, up_part_off, up_parts, up_con_off, up_cnt, up_status, up_iters, up_ab;
     // per pair
     DBuf<double> pm;    // [pairs][128] pose matrices
@@ -230,6 +244,11 @@ enum { D2G_OP_ENTER = 1, D2G_OP_SPLIT = 2, D2G_OP_SAVE = 3, D2G_OP_MID = 4, D2G_
 int run_cluster_ops(d2g_ctx* ctx, int n_active, const int32_t* d_cl_idx, const int32_t* d_op_off, const int4* d_ops,
                     const int32_t* d_part_off, const int32_t* d_parts, double* d_cl_step, double* d_cl_tmin,
                     double* d_frame_start, double* d_stash, int32_t* d_err);
+// Broad phase and cluster separation over the device bodies (d2g_broadphase.cu).
+int run_broad_phase(d2g_ctx* ctx, const float* d_aabb, int* n_out, int32_t* d_err);
+int run_clusters(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int n_dyn_total, int* n_clusters_out,
+                 int* n_parts_out, int32_t* d_err);
+int run_cluster_rollback(d2g_ctx* ctx, int32_t* d_err);
 // Contact filtering and sequential impulses (d2g_solve.cu).
 int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pairs, int n_rec, double margin,
                int* n_out);

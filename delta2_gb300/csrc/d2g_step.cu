@@ -413,7 +413,25 @@ __global__ void k_con_off(int n, const int32_t* __restrict__ pair_off, const int
     if (i <= n) con_off[i] = flt_off[pair_off[i]];
 }
 
+// The static bodies' current states, last_dt and sleeping flags, compacted.
+__global__ void k_gather_static(int n, const int32_t* __restrict__ idx, const double* __restrict__ cur,
+                                const double* __restrict__ last_dt, const uint8_t* __restrict__ sleeping,
+                                double* __restrict__ rec, uint8_t* __restrict__ sl) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int g = idx[k];
+    for (int q = 0; q < 14; q++) rec[15 * (size_t)k + q] = cur[14 * (size_t)g + q];
+    rec[15 * (size_t)k + 14] = last_dt[g];
+    sl[k] = sleeping[g];
+}
+
 }  // namespace
+
+int run_gather_static(d2g_ctx* ctx, int n, const int32_t* d_idx, double* d_rec, uint8_t* d_sleep) {
+    if (n > 0) SLAUNCH(k_gather_static, n, n, d_idx, ctx->cur.p, ctx->last_dt.p, ctx->sleeping.p, d_rec, d_sleep);
+    D2G_CUDA(cudaGetLastError());
+    return D2G_OK;
+}
 
 int run_outer_project(d2g_ctx* ctx, double opt_dt) {
     SLAUNCH(k_outer_project, ctx->n_bodies, ctx->n_bodies, opt_dt, ctx->cur.p, ctx->inv_inertia.p, ctx->last_dt.p,

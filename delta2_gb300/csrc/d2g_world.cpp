@@ -36,7 +36,7 @@
 
 namespace d2g {
 
-int broad_phase_pairs(const d2g_bodies* b, const float* local_aabb, std::vector<int32_t>& out);
+int run_gather_static(d2g_ctx* ctx, int n, const int32_t* d_idx, double* d_rec, uint8_t* d_sleep);
 int run_gather_f64(d2g_ctx* ctx, int n, const int32_t* d_idx, const double* d_src, double* d_dst);
 int run_con_off(d2g_ctx* ctx, int n, const int32_t* d_pair_off, const int32_t* d_flt_off, int32_t* d_con_off);
 int run_expand_contacts(d2g_ctx* ctx, int n_pairs, const int32_t* d_off, const double* d_pwarm,
@@ -140,9 +140,16 @@ struct WorldState {
     double gravity_z = -9.8;
     std::map<std::pair<int, int>, double> warm;
     int64_t stats[13] = {0};
-    // host mirrors of the device states, refreshed once per outer step
-    Pinned<double> h_last, h_cur, h_fut, h_last_dt;
-    Pinned<uint8_t> h_sleeping;
+    // static bodies: indices, slot of a body in that list, their records
+    std::vector<int32_t> static_ids, slot_of;
+    int n_dyn_total = 0;
+    DBuf<float> d_aabb;
+    DBuf<int32_t> d_static;
+    DBuf<double> d_st_rec;
+    DBuf<uint8_t> d_st_sleep;
+    Pinned<int32_t> h_cl;   // cluster CSR and flags copied back each step
+    Pinned<double> h_cld;   // cluster times, steps and the static records
+    Pinned<uint8_t> h_sleeping;  // static bodies' sleeping flags being written
     Pinned<double> h_rd;
     Pinned<int32_t> h_ri;
     Packer<int32_t> pk_round, pk_batch, pk_cl;
@@ -163,11 +170,13 @@ struct WorldState {
 
 void world_free(WorldState* w) {
     if (!w) return;
-    w->h_last.release();
-    w->h_cur.release();
-    w->h_fut.release();
-    w->h_last_dt.release();
+    w->h_cl.release();
+    w->h_cld.release();
     w->h_sleeping.release();
+    w->d_aabb.release();
+    w->d_static.release();
+    w->d_st_rec.release();
+    w->d_st_sleep.release();
     w->h_rd.release();
     w->h_ri.release();
     w->pk_round.release();
@@ -390,118 +399,55 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
     D2G_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int32_t), s));
     // :126-132 every body: last_dt doubles (capped), future projected
     RC(run_outer_project(c, opt_dt));
-    D2G_CUDA(cudaMemcpyAsync(W.h_last.p, c->last.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    D2G_CUDA(cudaMemcpyAsync(W.h_cur.p, c->cur.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    D2G_CUDA(cudaMemcpyAsync(W.h_fut.p, c->fut.p, 14 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    D2G_CUDA(cudaMemcpyAsync(W.h_last_dt.p, c->last_dt.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    D2G_CUDA(cudaMemcpyAsync(W.h_sleeping.p, c->sleeping.p, (size_t)n, cudaMemcpyDeviceToHost, s));
-    D2G_CUDA(cudaStreamSynchronize(s));
-    const uint8_t* is_static = c->h_is_static.data();
     W.mark(0);
-    // :134 broad phase
-    d2g_bodies hb;
-    memset(&hb, 0, sizeof(hb));
-    hb.n = n;
-    hb.is_static = is_static;
-    hb.geo_eps = c->h_geo_eps.data();
-    hb.last = W.h_last.p;
-    hb.cur = W.h_cur.p;
-    hb.fut = W.h_fut.p;
-    hb.last_dt = W.h_last_dt.p;
-    hb.bounding_radius = c->h_bounding_radius.data();
-    std::vector<int32_t> B;
-    RC(broad_phase_pairs(&hb, W.local_aabb.data(), B));
-    const int nb = (int)(B.size() / 2);
+    // :134 broad phase and :136 cluster separation (with its rollback), on the device
+    Engine& E = c->eng;
+    int nb = 0;
+    RC(run_broad_phase(c, W.d_aabb.p, &nb, W.err.p));
     W.mark(1);
-    // :136 separateCollisionClusters: components over moving-moving pairs
-    std::vector<int32_t> deg(n + 1, 0), adj;
-    for (int e = 0; e < nb; e++)
-        if (!is_static[B[2 * e]] && !is_static[B[2 * e + 1]]) {
-            deg[B[2 * e] + 1]++;
-            deg[B[2 * e + 1] + 1]++;
-        }
-    for (int i = 0; i < n; i++) deg[i + 1] += deg[i];
-    adj.assign(deg[n], 0);
-    {
-        std::vector<int32_t> fill(deg.begin(), deg.end() - 1);
-        for (int e = 0; e < nb; e++) {
-            const int a = B[2 * e], b = B[2 * e + 1];
-            if (is_static[a] || is_static[b]) continue;
-            adj[fill[a]++] = b;
-            adj[fill[b]++] = a;
-        }
+    int nc = 0, n_parts = 0;
+    RC(run_clusters(c, E.bp_pairs.p, nb, W.n_dyn_total, &nc, &n_parts, W.err.p));
+    RC(run_cluster_rollback(c, W.err.p));
+    // the clusters and the static bodies' records come back for the host schedule
+    const int n_st = (int)W.static_ids.size();
+    RC(W.h_cl.ensure(3 * (size_t)nc + n_parts + 2 * (size_t)nb + 8));
+    RC(W.h_cld.ensure(2 * (size_t)nc + 15 * (size_t)n_st + 8));
+    int32_t* h_part_off = W.h_cl.p;
+    int32_t* h_pair_off = h_part_off + nc + 1;
+    int32_t* h_ndyn = h_pair_off + nc + 1;
+    int32_t* h_sleep = h_ndyn + nc;
+    int32_t* h_parts = h_sleep + nc;
+    int32_t* h_pairs = h_parts + n_parts;
+    double* h_mct = W.h_cld.p;
+    double* h_step = h_mct + nc;
+    double* h_st = h_step + nc;  // static records: 14 (cur) + last_dt per static body
+    D2G_CUDA(cudaMemcpyAsync(h_part_off, E.cl_part_off.p, (nc + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaMemcpyAsync(h_pair_off, E.cl_pair_off.p, (nc + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (nc > 0) {
+        D2G_CUDA(cudaMemcpyAsync(h_ndyn, E.cl_n_dyn.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        D2G_CUDA(cudaMemcpyAsync(h_sleep, E.cl_sleep.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        D2G_CUDA(cudaMemcpyAsync(h_mct, E.cl_mct.p, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+        D2G_CUDA(cudaMemcpyAsync(h_step, E.cl_step.p, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+        D2G_CUDA(cudaMemcpyAsync(h_parts, E.cl_parts.p, n_parts * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     }
-    std::vector<int32_t> comp(n, -1), queue;
-    queue.reserve(n);
-    int n_comp = 0;
-    for (int st = 0; st < n; st++) {
-        if (comp[st] >= 0) continue;
-        comp[st] = n_comp;
-        queue.clear();
-        queue.push_back(st);
-        for (size_t h = 0; h < queue.size(); h++)
-            for (int q = deg[queue[h]]; q < deg[queue[h] + 1]; q++)
-                if (comp[adj[q]] < 0) {
-                    comp[adj[q]] = n_comp;
-                    queue.push_back(adj[q]);
-                }
-        n_comp++;
+    if (nb > 0)
+        D2G_CUDA(cudaMemcpyAsync(h_pairs, E.cl_pairs.p, 2 * (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (n_st > 0) {
+        RC(W.d_st_rec.ensure(15 * (size_t)n_st));
+        RC(run_gather_static(c, n_st, W.d_static.p, W.d_st_rec.p, W.d_st_sleep.p));
+        D2G_CUDA(cudaMemcpyAsync(h_st, W.d_st_rec.p, 15 * (size_t)n_st * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
-    // clusters with a moving body, in label order (static singletons dropped)
-    std::vector<int32_t> cl_of(n_comp, -1);
-    std::vector<HostCluster> cls;
-    for (int p = 0; p < n; p++) {
-        if (is_static[p]) continue;
-        if (cl_of[comp[p]] < 0) {
-            cl_of[comp[p]] = 0;  // mark
-        }
+    RC(check_err(c, W, "the broad phase or separateCollisionClusters"));
+    std::vector<HostCluster> cls(nc);
+    for (int k = 0; k < nc; k++) {
+        HostCluster& h = cls[k];
+        h.parts.assign(h_parts + h_part_off[k], h_parts + h_part_off[k + 1]);
+        h.pairs.assign(h_pairs + 2 * (size_t)h_pair_off[k], h_pairs + 2 * (size_t)h_pair_off[k + 1]);
+        h.n_dyn = h_ndyn[k];
+        h.mct = h_mct[k];
+        h.step = h_step[k];
+        h.sleeping = h_sleep[k] != 0;
     }
-    {
-        int k = 0;
-        for (int q = 0; q < n_comp; q++)
-            if (cl_of[q] == 0) cl_of[q] = k++;
-        cls.resize(k);
-    }
-    for (HostCluster& h : cls) {
-        h.mct = std::numeric_limits<double>::infinity();
-        h.step = std::numeric_limits<double>::infinity();
-        h.sleeping = true;
-    }
-    for (int p = 0; p < n; p++) {
-        if (is_static[p]) continue;
-        HostCluster& h = cls[cl_of[comp[p]]];
-        h.parts.push_back(p);
-        h.n_dyn++;
-        h.mct = dmin(h.mct, W.h_cur.p[14 * (size_t)p]);
-        h.step = dmin(h.step, W.h_last_dt.p[p]);
-        if (!W.h_sleeping.p[p]) h.sleeping = false;
-    }
-    for (int e = 0; e < nb; e++) {
-        const int a = B[2 * e], b = B[2 * e + 1];
-        if (is_static[a] && is_static[b]) continue;
-        const int dyn = is_static[a] ? b : a;
-        HostCluster& h = cls[cl_of[comp[dyn]]];
-        if (is_static[a] || is_static[b]) {
-            const int st = is_static[a] ? a : b;
-            bool in = false;
-            for (size_t q = h.n_dyn; q < h.parts.size(); q++) in = in || h.parts[q] == st;
-            if (!in) h.parts.push_back(st);
-        }
-        h.pairs.push_back(a);
-        h.pairs.push_back(b);
-    }
-    // :445-456 roll every moving body back to its cluster's minimum time
-    {
-        std::vector<double> t_body(n, -1.0);
-        for (const HostCluster& h : cls)
-            for (int q = 0; q < h.n_dyn; q++) t_body[h.parts[q]] = h.mct;
-        W.pk_round_d.clear();
-        const int i_t = W.pk_round_d.add(t_body);
-        RC(W.pk_round_d.upload(s));
-        RC(run_rollback(c, W.pk_round_d.ptr(i_t), W.err.p));
-        RC(check_err(c, W, "separateCollisionClusters"));
-    }
-    const int nc = (int)cls.size();
     W.mark(2);
     // :139-147 the earliest end of any cluster's step
     double min_final = std::numeric_limits<double>::infinity();
@@ -563,7 +509,7 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
             steps.push_back(cls[k].step);
             for (size_t q = cls[k].n_dyn; q < cls[k].parts.size(); q++) {
                 const int st = cls[k].parts[q];
-                if (!static_touched[st]) static_time[st] = W.h_cur.p[14 * (size_t)st];
+                if (!static_touched[st]) static_time[st] = h_st[15 * (size_t)W.slot_of[st]];
                 static_touched[st] = 1;
                 static_time[st] = static_time[st] + cls[k].step;
             }
@@ -627,16 +573,18 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         }
         for (int g = 0; g < n; g++) {
             if (last_r[g] < 0) continue;
-            W.h_last_dt.p[g] = M[last_r[g]].last_step;
-            W.h_sleeping.p[g] = (uint8_t)(M[last_r[g]].last_sleep ? 1 : 0);
-            D2G_CUDA(cudaMemcpyAsync(c->last_dt.p + g, W.h_last_dt.p + g, sizeof(double), cudaMemcpyHostToDevice, s));
-            D2G_CUDA(cudaMemcpyAsync(c->sleeping.p + g, W.h_sleeping.p + g, 1, cudaMemcpyHostToDevice, s));
+            double* ldt = h_st + 15 * (size_t)W.slot_of[g] + 14;
+            uint8_t* sl = W.h_sleeping.p + W.slot_of[g];
+            *ldt = M[last_r[g]].last_step;
+            *sl = (uint8_t)(M[last_r[g]].last_sleep ? 1 : 0);
+            D2G_CUDA(cudaMemcpyAsync(c->last_dt.p + g, ldt, sizeof(double), cudaMemcpyHostToDevice, s));
+            D2G_CUDA(cudaMemcpyAsync(c->sleeping.p + g, sl, 1, cudaMemcpyHostToDevice, s));
         }
     }
     // static bodies of sleeping clusters: the clock advanced, future = current
     for (int g = 0; g < n; g++) {
         if (!static_touched[g]) continue;
-        double* cur = W.h_cur.p + 14 * (size_t)g;
+        double* cur = h_st + 15 * (size_t)W.slot_of[g];
         cur[0] = static_time[g];
         D2G_CUDA(cudaMemcpyAsync(c->cur.p + 14 * (size_t)g, cur, 14 * sizeof(double), cudaMemcpyHostToDevice, s));
         D2G_CUDA(cudaMemcpyAsync(c->fut.p + 14 * (size_t)g, cur, 14 * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -674,11 +622,25 @@ extern "C" int d2g_world_configure(d2g_ctx* c, const float* local_aabb, float op
     W.warm.clear();
     for (int64_t& v : W.stats) v = 0;
     for (double& v : W.phase_ms) v = 0.0;
-    RC(W.h_last.ensure(14 * (size_t)n));
-    RC(W.h_cur.ensure(14 * (size_t)n));
-    RC(W.h_fut.ensure(14 * (size_t)n));
-    RC(W.h_last_dt.ensure(n));
-    RC(W.h_sleeping.ensure(n));
+    W.static_ids.clear();
+    W.slot_of.assign(n, -1);
+    W.n_dyn_total = 0;
+    for (int g = 0; g < n; g++) {
+        if (c->h_is_static[g]) {
+            W.slot_of[g] = (int)W.static_ids.size();
+            W.static_ids.push_back(g);
+        } else {
+            W.n_dyn_total++;
+        }
+    }
+    RC(W.d_aabb.ensure(6 * (size_t)n));
+    D2G_CUDA(cudaMemcpy(W.d_aabb.p, local_aabb, 6 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+    RC(W.d_static.ensure(W.static_ids.size() + 1));
+    RC(W.d_st_sleep.ensure(W.static_ids.size() + 1));
+    if (!W.static_ids.empty())
+        D2G_CUDA(cudaMemcpy(W.d_static.p, W.static_ids.data(), W.static_ids.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+    RC(W.h_sleeping.ensure(W.static_ids.size() + 1));
     RC(W.h_ri.ensure(64));
     RC(W.h_rd.ensure(64));
     RC(W.err.ensure(4));

@@ -169,6 +169,28 @@ int d2g_compare_trees_full_continuous_device(d2g_ctx* ctx, const int32_t* d_pair
                                              int32_t n_pairs, int32_t* n_contacts, const double** d_contacts,
                                              const int32_t** d_offsets, int64_t* counters);
 
+/* ------------------------------------------ broad phase on the device --
+ * broadPhaseEmbree(ParticleHandler&) over the context's device bodies
+ * (collision_detection/broad_phase_embree.cpp:87-116, 186-238, 266-289): the
+ * same pair set as d2g_broad_phase (float boxes, inclusive overlap, the
+ * swept-sphere filter within max(last_dt)), ascending (i, j), found by a
+ * sort-and-sweep on the GPU.  local_aabb: [n][6] host floats (Mesh::getAABB).
+ * D2G_ERR_STATE on an invalid state interpolation (the reference throws). */
+int d2g_ctx_broad_phase(d2g_ctx* ctx, const float* local_aabb, int32_t* pairs, int32_t capacity, int32_t* n_pairs);
+/* separateCollisionClusters (collision_detection/separate_clusters.cpp:
+ * 355-459) on the device: clusters are the components of the moving-moving
+ * pairs, numbered by their smallest body index (igl's labelling taken as
+ * breadth-first from the lowest index); a cluster's particles are its moving
+ * members ascending, then the static bodies it interacts with in order of
+ * first interaction; its interactions are the pairs in the given order.  The
+ * moving bodies' current states are rolled back to their cluster's minimum
+ * current time, as the reference does.  Clusters without a moving body are
+ * dropped.  Output sizes: particle_off and pair_off [n_bodies + 1], particles
+ * [n_bodies + n_pairs], cluster_pairs [2 n_pairs], min_current_time, step
+ * (minimum last_dt) and sleeping [n_bodies]. */
+int d2g_ctx_separate_clusters(d2g_ctx* ctx, const int32_t* pairs, int32_t n_pairs, int32_t* n_clusters,
+                              int32_t* particle_off, int32_t* particles, int32_t* pair_off, int32_t* cluster_pairs,
+                              double* min_current_time, double* step, uint8_t* sleeping);
 /* --------------------------------------------------- time-step selection --
  * fineCollisionClustersWithTimeStepSelection followed by the clamp of
  * TimeStepSelectionDynamicContinuous::selectTimeStep, for many clusters in one
