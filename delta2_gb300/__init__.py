@@ -78,7 +78,7 @@ def compare_trees_full_noalloc(device_scene, d_pairs, n_pairs, d_contacts, capac
 class SceneOpts(C.Structure):
     _fields_ = [("config", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("spacing", C.c_double), ("speed_sigma", C.c_double), ("seed", C.c_uint64), ("dt", C.c_float),
-                ("gravity_z", C.c_double), ("mu", C.c_double), ("hull_points", C.c_int32)]
+                ("gravity_z", C.c_double), ("mu", C.c_double), ("hull_points", C.c_int32), ("count", C.c_int32)]
 
 
 def library_path():
@@ -162,11 +162,70 @@ class Scene:
         return len(self.mesh)
 
 
+def concat_scenes(scenes):
+    """Independent scenes as one: trees and bodies concatenated (mesh ids and
+    the inner nodes' first-child indices shifted); returns the scene and the
+    scene index of every body.  Positions are left as they are, so every scene
+    computes exactly as it would alone."""
+    out = Scene()
+    node_base, mesh_base = 0, 0
+    offs, nodes, scene_of = [0], [], []
+    for k, sc in enumerate(scenes):
+        nd = np.array(sc.nodes, dtype=np.int32).copy()
+        inner = nd[:, 2] != 0
+        nd[inner, 0] += node_base
+        nodes.append(nd)
+        offs += [node_base + int(x) for x in sc.mesh_node_off[1:]]
+        node_base += len(nd)
+        scene_of.append(np.full(sc.n_bodies, k, np.int32))
+    out.mesh_node_off = np.array(offs, np.int32)
+    out.nodes = np.concatenate(nodes)
+    for f in ["ntris", "tris", "eps", "inner_eps"]:
+        setattr(out, f, np.concatenate([getattr(sc, f) for sc in scenes]))
+    meshes = []
+    for sc in scenes:
+        meshes.append(np.asarray(sc.mesh, np.int32) + mesh_base)
+        mesh_base += len(sc.mesh_node_off) - 1
+    out.mesh = np.concatenate(meshes)
+    for f in Scene.FIELDS_BODY:
+        if f != "mesh":
+            setattr(out, f, np.concatenate([getattr(sc, f) for sc in scenes]))
+    out.local_aabb = np.concatenate([sc.local_aabb for sc in scenes])
+    out.opt_dt = scenes[0].opt_dt
+    out.gravity_z = scenes[0].gravity_z
+    return out, np.concatenate(scene_of)
+
+
+def split_bodies(batch, scene_of, k):
+    """Body arrays of scene k out of a batched scene (a view for comparisons)."""
+    sel = scene_of == k
+    out = Scene()
+    for f in Scene.FIELDS_BODY:
+        setattr(out, f, getattr(batch, f)[sel])
+    return out
+
+
+def make_batch(n_scenes=256, seed=0, min_bodies=8, max_bodies=512, dt=0.0):
+    """The batched configuration: n_scenes independent mixed scenes (cubes,
+    64-point hulls and subdivision-2 icospheres in turn), each on its own
+    ground plane, with body counts drawn uniformly from [min_bodies,
+    max_bodies] by a seeded generator.  Returns (scene, scene_of_body,
+    per-scene list)."""
+    rng = np.random.default_rng(0xD2 + 3 + seed)
+    counts = rng.integers(min_bodies, max_bodies + 1, size=n_scenes)
+    scenes = []
+    for k, cnt in enumerate(counts):
+        nz = (int(cnt) + 63) // 64
+        scenes.append(make_scene(3, nx=8, ny=8, nz=nz, count=int(cnt), seed=seed * 100003 + k, dt=dt))
+    batch, scene_of = concat_scenes(scenes)
+    return batch, scene_of, scenes
+
+
 def make_scene(config=2, nx=0, ny=0, nz=0, spacing=0.0, speed_sigma=-1.0, seed=0, dt=0.0, gravity_z=-9.8, mu=0.0,
-               hull_points=64):
+               hull_points=64, count=0):
     """Synthetic scene of a benchmark configuration (host set-up, no GPU)."""
     L = lib()
-    o = SceneOpts(config, nx, ny, nz, spacing, speed_sigma, seed, dt, gravity_z, mu, hull_points)
+    o = SceneOpts(config, nx, ny, nz, spacing, speed_sigma, seed, dt, gravity_z, mu, hull_points, count)
     h = C.c_void_p()
     _check(L.d2g_scene_make(C.byref(o), C.byref(h)))
     try:
@@ -294,6 +353,11 @@ class Context:
     def set_bodies(self, scene):
         self._b = scene.bodies_struct()
         _check(lib().d2g_ctx_set_bodies(self.h, C.byref(self._b)))
+
+    def set_scenes(self, scene_of_body):
+        """Batch independent scenes: scene index of every body (after set_bodies)."""
+        self._scene_of = np.ascontiguousarray(scene_of_body, dtype=np.int32)
+        _check(lib().d2g_ctx_set_scenes(self.h, _p(self._scene_of, I32P)))
 
     def get_bodies(self, scene=None):
         scene = scene or self.scene

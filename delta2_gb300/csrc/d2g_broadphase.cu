@@ -58,8 +58,8 @@ __device__ __forceinline__ float fmax_ref(float a, float b) { return (a < b) ? b
 __global__ void k_bp_boxes(int n, const uint8_t* __restrict__ is_static, const double* __restrict__ last,
                            const double* __restrict__ cur, const double* __restrict__ fut,
                            const double* __restrict__ radius, const double* __restrict__ geo_eps,
-                           const float* __restrict__ aabb, float* __restrict__ box, uint32_t* __restrict__ key,
-                           int32_t* __restrict__ idx) {
+                           const float* __restrict__ aabb, const int32_t* __restrict__ scene,
+                           float* __restrict__ box, unsigned long long* __restrict__ key, int32_t* __restrict__ idx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float lo[3], hi[3];
@@ -108,9 +108,11 @@ __global__ void k_bp_boxes(int n, const uint8_t* __restrict__ is_static, const d
         box[6 * (size_t)i + 3 + k] = hi[k];
         finite = finite && lo[k] == lo[k] && hi[k] == hi[k];
     }
-    // order-preserving key of lower x (NaN boxes sort last and overlap nothing)
+    // scene, then an order-preserving key of lower x (NaN boxes sort last in
+    // their scene and overlap nothing)
     const uint32_t u = __float_as_uint(lo[0]);
-    key[i] = finite ? ((u & 0x80000000u) ? ~u : (u | 0x80000000u)) : 0xffffffffu;
+    const uint32_t xk = finite ? ((u & 0x80000000u) ? ~u : (u | 0x80000000u)) : 0xffffffffu;
+    key[i] = ((unsigned long long)(uint32_t)scene[i] << 32) | xk;
     idx[i] = finite ? i : -1 - i;
 }
 
@@ -123,8 +125,8 @@ __device__ __forceinline__ bool boxes_overlap(const float* a, const float* b) {
 // Sweep along x over the sorted boxes: count (pass 0) or write (pass 1) the
 // box-overlapping pairs (min, max) of each sorted position.
 __global__ void k_bp_sweep(int n, const int32_t* __restrict__ order, const float* __restrict__ box,
-                           const uint8_t* __restrict__ is_static, const int32_t* __restrict__ off,
-                           int32_t* __restrict__ cnt, int32_t* __restrict__ out) {
+                           const uint8_t* __restrict__ is_static, const int32_t* __restrict__ scene,
+                           const int32_t* __restrict__ off, int32_t* __restrict__ cnt, int32_t* __restrict__ out) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= n) return;
     const int p = order[u];
@@ -134,7 +136,8 @@ __global__ void k_bp_sweep(int n, const int32_t* __restrict__ order, const float
         int w = off ? off[u] : 0;
         for (int v = u + 1; v < n; v++) {
             const int q = order[v];
-            if (q < 0) break;  // the NaN boxes come last
+            if (q < 0) break;  // the NaN boxes come last in a scene
+            if (scene[q] != scene[p]) break;
             const float* bq = box + 6 * (size_t)q;
             if (bq[0] > bp[3]) break;
             if (is_static[p] && is_static[q]) continue;
@@ -431,10 +434,12 @@ int run_broad_phase(d2g_ctx* ctx, const float* d_aabb, int* n_out, int32_t* d_er
     RC(E.bp_cnt.ensure(n + 1));
     RC(E.bp_off.ensure(n + 1));
     BLAUNCH(k_bp_boxes, n, n, ctx->is_static.p, ctx->last.p, ctx->cur.p, ctx->fut.p, ctx->bounding_radius.p,
-            ctx->geo_eps.p, d_aabb, E.bp_box.p, E.bp_key.p, E.bp_idx.p);
-    RC(sort_pairs(ctx, E.bp_key.p, E.bp_key_s.p, E.bp_idx.p, E.bp_order.p, n, 32));
-    BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, (const int32_t*)nullptr, E.bp_cnt.p,
-            (int32_t*)nullptr);
+            ctx->geo_eps.p, d_aabb, ctx->scene.p, E.bp_box.p, E.bp_key.p, E.bp_idx.p);
+    int scene_bits = 0;
+    while (scene_bits < 31 && (1 << scene_bits) < ctx->n_scenes) scene_bits++;
+    RC(sort_pairs(ctx, E.bp_key.p, E.bp_key_s.p, E.bp_idx.p, E.bp_order.p, n, 32 + scene_bits));
+    BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, ctx->scene.p, (const int32_t*)nullptr,
+            E.bp_cnt.p, (int32_t*)nullptr);
     RC(bscan(ctx, E.bp_cnt.p, E.bp_off.p, n));
     int n_cand = 0;
     const int32_t* src = E.bp_off.p + n;
@@ -446,8 +451,8 @@ int run_broad_phase(d2g_ctx* ctx, const float* d_aabb, int* n_out, int32_t* d_er
     RC(E.bp_pkey2.ensure(n_cand + 1));
     int n_pairs = 0;
     if (n_cand > 0) {
-        BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, E.bp_off.p, (int32_t*)nullptr,
-                E.bp_cand.p);
+        BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, ctx->scene.p, E.bp_off.p,
+                (int32_t*)nullptr, E.bp_cand.p);
         BLAUNCH(k_bp_filter, n_cand, n_cand, E.bp_cand.p, ctx->is_static.p, ctx->last.p, ctx->cur.p,
                 ctx->bounding_radius.p, ctx->geo_eps.p, ctx->last_dt.p, E.bp_pkey.p, E.bp_flag.p, d_err);
         RC(bscan(ctx, E.bp_flag.p, E.bp_foff.p, n_cand));

@@ -110,6 +110,7 @@ int d2g_scene_make(const d2g_scene_opts* o, d2g_scene** out) {
     so.gravity_z = o->gravity_z;
     so.mu = o->mu;
     so.hull_points = o->hull_points > 3 ? o->hull_points : 64;
+    so.count = o->count;
     d2g_scene* s = new d2g_scene();
     std::string err;
     if (!d2g::make_scene(so, s->s, &err)) {
@@ -424,6 +425,11 @@ int d2g_ctx_set_bodies(d2g_ctx* c, const d2g_bodies* b) {
         RC(c->sleeping.ensure(n));
         D2G_CUDA(cudaMemsetAsync(c->sleeping.p, 0, n, c->stream));
     }
+    // one scene until d2g_ctx_set_scenes says otherwise
+    RC(c->scene.ensure(n));
+    D2G_CUDA(cudaMemsetAsync(c->scene.p, 0, n * sizeof(int32_t), c->stream));
+    c->h_scene.assign(n, 0);
+    c->n_scenes = 1;
     c->h_is_static.assign(b->is_static, b->is_static + n);
     c->h_geo_eps.assign(b->geo_eps, b->geo_eps + n);
     if (b->bounding_radius)
@@ -432,6 +438,27 @@ int d2g_ctx_set_bodies(d2g_ctx* c, const d2g_bodies* b) {
         c->h_bounding_radius.clear();
     D2G_CUDA(cudaStreamSynchronize(c->stream));
     c->n_bodies = b->n;
+    return D2G_OK;
+}
+
+int d2g_ctx_set_scenes(d2g_ctx* c, const int32_t* scene_of_body) {
+    if (!c || !scene_of_body || c->n_bodies <= 0) {
+        set_error("set the bodies before their scenes");
+        return D2G_ERR_STATE;
+    }
+    int n_scenes = 1;
+    for (int i = 0; i < c->n_bodies; i++) {
+        if (scene_of_body[i] < 0) {
+            set_error("negative scene index");
+            return D2G_ERR_INVALID;
+        }
+        n_scenes = std::max(n_scenes, scene_of_body[i] + 1);
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    RC(upload(c, c->scene, scene_of_body, (size_t)c->n_bodies));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    c->h_scene.assign(scene_of_body, scene_of_body + c->n_bodies);
+    c->n_scenes = n_scenes;
     return D2G_OK;
 }
 

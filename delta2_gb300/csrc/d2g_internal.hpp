@@ -146,7 +146,7 @@ struct Engine {
     DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
     // GPU broad phase (d2g_broadphase.cu)
     DBuf<float> bp_box;
-    DBuf<uint32_t> bp_key, bp_key_s;
+    DBuf<unsigned long long> bp_key, bp_key_s;
     DBuf<int32_t> bp_idx, bp_order, bp_cnt, bp_off, bp_cand, bp_flag, bp_foff, bp_pairs;
     DBuf<unsigned long long> bp_pkey, bp_pkey2;
     // GPU cluster separation (d2g_broadphase.cu)
@@ -205,6 +205,10 @@ struct d2g_ctx {
     d2g::DBuf<int32_t> mesh, sleep_steps;
     d2g::DBuf<uint8_t> is_static, sleeping;
     d2g::DBuf<double> geo_eps, mu, mass, inv_inertia, last, cur, fut, last_dt, bounding_radius;
+    // independent scenes batched in one context: scene of every body
+    d2g::DBuf<int32_t> scene;
+    std::vector<int32_t> h_scene;
+    int n_scenes = 1;
     // host copies of the constant body data the host-side stepper reads
     std::vector<uint8_t> h_is_static;
     std::vector<double> h_geo_eps, h_bounding_radius;

@@ -118,6 +118,7 @@ struct HostCluster {
     double mct = 0.0, step = 0.0;
     bool sleeping = true;
     int n_dyn = 0;
+    int scene = 0;
 };
 
 struct Frame {
@@ -450,12 +451,15 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
     }
     W.mark(2);
     // :139-147 the earliest end of any cluster's step
-    double min_final = std::numeric_limits<double>::infinity();
-    for (const HostCluster& h : cls) min_final = dmin(min_final, h.mct + h.step);
+    // (per scene: every scene is scheduled as its own world)
+    const double inf = std::numeric_limits<double>::infinity();
+    std::vector<double> min_final_s(c->n_scenes, inf), fine_s(c->n_scenes, inf);
+    for (HostCluster& h : cls) h.scene = c->h_scene[h.parts[0]];
+    for (const HostCluster& h : cls) min_final_s[h.scene] = dmin(min_final_s[h.scene], h.mct + h.step);
     // :149-170 time-step selection for the awake clusters that start in time
     std::vector<int> sel;
     for (int k = 0; k < nc; k++)
-        if (!(cls[k].mct > min_final) && !cls[k].sleeping) sel.push_back(k);
+        if (!(cls[k].mct > min_final_s[cls[k].scene]) && !cls[k].sleeping) sel.push_back(k);
     if (!sel.empty()) {
         std::vector<int32_t> pairs, pair_off(1, 0), part_off(1, 0), parts;
         for (int k : sel) {
@@ -487,15 +491,15 @@ int world_step_once(d2g_ctx* c, WorldState& W) {
         W.stats[10] += cnt[2];
     }
     W.mark(3);
-    double fine_min_final = std::numeric_limits<double>::infinity();
     for (int k = 0; k < nc; k++) {
-        if (cls[k].mct > min_final) continue;
-        fine_min_final = dmin(fine_min_final, cls[k].mct + (cls[k].sleeping ? opt_dt : cls[k].step));
+        const int sc = cls[k].scene;
+        if (cls[k].mct > min_final_s[sc]) continue;
+        fine_s[sc] = dmin(fine_s[sc], cls[k].mct + (cls[k].sleeping ? opt_dt : cls[k].step));
     }
     // :172-255 the clusters that start before the earliest end step
     std::vector<int> sleepers, R;
     for (int k = 0; k < nc; k++) {
-        if (cls[k].mct > fine_min_final) continue;
+        if (cls[k].mct > fine_s[cls[k].scene]) continue;
         (cls[k].sleeping ? sleepers : R).push_back(k);
     }
     std::vector<double> static_time(n, 0.0);

@@ -830,27 +830,48 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
         shared_mesh = scene_add_mesh(s, shared, tree_rng, err);
         if (shared_mesh < 0) return false;
     }
+    constexpr int kMixHulls = 4;
+    int mix_mesh[2 + kMixHulls];
+    Mesh mix_geom[2 + kMixHulls];
+    MassProps mix_mp[2 + kMixHulls];
+    for (int k = 0; k < 2 + kMixHulls; k++) mix_mesh[k] = -1;
     const double cx = 0.5 * (nx - 1) * spacing, cy = 0.5 * (ny - 1) * spacing;
     int body = 0;
     for (int iz = 0; iz < nz; iz++)
         for (int iy = 0; iy < ny; iy++)
             for (int ix = 0; ix < nx; ix++, body++) {
+                if (o.count > 0 && body >= o.count) break;
                 Mesh m;
                 MassProps mp;
                 int mesh_id = shared_mesh;
                 if (o.config != 1) {
                     int kind = o.config == 3 ? body % 3 : (o.config == 2 ? 1 : 2);
-                    if (kind == 0)
-                        m = make_cube(0.5);
-                    else if (kind == 1)
-                        m = make_hull(o.hull_points, half, rng);
-                    else
-                        m = make_icosphere(o.config == 5 ? 3 : 2, half, o.config == 5 ? 0.2 : 0.0, &rng);
-                    mp = mass_volume(m);
-                    shift_vertices(m, mp.com);
-                    mp.com[0] = mp.com[1] = mp.com[2] = 0.0;
-                    mesh_id = scene_add_mesh(s, m, tree_rng, err);
-                    if (mesh_id < 0) return false;
+                    // The mixed configuration shares meshes as the reference
+                    // shares MeshData: one cube, one icosphere and a pool of
+                    // kMixHulls hulls per scene, each built on first use.
+                    const int slot = kind == 0 ? 0 : (kind == 2 ? 1 : 2 + (body / 3) % kMixHulls);
+                    if (o.config == 3 && mix_mesh[slot] >= 0) {
+                        m = mix_geom[slot];
+                        mp = mix_mp[slot];
+                        mesh_id = mix_mesh[slot];
+                    } else {
+                        if (kind == 0)
+                            m = make_cube(0.5);
+                        else if (kind == 1)
+                            m = make_hull(o.hull_points, half, rng);
+                        else
+                            m = make_icosphere(o.config == 5 ? 3 : 2, half, o.config == 5 ? 0.2 : 0.0, &rng);
+                        mp = mass_volume(m);
+                        shift_vertices(m, mp.com);
+                        mp.com[0] = mp.com[1] = mp.com[2] = 0.0;
+                        mesh_id = scene_add_mesh(s, m, tree_rng, err);
+                        if (mesh_id < 0) return false;
+                        if (o.config == 3) {
+                            mix_mesh[slot] = mesh_id;
+                            mix_geom[slot] = m;
+                            mix_mp[slot] = mp;
+                        }
+                    }
                 } else {
                     m = shared;
                     mp = shared_mp;

@@ -82,6 +82,7 @@ struct SceneOpts {
     double gravity_z = -9.8;
     double mu = 0;
     int hull_points = 64;
+    int count = 0;  // > 0: bodies only in the first `count` grid cells
 };
 bool make_scene(const SceneOpts& o, Scene& s, std::string* err);
 

@@ -92,6 +92,7 @@ typedef struct d2g_scene_opts {
     double gravity_z;
     double mu;          /* 0 = default */
     int32_t hull_points;
+    int32_t count;      /* > 0: only the first `count` grid cells get a body */
 } d2g_scene_opts;
 
 typedef struct d2g_scene d2g_scene;
@@ -128,6 +129,12 @@ int d2g_ctx_sync(d2g_ctx* ctx);
  * MeshData / ParticleHandler ownership). */
 int d2g_ctx_set_trees(d2g_ctx* ctx, const d2g_trees* trees);
 int d2g_ctx_set_bodies(d2g_ctx* ctx, const d2g_bodies* bodies);
+/* Independent scenes batched in one context (no counterpart in the reference,
+ * whose process steps one world): scene index of every body.  Bodies of
+ * different scenes never pair, and the stepper schedules every scene as its
+ * own world (BroadPhaseEmbreeCluster::step per scene), so each scene evolves
+ * exactly as it would alone.  d2g_ctx_set_bodies resets all bodies to scene 0. */
+int d2g_ctx_set_scenes(d2g_ctx* ctx, const int32_t* scene_of_body);
 /* Copy the device body states (last/cur/fut, last_dt, sleep_steps, sleeping) back. */
 int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
 
