@@ -54,6 +54,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget (single thread)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--world-steps", type=int, default=24, help="outer steps timed for steps/s")
+    p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched configuration (0: skip)")
+    p.add_argument("--batch-steps", type=int, default=3, help="outer steps timed on the batched configuration")
     p.add_argument("--cpu-step-seconds", type=float, default=20.0, help="oracle stepper sample budget")
     p.add_argument("--seed", type=int, default=0)
     return p.parse_args()
@@ -250,6 +252,9 @@ def run_ours(args):
         import torch.distributed as dist
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     steps_line["value"] = world * 1e3 / float(t.item())
+    batch_line, batch_scenes = (None, None)
+    if args.batch_scenes > 0:
+        batch_line, batch_scenes = batched_steps(local_rank, args)
 
     if rank != 0:
         ctx.close()
@@ -278,6 +283,8 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, pairs, mt, args.cpu_seconds)
         steps_line["cpu_baseline"] = cpu_world_steps(steps_scene, steps_per, args.cpu_step_seconds)
+        if batch_line is not None:
+            batch_line["cpu_baseline"] = cpu_batched_steps(batch_scenes, args.cpu_step_seconds)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -287,7 +294,7 @@ def run_ours(args):
                    "dt": scene.opt_dt, "l2": "flushed before every timed step (512 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
-        "kernel_time_share": kernel_share, "world_steps": steps_line,
+        "kernel_time_share": kernel_share, "world_steps": steps_line, "batched_steps": batch_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
     }
@@ -431,6 +438,74 @@ def world_steps(local_rank, args):
                    "d2h_bytes_per_step": int(d2h),
                    "path": "d2g_world_step + d2g_ctx_get_bodies into pinned host memory every step"}}
     return out, s0, per_step
+
+
+def batched_steps(local_rank, args):
+    """The batched configuration (independent mixed scenes of 8-512 bodies,
+    one context): outer steps/s of every scene at once, and the same scenes
+    stepped one at a time on the GPU (one context each) for comparison."""
+    import delta2_gb300 as D
+
+    t0 = time.perf_counter()
+    batch, scene_of, scenes = D.make_batch(args.batch_scenes, seed=args.seed)
+    build_s = time.perf_counter() - t0
+    ctx = D.Context(local_rank)
+    ctx.set_scene(batch.copy())
+    ctx.set_scenes(scene_of)
+    ctx.world_configure(batch)
+    ctx.world_step(max(1, min(args.warmup, 2)))
+    ctx.world_configure(batch)
+    l0 = ctx.launches()
+    t0 = time.perf_counter()
+    ctx.world_step(args.batch_steps)
+    wall = time.perf_counter() - t0
+    launches = ctx.launches() - l0
+    stats = ctx.world_stats()
+    phases = ctx.world_timing()
+    ctx.close()
+    ctxs = []
+    for sc in scenes:
+        x = D.Context(local_rank)
+        x.set_scene(sc.copy())
+        x.world_configure(sc)
+        x.world_step(max(1, min(args.warmup, 2)))
+        ctxs.append(x)
+    t0 = time.perf_counter()
+    for _ in range(args.batch_steps):
+        for x in ctxs:
+            x.world_step(1)
+    wall_plain = time.perf_counter() - t0
+    for x in ctxs:
+        x.close()
+    k = args.batch_steps
+    return {"metric": "steps/s", "value": k / wall, "unit": "steps/s (every scene one outer step)",
+            "scenes": len(scenes), "bodies": int(batch.n_bodies), "ms_per_step": 1e3 * wall / k,
+            "gpu_launches": launches, "build_s": build_s,
+            "one_scene_at_a_time": {"value": k / wall_plain, "unit": "steps/s", "ms_per_step": 1e3 * wall_plain / k,
+                                    "path": "one context per scene, d2g_world_step per scene in turn"},
+            "phase_ms_per_step": {kk: v / k for kk, v in phases.items() if kk != "reserved"},
+            "stats_per_step": {kk: v / k for kk, v in stats.items()}}, scenes
+
+
+def cpu_batched_steps(scenes, budget_s):
+    """The oracle stepper over the batch's scenes in turn (one outer step
+    each) for about budget_s seconds, scaled to whole-batch steps/s."""
+    from oracle import oracle as O
+
+    done, t0 = 0, time.perf_counter()
+    for sc in scenes:
+        if time.perf_counter() - t0 > budget_s:
+            break
+        w = O.World(sc.copy(), sc.opt_dt, sc.gravity_z)
+        if w.step(1) != 0:
+            break
+        done += 1
+    dt = time.perf_counter() - t0
+    if done == 0:
+        return None
+    return {"value": (done / len(scenes)) / dt, "unit": "steps/s (every scene one outer step)", "cores": 1,
+            "kind": "port", "sample": f"the first outer step of {done} of the {len(scenes)} scenes, {dt:.1f} s "
+                                      f"single-threaded, CPU oracle g++ -O2, scaled by scene count"}
 
 
 def cpu_world_steps(scene, per_step_gpu, budget_s):

@@ -552,3 +552,62 @@ class Context:
                 continue
             _check(rc)
             return out[:off[-1]].copy(), off, cnt
+
+
+MLP_PARAMS = 19458
+
+
+class Mlp:
+    """The learned TOI proposal network (d2g_mlp_*): 20-128-128-2, SiLU, BF16
+    weights and activations, trained by the library's own kernels."""
+
+    def __init__(self, ctx, seed=0):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        _check(lib().d2g_mlp_create(ctx.h, C.c_uint64(seed), C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().d2g_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        _check(lib().d2g_mlp_params(self.h, _p(p, F32P), MLP_PARAMS))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().d2g_mlp_set_params(self.h, _p(p, F32P), MLP_PARAMS))
+
+    def set_normalization(self, mean, std):
+        m = np.ascontiguousarray(mean, dtype=np.float32)
+        sd = np.ascontiguousarray(std, dtype=np.float32)
+        self._norm = (m, sd)
+        _check(lib().d2g_mlp_set_normalization(self.h, _p(m, F32P), _p(sd, F32P)))
+
+    def predict(self, feats):
+        f = np.ascontiguousarray(feats, dtype=np.float32).reshape(-1, 20)
+        out = np.zeros((max(1, len(f)), 2), np.float32)
+        _check(lib().d2g_mlp_predict(self.h, _p(f, F32P), len(f), _p(out, F32P)))
+        return out[:len(f)]
+
+    def gradient(self, feats, targets):
+        f = np.ascontiguousarray(feats, dtype=np.float32).reshape(-1, 20)
+        y = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1, 2)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(lib().d2g_mlp_gradient(self.h, _p(f, F32P), _p(y, F32P), len(f), _p(g, F32P), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, feats, targets, epochs=1, batch=4096, lr=1e-3, seed=0):
+        f = np.ascontiguousarray(feats, dtype=np.float32).reshape(-1, 20)
+        y = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1, 2)
+        losses = np.zeros(max(1, epochs), np.float32)
+        _check(lib().d2g_mlp_train(self.h, _p(f, F32P), _p(y, F32P), len(f), int(epochs), int(batch),
+                                   C.c_float(lr), C.c_uint64(seed), _p(losses, F32P)))
+        return losses[:epochs]
+

@@ -268,6 +268,30 @@ int d2g_world_warm(d2g_ctx* ctx, int32_t* keys, double* values, int32_t capacity
  * 7 solve and state shift, 8 recursion bookkeeping and static bodies. */
 #define D2G_WORLD_PHASES 10
 int d2g_world_timing(d2g_ctx* ctx, double* ms, int32_t n);
+/* ------------------------------------------- learned TOI proposal (MLP) --
+ * No counterpart in the reference.  A 20-128-128-2 MLP with SiLU, BF16
+ * weights and activations and FP32 accumulation, trained and run by this
+ * library's own tensor-core kernels.  Input: the 20 FP32 features of a CCD
+ * pair query (B's pose in A's frame: rotation 3x3 row major and translation;
+ * relative linear and angular velocity in A's frame; the two bodies' bounding
+ * radii), standardised with d2g_mlp_set_normalization.  Output per query:
+ * (normalised time of impact, hit logit).  Loss: squared TOI error plus the
+ * hit's binary cross-entropy, averaged over the batch.  Parameters (FP32
+ * master copy, D2G_MLP_PARAMS floats): W1 [128][20], b1 [128], W2 [128][128],
+ * b2 [128], W3 [2][128], b3 [2].  Training is Adam (0.9, 0.999, 1e-8) over
+ * shuffled mini-batches. */
+#define D2G_MLP_PARAMS 19458
+typedef struct d2g_mlp d2g_mlp;
+int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out);
+void d2g_mlp_destroy(d2g_mlp* mlp);
+int d2g_mlp_params(d2g_mlp* mlp, float* params, int32_t n);
+int d2g_mlp_set_params(d2g_mlp* mlp, const float* params, int32_t n);
+int d2g_mlp_set_normalization(d2g_mlp* mlp, const float* mean20, const float* std20);
+int d2g_mlp_predict(d2g_mlp* mlp, const float* features, int32_t n, float* out);
+/* Gradient of the mean loss over n samples (targets [n][2]: TOI, hit). */
+int d2g_mlp_gradient(d2g_mlp* mlp, const float* features, const float* targets, int32_t n, float* grad, float* loss);
+int d2g_mlp_train(d2g_mlp* mlp, const float* features, const float* targets, int32_t n, int32_t epochs, int32_t batch,
+                  float lr, uint64_t seed, float* epoch_loss);
 /* ------------------------------------ allocation-free discrete narrow phase
  * No counterpart in the reference.  The same compareTreesFull traversal and
  * contacts as d2g_compare_trees_full, for callers that may not allocate
