@@ -80,3 +80,49 @@ def dataset(ctx, n_queries, seed=0, **kw):
         total += len(f)
         k += 1
     return np.concatenate(feats)[:n_queries], np.concatenate(targs)[:n_queries]
+
+
+def report(ctx, n_train=1_800_000, n_test=200_000, epochs=8, batch=4096, lr=2e-3, seed=0):
+    """Train on n_train queries (cube scenes of one seed range), evaluate on
+    n_test queries of other seeds; returns a dict of the figures."""
+    import time
+
+    t0 = time.perf_counter()
+    f_tr, y_tr = dataset(ctx, n_train, seed=2 * seed + 1)
+    f_te, y_te = dataset(ctx, n_test, seed=2 * seed + 2)
+    gen_s = time.perf_counter() - t0
+    net = D.Mlp(ctx, seed=seed)
+    net.set_normalization(f_tr.mean(0), f_tr.std(0))
+    t0 = time.perf_counter()
+    losses = net.train(f_tr, y_tr, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    train_s = time.perf_counter() - t0
+    net.predict(f_te[:4096])
+    t0 = time.perf_counter()
+    out = net.predict(f_te)
+    pred_s = time.perf_counter() - t0
+    hit = y_te[:, 1] > 0.5
+    ph = out[:, 1] > 0
+    toi_err = np.abs(np.clip(out[hit, 0], 0, 1) - y_te[hit, 0])
+    return {
+        "train_queries": int(len(f_tr)), "test_queries": int(len(f_te)), "hit_rate": float(hit.mean()),
+        "epochs": epochs, "loss_per_epoch": [float(x) for x in losses],
+        "hit_accuracy": float(np.mean(ph == hit)), "hit_recall": float(np.mean(ph[hit])) if hit.any() else None,
+        "miss_rate": float(np.mean(~ph[hit])) if hit.any() else None,
+        "false_alarm_rate": float(np.mean(ph[~hit])) if (~hit).any() else None,
+        "toi_mae_on_hits": float(toi_err.mean()) if hit.any() else None,
+        "toi_p90_err_on_hits": float(np.quantile(toi_err, 0.9)) if hit.any() else None,
+        "train_samples_per_s": len(f_tr) * epochs / train_s, "predict_samples_per_s_e2e": len(f_te) / pred_s,
+        "data_generation_s": gen_s,
+    }
+
+
+if __name__ == "__main__":
+    import json
+    import sys
+
+    ctx = D.Context(0)
+    kw = {}
+    if len(sys.argv) > 1:
+        kw["n_train"] = int(sys.argv[1])
+        kw["n_test"] = max(1000, int(sys.argv[1]) // 9)
+    print(json.dumps(report(ctx, **kw)))
