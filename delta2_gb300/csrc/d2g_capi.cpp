@@ -381,6 +381,9 @@ int d2g_ctx_set_trees(d2g_ctx* c, const d2g_trees* t) {
             eu[k] = std::nextafter((float)t->eps[k], INFINITY);
         }
         RC(upload(c, c->tri_sph, sph.data(), sph.size()));
+        std::vector<float> t32(72 * (size_t)N);
+        for (size_t k = 0; k < t32.size(); k++) t32[k] = (float)t->tris[k];
+        RC(upload(c, c->tri32, t32.data(), t32.size()));
         RC(upload(c, c->eps_up, eu.data(), eu.size()));
     }
     D2G_CUDA(cudaStreamSynchronize(c->stream));

@@ -177,6 +177,243 @@ __device__ __forceinline__ void store_prim(PrimResult* __restrict__ r, double di
     r->toc = toc;
 }
 
+// ---------------------------------------------- FP32 candidate filtering ---
+// Every primitive CCD test returns a distance between a point of a box built
+// from its inputs and a point of a second box: for edgeEdgeCCD the world
+// positions of the two edges' endpoints at the start and the end; for
+// pointTriCCDLinear the point carried into the triangle's frame at the start
+// and the end, then through the triangle body's start and end transforms, and
+// the triangle's vertices through the same two transforms (the returned
+// points are lerps of those).  A box gap above the hit threshold means the
+// test cannot hit (a soup sub-test with such a distance can never be the best
+// of a triangle pair that hits), so the test is recorded as no contact (+inf)
+// and left out of the FP64 work list.  The gap is computed in FP32 and only
+// used beyond a margin (1 mm plus 4e-6 of the largest coordinate involved)
+// far above the FP32 and FP64 rounding at scene scale.
+
+struct Box32 {
+    float lo[3], hi[3];
+};
+__device__ __forceinline__ void box_init(Box32& b) {
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = 3.4e38f;
+        b.hi[k] = -3.4e38f;
+    }
+}
+// adds M (3x4 rows, FP32) applied to (x, y, z); returns the point in o
+__device__ __forceinline__ void box_add(Box32& b, const float* M, float x, float y, float z, float* o, float& mag) {
+    for (int r = 0; r < 3; r++) {
+        const float v = M[4 * r] * x + M[4 * r + 1] * y + M[4 * r + 2] * z + M[4 * r + 3];
+        o[r] = v;
+        b.lo[r] = fminf(b.lo[r], v);
+        b.hi[r] = fmaxf(b.hi[r], v);
+        mag = fmaxf(mag, fabsf(v));
+    }
+}
+__device__ __forceinline__ float box_gap(const Box32& a, const Box32& b) {
+    float g2 = 0.f;
+    for (int k = 0; k < 3; k++) {
+        const float g = fmaxf(b.lo[k] - a.hi[k], a.lo[k] - b.hi[k]);
+        if (g > 0.f) g2 += g * g;
+    }
+    return sqrtf(g2);
+}
+
+// Indices of PM_* matrices in the FP32 pose block (8 x 12 floats per pair).
+__device__ __forceinline__ const float* pm32_of(const float* pm32, int pair, int which) {
+    return pm32 + (size_t)96 * pair + 12 * which;
+}
+enum { P32_AS = 0, P32_AE, P32_BS, P32_BE, P32_ABS, P32_ABE, P32_BAS, P32_BAE };
+
+__global__ void k_ccd_pm32(int n, const double* __restrict__ pm, float* __restrict__ pm32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * 96) return;
+    const int p = i / 96, w = (i % 96) / 12, r = i % 12;
+    pm32[i] = (float)pm[(size_t)PM_SIZE * p + 16 * w + r];
+}
+
+// Point-triangle work item j (the decoding of k_prim_pt): which pair, which
+// point (body-local), which triangle (body-local) and which transforms.
+struct PtWork {
+    int pair, pt_node, pt_tri, pt_vert, tri_node, tri_idx, mC, mT;  // mC: point frame pair, mT: triangle body
+    PrimResult* out;
+    int32_t* hit;
+};
+__device__ __forceinline__ PtWork decode_pt(int j, int n_tp, const int32_t* items, const Entry* soup,
+                                            const Entry* conn, const int32_t* nn_off, int n_conn,
+                                            const int32_t* ntris, PrimResult* sub, PrimResult* cres, int32_t* chit) {
+    PtWork w;
+    w.hit = nullptr;
+    if (j < 6 * n_tp) {
+        const int k = j / 6, q = j % 6;
+        const int slot = items[k];
+        const Entry e = soup[slot >> 6];
+        const int i = q >> 1;
+        w.pair = e.pair;
+        if (q & 1) {
+            w.pt_node = e.nb, w.pt_tri = slot & 7, w.tri_node = e.na, w.tri_idx = (slot >> 3) & 7;
+            w.mC = P32_BAS, w.mT = P32_AS;
+        } else {
+            w.pt_node = e.na, w.pt_tri = (slot >> 3) & 7, w.tri_node = e.nb, w.tri_idx = slot & 7;
+            w.mC = P32_ABS, w.mT = P32_BS;
+        }
+        w.pt_vert = i;
+        w.out = sub + 15 * (size_t)k + 5 * i + (q & 1);
+        return w;
+    }
+    const int jp = j - 6 * n_tp;
+    const int ei = find_entry(nn_off, n_conn, 6, jp);
+    const Entry e = conn[ei];
+    const int l = jp - 6 * nn_off[ei];
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    const int n1 = 3 * na * nb;
+    w.pair = e.pair;
+    if (l < n1) {
+        const int vi = l / nb, jj = l % nb;
+        w.pt_node = e.na, w.pt_tri = vi / 3, w.pt_vert = vi % 3, w.tri_node = e.nb, w.tri_idx = jj;
+        w.mC = P32_ABS, w.mT = P32_BS;
+    } else {
+        const int m = l - n1;
+        const int vi = m / na, jj = m % na;
+        w.pt_node = e.nb, w.pt_tri = vi / 3, w.pt_vert = vi % 3, w.tri_node = e.na, w.tri_idx = jj;
+        w.mC = P32_BAS, w.mT = P32_AS;
+    }
+    const size_t item = 15 * (size_t)nn_off[ei] + l;
+    w.out = cres + item;
+    w.hit = chit + item;
+    return w;
+}
+
+// Edge-edge work item j (the decoding of k_prim_ee).
+struct EeWork {
+    int pair, na, nb, aTri, aEdge, bTri, bEdge;
+    PrimResult* out;
+    int32_t* hit;
+};
+__device__ __forceinline__ EeWork decode_ee(int j, int n_tp, const int32_t* items, const Entry* soup,
+                                            const Entry* conn, const int32_t* nn_off, int n_conn,
+                                            const int32_t* ntris, PrimResult* sub, PrimResult* cres, int32_t* chit) {
+    EeWork w;
+    w.hit = nullptr;
+    Entry e;
+    if (j < 9 * n_tp) {
+        const int k = j / 9, q = j % 9;
+        const int slot = items[k];
+        e = soup[slot >> 6];
+        w.aTri = (slot >> 3) & 7;
+        w.bTri = slot & 7;
+        w.aEdge = q / 3;
+        w.bEdge = q % 3;
+        w.out = sub + 15 * (size_t)k + 5 * w.aEdge + 2 + w.bEdge;
+    } else {
+        const int jp = j - 9 * n_tp;
+        const int ei = find_entry(nn_off, n_conn, 9, jp);
+        e = conn[ei];
+        const int m = jp - 9 * nn_off[ei];
+        const int na = ntris[e.na], nb = ntris[e.nb];
+        const int ea = m / (3 * nb), eb = m % (3 * nb);
+        w.aTri = ea / 3;
+        w.aEdge = ea % 3;
+        w.bTri = eb / 3;
+        w.bEdge = eb % 3;
+        const size_t item = 15 * (size_t)nn_off[ei] + 6 * (size_t)na * nb + m;
+        w.out = cres + item;
+        w.hit = chit + item;
+    }
+    w.pair = e.pair;
+    w.na = e.na;
+    w.nb = e.nb;
+    return w;
+}
+
+__device__ __forceinline__ void record_no_contact(PrimResult* out, int32_t* hit) {
+    store_prim(out, 1.0 / 0.0, mk(0, 0, 0), mk(0, 0, 0), 1.0);
+    if (hit) *hit = 0;
+}
+
+__device__ __forceinline__ void warp_survivors(int j, bool keep, uint32_t* mask, int32_t* cnt, int n_total) {
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if ((threadIdx.x & 31) == 0 && j < n_total) {
+        mask[j >> 5] = m;
+        cnt[j >> 5] = __popc(m);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, const int32_t* __restrict__ items,
+                                                        const Entry* __restrict__ soup, const Entry* __restrict__ conn,
+                                                        const int32_t* __restrict__ nn_off, int n_conn,
+                                                        const float* __restrict__ pm32,
+                                                        const int32_t* __restrict__ ntris,
+                                                        const float* __restrict__ tri32,
+                                                        const float* __restrict__ search, PrimResult* __restrict__ sub,
+                                                        PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
+                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool keep = false;
+    if (j < n_total) {
+        const PtWork w = decode_pt(j, n_tp, items, soup, conn, nn_off, n_conn, ntris, sub, cres, chit);
+        const float* pt = tri32 + ((size_t)w.pt_node * 8 + w.pt_tri) * 9 + 3 * w.pt_vert;
+        const float* tv = tri32 + ((size_t)w.tri_node * 8 + w.tri_idx) * 9;
+        const float *Cs = pm32_of(pm32, w.pair, w.mC), *Ce = pm32_of(pm32, w.pair, w.mC + 1);
+        const float *tS = pm32_of(pm32, w.pair, w.mT), *tE = pm32_of(pm32, w.pair, w.mT + 1);
+        float mag = 0.f, ps[3], pe[3], o[3];
+        Box32 bp, bq, scratch;
+        box_init(bp);
+        box_init(bq);
+        box_init(scratch);
+        box_add(scratch, Cs, pt[0], pt[1], pt[2], ps, mag);
+        box_add(scratch, Ce, pt[0], pt[1], pt[2], pe, mag);
+        box_add(bp, tS, ps[0], ps[1], ps[2], o, mag);
+        box_add(bp, tS, pe[0], pe[1], pe[2], o, mag);
+        box_add(bp, tE, ps[0], ps[1], ps[2], o, mag);
+        box_add(bp, tE, pe[0], pe[1], pe[2], o, mag);
+        for (int v = 0; v < 3; v++) {
+            box_add(bq, tS, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+            box_add(bq, tE, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+        }
+        const float thr = search[w.pair];
+        keep = !(box_gap(bp, bq) > thr + (1e-3f + 4e-6f * (mag + thr)));  // NaN keeps the test
+        if (!keep) record_no_contact(w.out, w.hit);
+    }
+    warp_survivors(j, keep, mask, cnt, n_total);
+}
+
+__global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, const int32_t* __restrict__ items,
+                                                        const Entry* __restrict__ soup, const Entry* __restrict__ conn,
+                                                        const int32_t* __restrict__ nn_off, int n_conn,
+                                                        const float* __restrict__ pm32,
+                                                        const int32_t* __restrict__ ntris,
+                                                        const float* __restrict__ tri32,
+                                                        const float* __restrict__ search, PrimResult* __restrict__ sub,
+                                                        PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
+                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool keep = false;
+    if (j < n_total) {
+        const EeWork w = decode_ee(j, n_tp, items, soup, conn, nn_off, n_conn, ntris, sub, cres, chit);
+        const float* ta = tri32 + ((size_t)w.na * 8 + w.aTri) * 9;
+        const float* tb = tri32 + ((size_t)w.nb * 8 + w.bTri) * 9;
+        const int a0 = w.aEdge, a1 = w.aEdge == 2 ? 0 : w.aEdge + 1;
+        const int b0 = w.bEdge, b1 = w.bEdge == 2 ? 0 : w.bEdge + 1;
+        float mag = 0.f, o[3];
+        Box32 ba, bb;
+        box_init(ba);
+        box_init(bb);
+        for (int m = 0; m < 2; m++) {
+            const float* MA = pm32_of(pm32, w.pair, P32_AS + m);
+            const float* MB = pm32_of(pm32, w.pair, P32_BS + m);
+            box_add(ba, MA, ta[3 * a0], ta[3 * a0 + 1], ta[3 * a0 + 2], o, mag);
+            box_add(ba, MA, ta[3 * a1], ta[3 * a1 + 1], ta[3 * a1 + 2], o, mag);
+            box_add(bb, MB, tb[3 * b0], tb[3 * b0 + 1], tb[3 * b0 + 2], o, mag);
+            box_add(bb, MB, tb[3 * b1], tb[3 * b1 + 1], tb[3 * b1 + 2], o, mag);
+        }
+        const float thr = search[w.pair];
+        keep = !(box_gap(ba, bb) > thr + (1e-3f + 4e-6f * (mag + thr)));
+        if (!keep) record_no_contact(w.out, w.hit);
+    }
+    warp_survivors(j, keep, mask, cnt, n_total);
+}
+
 __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, const int32_t* __restrict__ items,
                                                         const Entry* __restrict__ soup, const Entry* __restrict__ conn,
                                                         const int32_t* __restrict__ nn_off, int n_conn,
@@ -185,9 +422,12 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, c
                                                         const double* __restrict__ tris,
                                                         const float* __restrict__ search,
                                                         PrimResult* __restrict__ sub, PrimResult* __restrict__ cres,
-                                                        int32_t* __restrict__ chit) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_total) return;
+                                                        int32_t* __restrict__ chit, const int32_t* __restrict__ list,
+                                                        const int32_t* __restrict__ n_list) {
+    // work item list[kk] (every item when list is null)
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= n_total || (n_list && kk >= *n_list)) return;
+    const int j = list ? list[kk] : kk;
     if (j < 6 * n_tp) {
         const int k = j / 6, w = j % 6;
         const int slot = items[k];
@@ -239,9 +479,12 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_ee(int n_tp, int n_total, c
                                                         const double* __restrict__ tris,
                                                         const float* __restrict__ search,
                                                         PrimResult* __restrict__ sub, PrimResult* __restrict__ cres,
-                                                        int32_t* __restrict__ chit) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_total) return;
+                                                        int32_t* __restrict__ chit, const int32_t* __restrict__ list,
+                                                        const int32_t* __restrict__ n_list) {
+    // work item list[kk] (every item when list is null)
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= n_total || (n_list && kk >= *n_list)) return;
+    const int j = list ? list[kk] : kk;
     Entry e;
     int aTri, aEdge, bTri, bEdge;
     size_t item = 0;
@@ -352,17 +595,19 @@ __global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entr
 // hit test dist < float(search) + eps_a + eps_b (comparison_dist.h:223-236).
 // Candidate slots of the discrete narrow phase.  A (node pair, ta, tb) slot
 // can only hit (comparison_dist.h:231-233) when the triangles are closer than
-// thr = search + eps_a + eps_b; their bounding spheres (centroid, radius
-// rounded up) give the lower bound |c_a - c_b| - r_a - r_b on that distance.
-// It is evaluated in FP32 and a slot is dropped only when the bound exceeds
-// thr by a margin (1 mm plus 4e-6 of the magnitudes involved) far above the
-// FP32 rounding of the bound and the FP64 rounding of the exact test, so every
-// slot that hits survives.  Dropped slots produce nothing in the reference
+// thr = search + eps_a + eps_b.  Two lower bounds on that distance: the
+// bounding spheres' |c_a - c_b| - r_a - r_b (centroid, radius rounded up) and
+// the gap between the boxes of the transformed triangles.  The larger is
+// evaluated in FP32 and a slot is dropped only when it exceeds thr by a margin
+// (1 mm plus 4e-6 of the magnitudes involved) far above the FP32 rounding of
+// the bound and the FP64 rounding of the exact test, so every slot that hits
+// survives.  Dropped slots produce nothing in the reference
 // either.  One thread per slot; per warp a survivor mask and count.  The valid
 // slots (ta < ntris_a, tb < ntris_b) are counted for the statistics.
 __global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __restrict__ front,
                                                     const float* __restrict__ pm32, const int32_t* __restrict__ ntris,
-                                                    const float4* __restrict__ sph, const float* __restrict__ eps_up,
+                                                    const float4* __restrict__ sph, const float* __restrict__ tri32,
+                                                    const float* __restrict__ eps_up,
                                                     const float* __restrict__ search, uint32_t* __restrict__ mask,
                                                     int32_t* __restrict__ cnt, int32_t* __restrict__ tri_pairs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -385,7 +630,29 @@ __global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __
             const float mag = fabsf(A[3]) + fabsf(A[7]) + fabsf(A[11]) + fabsf(B[3]) + fabsf(B[7]) + fabsf(B[11]) +
                               fabsf(sa.x) + fabsf(sa.y) + fabsf(sa.z) + fabsf(sb.x) + fabsf(sb.y) + fabsf(sb.z) +
                               sa.w + sb.w + thr;
-            const float lb = sqrtf(dx * dx + dy * dy + dz * dz) - sa.w - sb.w;
+            float lb = sqrtf(dx * dx + dy * dy + dz * dz) - sa.w - sb.w;
+            // the gap between the transformed triangles' boxes is a second lower bound
+            const float* va = tri32 + ((size_t)e.na * 8 + ta) * 9;
+            const float* vb = tri32 + ((size_t)e.nb * 8 + tb) * 9;
+            float gap2 = 0.f;
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                float alo = 3.4e38f, ahi = -3.4e38f, blo = 3.4e38f, bhi = -3.4e38f;
+#pragma unroll
+                for (int v = 0; v < 3; v++) {
+                    const float wa = A[4 * r] * va[3 * v] + A[4 * r + 1] * va[3 * v + 1] + A[4 * r + 2] * va[3 * v + 2] +
+                                     A[4 * r + 3];
+                    const float wb = B[4 * r] * vb[3 * v] + B[4 * r + 1] * vb[3 * v + 1] + B[4 * r + 2] * vb[3 * v + 2] +
+                                     B[4 * r + 3];
+                    alo = fminf(alo, wa);
+                    ahi = fmaxf(ahi, wa);
+                    blo = fminf(blo, wb);
+                    bhi = fmaxf(bhi, wb);
+                }
+                const float g = fmaxf(blo - ahi, alo - bhi);
+                if (g > 0.f) gap2 += g * g;
+            }
+            lb = fmaxf(lb, sqrtf(gap2));
             keep = !(lb > thr + (1e-3f + 4e-6f * mag));  // NaN keeps the slot
         }
     }
@@ -794,6 +1061,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
     int n_soup = n_pairs, n_conn = 0;
+    int level_pm32 = 0;  // FP32 poses made once per call
     while (n_soup > 0 || n_conn > 0) {
         c_levels++;
         c_node += n_soup + n_conn;
@@ -831,16 +1099,44 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         RC(E.cflag_off.ensure(15 * (size_t)P + 1));
         if (n_soup > 0) LAUNCH(k_compact, n_slots, n_slots, E.flags.p, E.flag_off.p, E.items.p);
         const int n_pt = 6 * K + 6 * P, n_ee = 9 * K + 9 * P;
+        // FP32 bounds drop the tests that cannot hit; the FP64 kernels run on
+        // the compacted survivors
+        const int w_pt = (n_pt + 31) / 32, w_ee = (n_ee + 31) / 32;
+        RC(E.ccd_mask.ensure((size_t)w_pt + w_ee + 2));
+        RC(E.ccd_cnt.ensure((size_t)w_pt + w_ee + 2));
+        RC(E.ccd_off.ensure((size_t)w_pt + w_ee + 4));
+        RC(E.ccd_list.ensure((size_t)n_pt + n_ee + 2));
+        uint32_t* mask_pt = E.ccd_mask.p;
+        uint32_t* mask_ee = E.ccd_mask.p + w_pt;
+        int32_t* cnt_pt = E.ccd_cnt.p;
+        int32_t* cnt_ee = E.ccd_cnt.p + w_pt;
+        int32_t* off_pt = E.ccd_off.p;
+        int32_t* off_ee = E.ccd_off.p + w_pt + 1;
+        int32_t* list_pt = E.ccd_list.p;
+        int32_t* list_ee = E.ccd_list.p + n_pt;
+        if (n_pt > 0 || n_ee > 0) {
+            RC(E.pm32c.ensure((size_t)96 * n_pairs + 1));
+            if (level_pm32 == 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);
+            level_pm32 = 1;
+        }
         if (n_pt > 0) {
+            LAUNCH(k_ccd_mask_pt, n_pt, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
+                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_pt, cnt_pt);
+            RC(scan(ctx, cnt_pt, off_pt, w_pt));
+            LAUNCH(k_np_items, n_pt, n_pt, mask_pt, off_pt, list_pt);
             const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_pt);
             LAUNCHB(k_prim_pt, n_pt, kPrimBlock, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
-                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p);
+                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_pt, off_pt + w_pt);
             prof_end(ctx, pf);
         }
         if (n_ee > 0) {
+            LAUNCH(k_ccd_mask_ee, n_ee, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
+                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee, cnt_ee);
+            RC(scan(ctx, cnt_ee, off_ee, w_ee));
+            LAUNCH(k_np_items, n_ee, n_ee, mask_ee, off_ee, list_ee);
             const int pf = prof_begin(ctx, PROF_CONN, n_ee);
             LAUNCHB(k_prim_ee, n_ee, kPrimBlock, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
-                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p);
+                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_ee, off_ee + w_ee);
             prof_end(ctx, pf);
         }
         // (3) soup fold and finals, leaf-pair finals, expansion; one synchronisation
@@ -931,7 +1227,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
         RC(E.np_cnt.ensure(n_words + 1));
         RC(E.np_off.ensure(n_words + 1));
         RC(E.items.ensure(n_slots + 1));
-        LAUNCH(k_np_mask, n_slots, n_slots, E.soup.p, E.pm32.p, ctx->ntris.p, ctx->tri_sph.p, ctx->eps_up.p,
+        LAUNCH(k_np_mask, n_slots, n_slots, E.soup.p, E.pm32.p, ctx->ntris.p, ctx->tri_sph.p, ctx->tri32.p, ctx->eps_up.p,
                E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p);
         RC(scan(ctx, E.np_cnt.p, E.np_off.p, n_words));
         LAUNCH(k_np_items, n_slots, n_slots, E.np_mask.p, E.np_off.p, E.items.p);

@@ -134,6 +134,10 @@ struct Engine {
     DBuf<int32_t> flt_idx, flt_order, flt_keep, flt_pos, flt_cnt, flt_off, np_tri;
     DBuf<unsigned long long> flt_keys, flt_keys_s;
     DBuf<double> flt_mid;
+    // CCD candidates: FP32 poses (8 per pair), survivor masks, counts, lists
+    DBuf<float> pm32c;
+    DBuf<uint32_t> ccd_mask;
+    DBuf<int32_t> ccd_cnt, ccd_off, ccd_list;
     // discrete narrow-phase candidates: FP32 poses, survivor masks and offsets
     DBuf<float> pm32;
     DBuf<uint32_t> np_mask;
@@ -200,6 +204,7 @@ struct d2g_ctx {
     d2g::DBuf<double> tris, eps, inner_eps;
     d2g::DBuf<float4> tri_sph;  // per tree triangle: centroid, bounding radius (rounded up), FP32
     d2g::DBuf<float> eps_up;    // eps rounded up to FP32
+    d2g::DBuf<float> tri32;     // bucket triangles in FP32 ([N][8][9])
     // bodies
     int n_bodies = 0;
     d2g::DBuf<int32_t> mesh, sleep_steps;
