@@ -236,6 +236,25 @@ def run_ours(args):
     launches = ctx.launches() - launches0
     prof = {k: ctx.profile(k) for k in (D.PROF_SOUP_FILTER, D.PROF_SOUP_CCD, D.PROF_CONN)}
     ctx.set_profiling(False)
+    # the FP64-exact mode: every primitive test in FP64 (identical contacts)
+    ctx.set_fp32_bounds(False)
+    step()
+    exact_ms = 0.0
+    n_exact = max(2, args.steps // 4)
+    for _ in range(n_exact):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n_exact_contacts = step()[0]
+        e1.record(stream)
+        e1.synchronize()
+        exact_ms += e0.elapsed_time(e1)
+    ctx.set_fp32_bounds(True)
+    modes = {"fp32_bounds": {"value": n_pairs * args.steps / (total_ms / 1e3), "contacts": int(n_contacts)},
+             "fp64_exact": {"value": n_pairs * n_exact / (exact_ms / 1e3), "contacts": int(n_exact_contacts),
+                            "steps": n_exact}}
 
     t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -294,7 +313,8 @@ def run_ours(args):
                    "dt": scene.opt_dt, "l2": "flushed before every timed step (512 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
-        "kernel_time_share": kernel_share, "world_steps": steps_line, "batched_steps": batch_line,
+        "kernel_time_share": kernel_share, "precision_modes": modes, "world_steps": steps_line,
+        "batched_steps": batch_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
     }

@@ -354,6 +354,11 @@ class Context:
         self._b = scene.bodies_struct()
         _check(lib().d2g_ctx_set_bodies(self.h, C.byref(self._b)))
 
+    def set_fp32_bounds(self, enable):
+        """FP32 candidate bounds before the FP64 primitive tests (default on;
+        results are identical either way)."""
+        _check(lib().d2g_ctx_set_fp32_bounds(self.h, int(bool(enable))))
+
     def set_scenes(self, scene_of_body):
         """Batch independent scenes: scene index of every body (after set_bodies)."""
         self._scene_of = np.ascontiguousarray(scene_of_body, dtype=np.int32)

@@ -481,6 +481,15 @@ int d2g_ctx_get_bodies(d2g_ctx* c, d2g_bodies* b) {
     return D2G_OK;
 }
 
+int d2g_ctx_set_fp32_bounds(d2g_ctx* c, int32_t enable) {
+    if (!c) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.fp32_bounds = enable != 0;
+    return D2G_OK;
+}
+
 int d2g_ctx_launches(d2g_ctx* c, int64_t* launches) {
     if (!c || !launches) {
         set_error("null argument");

@@ -347,7 +347,8 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, c
                                                         const float* __restrict__ tri32,
                                                         const float* __restrict__ search, PrimResult* __restrict__ sub,
                                                         PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
-                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt) {
+                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt,
+                                                        int use_bounds) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
     if (j < n_total) {
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, c
             box_add(bq, tE, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
         }
         const float thr = search[w.pair];
-        keep = !(box_gap(bp, bq) > thr + (1e-3f + 4e-6f * (mag + thr)));  // NaN keeps the test
+        keep = !use_bounds || !(box_gap(bp, bq) > thr + (1e-3f + 4e-6f * (mag + thr)));  // NaN keeps the test
         if (!keep) record_no_contact(w.out, w.hit);
     }
     warp_survivors(j, keep, mask, cnt, n_total);
@@ -386,7 +387,8 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, c
                                                         const float* __restrict__ tri32,
                                                         const float* __restrict__ search, PrimResult* __restrict__ sub,
                                                         PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
-                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt) {
+                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt,
+                                                        int use_bounds) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
     if (j < n_total) {
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, c
             box_add(bb, MB, tb[3 * b1], tb[3 * b1 + 1], tb[3 * b1 + 2], o, mag);
         }
         const float thr = search[w.pair];
-        keep = !(box_gap(ba, bb) > thr + (1e-3f + 4e-6f * (mag + thr)));
+        keep = !use_bounds || !(box_gap(ba, bb) > thr + (1e-3f + 4e-6f * (mag + thr)));
         if (!keep) record_no_contact(w.out, w.hit);
     }
     warp_survivors(j, keep, mask, cnt, n_total);
@@ -609,7 +611,8 @@ __global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __
                                                     const float4* __restrict__ sph, const float* __restrict__ tri32,
                                                     const float* __restrict__ eps_up,
                                                     const float* __restrict__ search, uint32_t* __restrict__ mask,
-                                                    int32_t* __restrict__ cnt, int32_t* __restrict__ tri_pairs) {
+                                                    int32_t* __restrict__ cnt, int32_t* __restrict__ tri_pairs,
+                                                    int use_bounds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false, keep = false;
     if (i < n_slots) {
@@ -653,7 +656,7 @@ __global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __
                 if (g > 0.f) gap2 += g * g;
             }
             lb = fmaxf(lb, sqrtf(gap2));
-            keep = !(lb > thr + (1e-3f + 4e-6f * mag));  // NaN keeps the slot
+            keep = !use_bounds || !(lb > thr + (1e-3f + 4e-6f * mag));  // NaN keeps the slot
         }
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -1121,7 +1124,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         }
         if (n_pt > 0) {
             LAUNCH(k_ccd_mask_pt, n_pt, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
-                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_pt, cnt_pt);
+                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_pt, cnt_pt,
+                   E.fp32_bounds ? 1 : 0);
             RC(scan(ctx, cnt_pt, off_pt, w_pt));
             LAUNCH(k_np_items, n_pt, n_pt, mask_pt, off_pt, list_pt);
             const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_pt);
@@ -1131,7 +1135,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         }
         if (n_ee > 0) {
             LAUNCH(k_ccd_mask_ee, n_ee, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
-                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee, cnt_ee);
+                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee, cnt_ee,
+                   E.fp32_bounds ? 1 : 0);
             RC(scan(ctx, cnt_ee, off_ee, w_ee));
             LAUNCH(k_np_items, n_ee, n_ee, mask_ee, off_ee, list_ee);
             const int pf = prof_begin(ctx, PROF_CONN, n_ee);
@@ -1228,7 +1233,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
         RC(E.np_off.ensure(n_words + 1));
         RC(E.items.ensure(n_slots + 1));
         LAUNCH(k_np_mask, n_slots, n_slots, E.soup.p, E.pm32.p, ctx->ntris.p, ctx->tri_sph.p, ctx->tri32.p, ctx->eps_up.p,
-               E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p);
+               E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p, E.fp32_bounds ? 1 : 0);
         RC(scan(ctx, E.np_cnt.p, E.np_off.p, n_words));
         LAUNCH(k_np_items, n_slots, n_slots, E.np_mask.p, E.np_off.p, E.items.p);
         const int pf = prof_begin(ctx, PROF_NP, n_slots);

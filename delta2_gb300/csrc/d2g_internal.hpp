@@ -180,6 +180,7 @@ struct Engine {
     // instrumentation: kernel launches issued, and optional per-kernel event timing
     long long launches = 0;
     bool profiling = false;
+    bool fp32_bounds = true;  // FP32 candidate bounds before the FP64 tests (results identical either way)
     struct Pending {
         int kind;
         cudaEvent_t e0, e1;

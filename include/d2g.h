@@ -138,6 +138,12 @@ int d2g_ctx_set_scenes(d2g_ctx* ctx, const int32_t* scene_of_body);
 /* Copy the device body states (last/cur/fut, last_dt, sleep_steps, sleeping) back. */
 int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
 
+/* Mixed precision (no reference counterpart): with enable != 0 (the
+ * default) the discrete narrow phase and the CCD first bound every
+ * primitive test in FP32 (bounding spheres and box gaps, with a margin far
+ * above FP32 and FP64 rounding) and run the FP64 test only where a hit is
+ * possible; with 0 every test runs in FP64.  Results are identical. */
+int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library launched on the context, and, with profiling on, CUDA-event times
  * of the dominant kernels: kind 0 swept-box filter, 1 point-triangle CCD

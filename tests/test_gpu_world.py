@@ -149,3 +149,22 @@ def test_solve_matches_oracle(ctx):
     ref_warm = ref_world.warm()
     assert {k: np.float64(v).view(np.uint64) for k, v in warm.items()} == \
         {k: np.float64(v).view(np.uint64) for k, v in ref_warm.items()}
+
+
+def test_fp32_bounds_do_not_change_results(ctx):
+    # the FP64-exact mode (every primitive test in FP64) and the default FP32
+    # candidate bounds give the same contacts, bit for bit
+    s = D.make_scene(2, nx=4, ny=4, nz=4, speed_sigma=2.0, seed=9)
+    pairs = D.broad_phase(s)
+    mt = np.full(len(pairs), np.float64(np.float32(s.opt_dt)) * 4)
+    out = {}
+    for mode in (True, False):
+        ctx.set_scene(s.copy())
+        ctx.set_fp32_bounds(mode)
+        c1, o1, k1 = ctx.compare_trees_full_continuous(pairs, mt)
+        c2, o2, k2 = ctx.compare_trees_full(pairs)
+        out[mode] = (c1, o1, k1, c2, o2, k2)
+    ctx.set_fp32_bounds(True)
+    for a, b in zip(out[True], out[False]):
+        assert np.array_equal(bits(np.asarray(a)), bits(np.asarray(b)))
+    assert len(out[True][0]) > 0 and len(out[True][3]) > 0
