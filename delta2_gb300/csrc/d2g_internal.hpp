@@ -146,7 +146,8 @@ struct Engine {
     // sequential-impulse solve
     DBuf<unsigned long long> sv_keys, sv_keys_out;
     DBuf<int32_t> sv_vals, sv_order, sv_wave_idx, sv_wave_off, sv_wave_cursor;
-    DBuf<double> sv_static_imp;
+    DBuf<double> sv_static_imp, sv_sdelta;
+    DBuf<int32_t> sv_scon, sv_list, sv_grid;
     DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
     // GPU broad phase (d2g_broadphase.cu)
     DBuf<float> bp_box;
@@ -265,5 +266,6 @@ int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pa
 int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts, int n_parts,
               const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
               const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
-              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm);
+              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm,
+              const int32_t* h_con_off = nullptr);
 }  // namespace d2g

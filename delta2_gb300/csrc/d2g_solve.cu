@@ -16,6 +16,9 @@
 // reads for them is accumulated from per-contact deltas in sorted order).
 #include <cub/cub.cuh>
 
+#include <algorithm>
+#include <vector>
+
 #include "d2g_geom.cuh"
 #include "d2g_internal.hpp"
 
@@ -25,6 +28,8 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr int kSolveBlock = 256;
+constexpr int kGridMinContacts = 128;  // a cluster this large may take a cooperative grid
+constexpr int kGridMaxClusters = 8;    // ... when the call has at most this many clusters
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -135,8 +140,8 @@ struct ConWork {
     double local_A[3], local_B[3], n[3];
     double start_dist, mass_eff, outer, impulse, impulse_offset;
     double last_fi[3], last_rot_A[3], last_rot_B[3], upd_total[3];
-    double static_delta[3];
     int a, b, level, pair_cnt;
+    int spos;  // position among the contacts touching a static body, -1 if none
 };
 
 __device__ __forceinline__ V3 ld3(const double* p) { return mk(p[0], p[1], p[2]); }
@@ -185,29 +190,123 @@ __device__ __forceinline__ V3 xf12(V3 p, const double* T) {
 
 __device__ __forceinline__ bool block_any(bool v) { return __syncthreads_or(v ? 1 : 0) != 0; }
 
-// One block per cluster.
-__global__ void __launch_bounds__(kSolveBlock)
-    k_solve(int n_clusters, const int32_t* __restrict__ cl_part_off, const int32_t* __restrict__ cl_parts,
-            const int32_t* __restrict__ cl_con_off, const int32_t* __restrict__ order, const double* __restrict__ rec,
-            const int32_t* __restrict__ pair_cnt, const double* __restrict__ warm, const double* __restrict__ cl_step,
-            const uint8_t* __restrict__ is_static, const double* __restrict__ mass, const double* __restrict__ ii,
-            const double* __restrict__ mu, const double* __restrict__ cur, double* __restrict__ fut, double gravity_z,
-            BodyWork* __restrict__ bw, ConWork* __restrict__ cw, int32_t* __restrict__ wave_idx,
-            int32_t* __restrict__ wave_off, int32_t* __restrict__ wave_cursor, double* __restrict__ static_imp, int32_t* __restrict__ status,
-            int32_t* __restrict__ iters, double* __restrict__ out_impulse, int32_t* __restrict__ out_ab,
-            const int32_t* __restrict__ con_pair, double* __restrict__ pair_warm) {
-    const int k = blockIdx.x;
-    if (k >= n_clusters) return;
-    const int tid = threadIdx.x, nt = blockDim.x;
+// Synchronisation of one cluster's solve: the threads of one block, or every
+// thread of a cooperative grid (all blocks resident) for a large cluster.
+// The grid barrier is a generation counter in global memory with the fences
+// of a grid-wide barrier; its wait is bounded, and a barrier that gives up
+// records the fact so the kernel can stop and report it.
+struct SolveSync {
+    bool grid;
+    unsigned int* count;  // grid barrier arrivals
+    unsigned int* gen;    // grid barrier generation
+    int32_t* flags;       // grid: [0] fail, [1] levels, [2] static contacts, [3], [4] "moved" by parity, [5] spin error
+};
+
+__device__ bool solve_sync(const SolveSync& S) {
+    if (!S.grid) {
+        __syncthreads();
+        return true;
+    }
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int my = atomicAdd(S.gen, 0u);
+        __threadfence();
+        if (atomicAdd(S.count, 1u) == gridDim.x - 1) {
+            atomicExch(S.count, 0u);
+            __threadfence();
+            atomicAdd(S.gen, 1u);
+        } else {
+            unsigned long long spins = 0;
+            while (((volatile unsigned int*)S.gen)[0] == my) {
+                if (++spins > (1ull << 25)) {  // several seconds: the other blocks are gone
+                    atomicExch(S.flags + 5, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// true when any thread of the cluster's solve passes v; slot 3 or 4 by the
+// iteration's parity (the other slot is cleared for the next iteration).
+__device__ bool solve_any(const SolveSync& S, bool v, int parity, bool* ok) {
+    if (!S.grid) return block_any(v);
+    const bool blk = __syncthreads_or(v ? 1 : 0) != 0;
+    if (threadIdx.x == 0 && blk) atomicOr(S.flags + 3 + parity, 1);
+    *ok = solve_sync(S) && *ok;
+    const bool r = ((volatile int32_t*)S.flags)[3 + parity] != 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) S.flags[3 + (parity ^ 1)] = 0;
+    return r;
+}
+
+// Arguments of a cluster solve.
+struct SolveArgs {
+    const int32_t *cl_part_off, *cl_parts, *cl_con_off, *order;
+    const double* rec;
+    const int32_t* pair_cnt;
+    const double *warm, *cl_step;
+    const uint8_t* is_static;
+    const double *mass, *ii, *mu, *cur;
+    double* fut;
+    double gravity_z;
+    BodyWork* bw;
+    ConWork* cw;
+    int32_t *wave_idx, *wave_off, *wave_cursor, *scon;
+    double* sdelta;  // per contact touching a static body: its impulse delta on that body
+    double* static_imp;
+    int32_t *status, *iters;
+    double* out_impulse;
+    int32_t* out_ab;
+    const int32_t* con_pair;
+    double* pair_warm;
+};
+
+#define SYNC()                           \
+    do {                                 \
+        if (!solve_sync(S)) {            \
+            if (tid == 0) status[k] = 3; \
+            return;                      \
+        }                                \
+    } while (0)
+
+// SequentialImpulses::solve of cluster k.  tid / nt: this thread's index
+// among the cluster's threads and their count; G blocks cooperate (G = 1 for
+// one block), gb is this block's index among them.  In a grid the indices
+// interleave the blocks, so consecutive bodies, contacts and warps of a wave
+// land on different SMs.  shv: three ints shared by those threads.
+__device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, const SolveSync& S,
+                           const SolveArgs& a) {
+    const int32_t *cl_part_off = a.cl_part_off, *cl_parts = a.cl_parts, *cl_con_off = a.cl_con_off,
+                  *order = a.order, *pair_cnt = a.pair_cnt, *con_pair = a.con_pair;
+    const double *rec = a.rec, *warm = a.warm, *cl_step = a.cl_step, *mass = a.mass, *ii = a.ii, *mu = a.mu,
+                 *cur = a.cur;
+    const uint8_t* is_static = a.is_static;
+    double* fut = a.fut;
+    const double gravity_z = a.gravity_z;
+    BodyWork* bw = a.bw;
+    ConWork* cw = a.cw;
+    int32_t *wave_idx = a.wave_idx, *wave_off = a.wave_off, *wave_cursor = a.wave_cursor, *scon = a.scon;
+    double* sdelta = a.sdelta;
+    double* static_imp = a.static_imp;
+    int32_t *status = a.status, *iters = a.iters, *out_ab = a.out_ab;
+    double *out_impulse = a.out_impulse, *pair_warm = a.pair_warm;
     const int p0 = cl_part_off[k], p1 = cl_part_off[k + 1];
     const int c0 = cl_con_off[k], c1 = cl_con_off[k + 1];
     const int nc = c1 - c0;
     const double t = cl_step[k];
-    __shared__ int s_fail, s_levels;
+    bool ok = true;
 
     // ---- contacts in sorted order: local frames, normal mass, failure test (:109-168)
-    if (tid == 0) s_fail = 0;
-    __syncthreads();
+    if (tid == 0) shv[0] = 0;
+    SYNC();
     for (int i = tid; i < nc; i += nt) {
         ConWork& C = cw[c0 + i];
         const double* h = rec + 14 * (size_t)order[c0 + i];
@@ -216,7 +315,7 @@ __global__ void __launch_bounds__(kSolveBlock)
         C.b = (int)h[12];
         C.pair_cnt = pair_cnt[order[c0 + i]];
         C.start_dist = norm(A - B);
-        if (C.start_dist < 1e-6 && t > 1e-4) atomicExch(&s_fail, 1);
+        if (C.start_dist < 1e-6 && t > 1e-4) atomicExch(&shv[0], 1);
         double T[16], Ti[16];
         const State fa = load_state(fut + 14 * (size_t)C.a), fb = load_state(fut + 14 * (size_t)C.b);
         transformation(fa.q, fa.x, T);
@@ -237,8 +336,8 @@ __global__ void __launch_bounds__(kSolveBlock)
         C.impulse_offset = 0.0;
         for (int q = 0; q < 3; q++) C.last_fi[q] = C.last_rot_A[q] = C.last_rot_B[q] = 0.0;
     }
-    __syncthreads();
-    if (s_fail) {
+    SYNC();
+    if (((volatile int*)shv)[0]) {
         if (tid == 0) status[k] = 1;
         return;
     }
@@ -259,7 +358,7 @@ __global__ void __launch_bounds__(kSolveBlock)
         W.last_level = -1;
         if (is_static[g]) st3(static_imp + 3 * (size_t)i, f * t);
     }
-    __syncthreads();
+    SYNC();
     // ---- wave schedule (sequential, integer work only)
     if (tid == 0) {
         int levels = 0;
@@ -280,10 +379,21 @@ __global__ void __launch_bounds__(kSolveBlock)
         int32_t* cursor = wave_cursor + c0 + k;
         for (int l = 0; l < levels; l++) cursor[l] = wave_off[c0 + k + l];
         for (int i = 0; i < nc; i++) wave_idx[c0 + cursor[cw[c0 + i].level]++] = i;
-        s_levels = levels;
+        // the contacts touching a static body, in sorted order, for its impulse
+        // sums: each writes its delta at its position, scon holds the body
+        int ns = 0;
+        for (int i = 0; i < nc; i++) {
+            ConWork& C = cw[c0 + i];
+            const bool sa = is_static[C.a], sb = is_static[C.b];
+            C.spos = (sa || sb) ? ns : -1;
+            if (sa || sb) scon[c0 + ns++] = sa ? C.a : C.b;
+        }
+        shv[1] = levels;
+        shv[2] = ns;
     }
-    __syncthreads();
-    const int levels = s_levels;
+    SYNC();
+    const int levels = ((volatile int*)shv)[1];
+    const int n_scon = ((volatile int*)shv)[2];
     const int* woff = wave_off + c0 + k;
     const int* widx = wave_idx + c0;
 
@@ -293,10 +403,8 @@ __global__ void __launch_bounds__(kSolveBlock)
             const int g = cl_parts[i];
             if (!is_static[g]) continue;
             V3 s = ld3(static_imp + 3 * (size_t)i);
-            for (int j = 0; j < nc; j++) {
-                const ConWork& C = cw[c0 + j];
-                if (C.a == g || C.b == g) s = s + ld3(C.static_delta);
-            }
+            for (int q = 0; q < n_scon; q++)
+                if (scon[c0 + q] == g) s = s + ld3(sdelta + 3 * (size_t)(c0 + q));
             st3(static_imp + 3 * (size_t)i, s);
         }
     };
@@ -322,39 +430,41 @@ __global__ void __launch_bounds__(kSolveBlock)
             } else {
                 sd = -u;
             }
-            st3(C.static_delta, sd);
+            if (C.spos >= 0) st3(sdelta + 3 * (size_t)(c0 + C.spos), sd);
         }
-        __syncthreads();
+        SYNC();
     }
     static_sum();
-    __syncthreads();
+    SYNC();
     for (int k2 = tid; k2 < 2 * (p1 - p0); k2 += nt) {  // two lanes per body: FS, FSf
         const int g = cl_parts[p0 + (k2 >> 1)];
         if (!is_static[g]) integrate_one(bw[g], fut + 14 * (size_t)g, mass[g], t, k2 & 1);
     }
-    __syncthreads();
+    SYNC();
 
     int it_n = 0, it_f = 0;
     if (nc > 0) {
         // ---- normal loop (:230-395)
         bool converged = false;
+        // every iteration compares the moving bodies' impulses with their values
+        // at its start (kept in last_imp, refreshed by the convergence test);
+        // static bodies keep their running sums in static_imp
+        for (int i = p0 + tid; i < p1; i += nt) {
+            const int g = cl_parts[i];
+            if (!is_static[g])
+                for (int q = 0; q < 3; q++) bw[g].last_imp[q] = bw[g].imp[q];
+        }
+        SYNC();
         while (!converged && it_n < 1000) {
-            for (int i = p0 + tid; i < p1; i += nt) {
-                const int g = cl_parts[i];
-                double* li = is_static[g] ? nullptr : bw[g].last_imp;
-                if (li)
-                    for (int q = 0; q < 3; q++) li[q] = bw[g].imp[q];
-            }
-            // static bodies keep their running sums in static_imp; remember them
-            __syncthreads();
             for (int l = 0; l < levels; l++) {
                 // Four lanes per contact, one warp instruction stream: lane bit 0
                 // picks the body side (A, B), bit 1 the integrated state (FS,
                 // FSf).  FP64 latency, not lane count, bounds a wave, so the
                 // sides and the four integrations run side by side.
                 const int end4 = 4 * woff[l + 1];
-                for (int base = 4 * woff[l] + (tid & ~31); base < end4; base += nt) {
-                    const int lane = tid & 31, quad = lane & ~3, side = lane & 1, variant = (lane >> 1) & 1;
+                const int wslot = (int)(threadIdx.x >> 5) * G + gb, nwarps = (int)(blockDim.x >> 5) * G;
+                for (int base = 4 * woff[l] + 32 * wslot; base < end4; base += 32 * nwarps) {
+                    const int lane = threadIdx.x & 31, quad = lane & ~3, side = lane & 1, variant = (lane >> 1) & 1;
                     const int qq = base + lane;
                     const bool act = qq < end4;
                     ConWork& C = cw[c0 + widx[act ? (qq >> 2) : woff[l]]];
@@ -395,13 +505,13 @@ __global__ void __launch_bounds__(kSolveBlock)
                         if (side == 0) {
                             C.impulse = imp1;
                             C.impulse_offset = off1;
-                            st3(C.static_delta, sa ? u : (sb ? -u : mk(0, 0, 0)));
+                            if (C.spos >= 0) st3(sdelta + 3 * (size_t)(c0 + C.spos), sa ? u : -u);
                         }
                     }
                     __syncwarp();
                     if (act && !st) integrate_one(W, fut + 14 * (size_t)g, mass[g], t, variant);
                 }
-                __syncthreads();
+                SYNC();
             }
             // convergence over every particle of the cluster (:380-387)
             bool moved = false;
@@ -410,17 +520,21 @@ __global__ void __launch_bounds__(kSolveBlock)
                 if (is_static[g]) {
                     const V3 before = ld3(static_imp + 3 * (size_t)i);
                     V3 s = before;
-                    for (int j = 0; j < nc; j++) {
-                        const ConWork& C = cw[c0 + j];
-                        if (C.a == g || C.b == g) s = s + ld3(C.static_delta);
-                    }
+                    for (int q = 0; q < n_scon; q++)
+                        if (scon[c0 + q] == g) s = s + ld3(sdelta + 3 * (size_t)(c0 + q));
                     st3(static_imp + 3 * (size_t)i, s);
                     if (norm(s - before) > 1e-6) moved = true;
                 } else {
-                    if (norm(ld3(bw[g].imp) - ld3(bw[g].last_imp)) > 1e-6) moved = true;
+                    const V3 now = ld3(bw[g].imp);
+                    if (norm(now - ld3(bw[g].last_imp)) > 1e-6) moved = true;
+                    st3(bw[g].last_imp, now);
                 }
             }
-            converged = !block_any(moved);
+            converged = !solve_any(S, moved, it_n & 1, &ok);
+            if (!ok) {
+                if (tid == 0) status[k] = 3;
+                return;
+            }
             it_n++;
         }
         // ---- friction loop (:397-607)
@@ -459,7 +573,7 @@ __global__ void __launch_bounds__(kSolveBlock)
                 total = normalized(total) * dclamp(norm(total), 0.0, max_force);
                 st3(C.upd_total, total);
             }
-            __syncthreads();
+            SYNC();
             bool big = false;
             for (int l = 0; l < levels; l++) {  // pass 2: ordered accumulation
                 for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
@@ -479,7 +593,7 @@ __global__ void __launch_bounds__(kSolveBlock)
                         st3(B.imp, ld3(B.imp) - u);
                     else
                         sd = -u;
-                    st3(C.static_delta, sd);
+                    if (C.spos >= 0) st3(sdelta + 3 * (size_t)(c0 + C.spos), sd);
                     if (norm(u) > 1e-4) big = true;
                     const V3 rfA = calc_torque(ld3(C.last_fi), p1A, ld3(A.FS + 8));
                     const V3 rfB = calc_torque(-ld3(C.last_fi), p1B, ld3(B.FS + 8));
@@ -496,18 +610,22 @@ __global__ void __launch_bounds__(kSolveBlock)
                     if (!sa) st3(A.roff, ld3(A.roff) + calc_torque(uo, p1A, ld3(A.FS + 8)));
                     if (!sb) st3(B.roff, ld3(B.roff) + calc_torque(-uo, p1B, ld3(B.FS + 8)));
                 }
-                __syncthreads();
+                SYNC();
             }
             // (the static bodies' impulse sums are read only by the normal loop's test)
             for (int k2 = tid; k2 < 2 * (p1 - p0); k2 += nt) {  // two lanes per body: FS, FSf
                 const int g = cl_parts[p0 + (k2 >> 1)];
                 if (!is_static[g]) integrate_one(bw[g], fut + 14 * (size_t)g, mass[g], t, k2 & 1);
             }
-            converged = !block_any(big);
+            converged = !solve_any(S, big, (it_n + it_f) & 1, &ok);
+            if (!ok) {
+                if (tid == 0) status[k] = 3;
+                return;
+            }
             it_f++;
         }
     }
-    __syncthreads();
+    SYNC();
     // ---- write back (:622-624) and the contacts' impulses for the warm start
     for (int i = p0 + tid; i < p1; i += nt) {
         const int g = cl_parts[i];
@@ -532,6 +650,22 @@ __global__ void __launch_bounds__(kSolveBlock)
                 pair_warm[con_pair[oi]] = pair_cnt[oi] == 1 ? 0.0 + cw[c0 + i].impulse : cw[c0 + i].impulse;
             }
     }
+}
+
+#undef SYNC
+
+// One block per cluster (clusters cl_list[b], or b when cl_list is null).
+__global__ void __launch_bounds__(kSolveBlock) k_solve(int n_list, const int32_t* __restrict__ cl_list, SolveArgs a) {
+    if ((int)blockIdx.x >= n_list) return;
+    __shared__ int s_local[3];
+    const SolveSync S{false, nullptr, nullptr, nullptr};
+    solve_body(cl_list ? cl_list[blockIdx.x] : (int)blockIdx.x, threadIdx.x, blockDim.x, 0, 1, s_local, S, a);
+}
+
+// Every block of a cooperative grid on cluster k (all blocks resident).
+__global__ void __launch_bounds__(kSolveBlock) k_solve_grid(int k, SolveSync S, SolveArgs a) {
+    solve_body(k, threadIdx.x * gridDim.x + blockIdx.x, gridDim.x * blockDim.x, blockIdx.x, gridDim.x, S.flags, S,
+               a);
 }
 
 // Sort key of Contact::operator< (contact.h:17-21) as orderable bits
@@ -629,9 +763,12 @@ int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pa
 int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int32_t* d_parts, int n_parts,
               const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
               const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
-              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm) {
+              double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm,
+              const int32_t* h_con_off) {
     Engine& E = ctx->eng;
     cudaStream_t s = ctx->stream;
+    RC(E.sv_scon.ensure(n_con + 1));
+    RC(E.sv_sdelta.ensure(3 * (size_t)n_con + 3));
     RC(E.sv_keys.ensure(n_con + 1));
     RC(E.sv_keys_out.ensure(n_con + 1));
     RC(E.sv_vals.ensure(n_con + 1));
@@ -656,14 +793,83 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
                                                           d_con_off + 1, 0, 64, s));
     }
     if (n_clusters > 0) {
+        SolveArgs a;
+        a.cl_part_off = d_part_off;
+        a.cl_parts = d_parts;
+        a.cl_con_off = d_con_off;
+        a.order = E.sv_order.p;
+        a.rec = d_rec;
+        a.pair_cnt = d_pair_cnt;
+        a.warm = d_warm;
+        a.cl_step = d_step;
+        a.is_static = ctx->is_static.p;
+        a.mass = ctx->mass.p;
+        a.ii = ctx->inv_inertia.p;
+        a.mu = ctx->mu.p;
+        a.cur = ctx->cur.p;
+        a.fut = ctx->fut.p;
+        a.gravity_z = gravity_z;
+        a.bw = bw;
+        a.cw = cw;
+        a.wave_idx = E.sv_wave_idx.p;
+        a.wave_off = E.sv_wave_off.p;
+        a.wave_cursor = E.sv_wave_cursor.p;
+        a.scon = E.sv_scon.p;
+        a.sdelta = E.sv_sdelta.p;
+        a.static_imp = E.sv_static_imp.p;
+        a.status = d_status;
+        a.iters = d_iters;
+        a.out_impulse = d_out_impulse;
+        a.out_ab = d_out_ab;
+        a.con_pair = d_con_pair;
+        a.pair_warm = d_pair_warm;
+        // A large cluster among few is solved by a cooperative grid over the
+        // SMs; the others one block each.
+        std::vector<int32_t> small, big;
+        for (int c = 0; c < n_clusters; c++) {
+            const int nck = h_con_off ? h_con_off[c + 1] - h_con_off[c] : 0;
+            if (h_con_off && n_clusters <= kGridMaxClusters && nck >= kGridMinContacts)
+                big.push_back(c);
+            else
+                small.push_back(c);
+        }
         const int pf = prof_mark_begin(ctx, PROF_SOLVE, n_con);
-        k_solve<<<n_clusters, kSolveBlock, 0, s>>>(
-            n_clusters, d_part_off, d_parts, d_con_off, E.sv_order.p, d_rec, d_pair_cnt, d_warm, d_step,
-            ctx->is_static.p, ctx->mass.p, ctx->inv_inertia.p, ctx->mu.p, ctx->cur.p, ctx->fut.p, gravity_z,
-            bw, cw, E.sv_wave_idx.p, E.sv_wave_off.p, E.sv_wave_cursor.p, E.sv_static_imp.p, d_status, d_iters,
-            d_out_impulse, d_out_ab, d_con_pair, d_pair_warm);
+        if (!small.empty()) {
+            const int32_t* d_list = nullptr;
+            if (!big.empty()) {
+                RC(E.sv_list.ensure(small.size() + 1));
+                D2G_CUDA(cudaMemcpyAsync(E.sv_list.p, small.data(), small.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, s));
+                d_list = E.sv_list.p;
+            }
+            k_solve<<<(int)small.size(), kSolveBlock, 0, s>>>((int)small.size(), d_list, a);
+            ctx->eng.launches++;
+        }
+        if (!big.empty()) {
+            int dev_sms = 0, per_sm = 0;
+            D2G_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+            D2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_grid, kSolveBlock, 0));
+            const int G_max = std::max(1, std::min(dev_sms, dev_sms * per_sm));
+            RC(E.sv_grid.ensure(16 * big.size() + 16));
+            D2G_CUDA(cudaMemsetAsync(E.sv_grid.p, 0, (16 * big.size() + 16) * sizeof(int32_t), s));
+            for (size_t b = 0; b < big.size(); b++) {
+                SolveSync S;
+                S.grid = true;
+                S.count = (unsigned int*)(E.sv_grid.p + 16 * b);
+                S.gen = (unsigned int*)(E.sv_grid.p + 16 * b + 1);
+                S.flags = E.sv_grid.p + 16 * b + 4;
+                int k = big[b];
+                // about one warp of contacts per SM and wave: fewer blocks for
+                // smaller clusters keep the grid barriers cheap
+                const int nck = h_con_off[k + 1] - h_con_off[k];
+                const int G = std::max(1, std::min(G_max, std::max(8, nck / 16)));
+                void* args[] = {&k, &S, &a};
+                D2G_CUDA(cudaLaunchCooperativeKernel((const void*)k_solve_grid, dim3(G), dim3(kSolveBlock), args, 0,
+                                                     s));
+                ctx->eng.launches++;
+            }
+        }
         prof_mark_end(ctx, pf);
-        ctx->eng.launches++;
     }
     D2G_CUDA(cudaGetLastError());
     return D2G_OK;

@@ -263,14 +263,19 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
                            W.con_pair.p));
     W.mark(6);
     RC(run_con_off(c, nA, W.pk_batch.ptr(i_pairoff), E.flt_off.p, W.con_off.p));
+    // the contact count of every cluster decides how it is solved (one block, or a grid)
+    const size_t ni = (size_t)nA * 4 + n_pairs + 1;
+    RC(W.h_ri.ensure(ni + nA + 8));
+    int32_t* h_con_off = W.h_ri.p + ni + 4;
+    D2G_CUDA(cudaMemcpyAsync(h_con_off, W.con_off.p, (nA + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    D2G_CUDA(cudaStreamSynchronize(s));
     RC(run_solve(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), (int)parts.size(), W.con_off.p, n_kept,
                  E.flt.p, W.con_cnt.p, W.con_warm.p, W.step_a.p, W.gravity_z, W.status.p, W.iters.p, W.con_imp.p,
-                 W.con_ab.p, W.con_pair.p, W.pair_warm.p));
+                 W.con_ab.p, W.con_pair.p, W.pair_warm.p, h_con_off));
     RC(run_pde_finish(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), W.step_a.p, W.status.p,
                       W.will_sleep.p));
     // results back: status, iterations, will_sleep, kept counts (int); step, pair warm (double)
-    const size_t ni = (size_t)nA * 4 + n_pairs + 1;
-    RC(W.h_ri.ensure(ni + 1));
+
     RC(W.h_rd.ensure((size_t)nA + n_pairs + 1));
     int32_t* hi = W.h_ri.p + 1;
     D2G_CUDA(cudaMemcpyAsync(hi, W.status.p, nA * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -290,6 +295,11 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
     W.stats[11] += cnt[0];
     W.stats[12] += cnt[1];
     ok_out.assign(nA, 0);
+    for (int b = 0; b < nA; b++)
+        if (hi[b] == 3) {
+            set_error("a grid barrier of the sequential-impulse solve gave up waiting");
+            return D2G_SPIN_LIMIT;
+        }
     for (int b = 0; b < nA; b++) {
         Machine& m = M[act[b]];
         m.last_step = W.h_rd.p[b];

@@ -168,3 +168,11 @@ def test_fp32_bounds_do_not_change_results(ctx):
     for a, b in zip(out[True], out[False]):
         assert np.array_equal(bits(np.asarray(a)), bits(np.asarray(b)))
     assert len(out[True][0]) > 0 and len(out[True][3]) > 0
+
+
+def test_world_cube_pile_grid_solve(ctx):
+    # the 64-cube configuration: one cluster whose contacts grow past the
+    # threshold where the solve runs as a cooperative grid over the SMs
+    s = D.make_scene(1)
+    st = run_world(ctx, s, 100)
+    assert st["np_contacts"] > 0
