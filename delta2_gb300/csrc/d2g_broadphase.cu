@@ -122,75 +122,107 @@ __device__ __forceinline__ bool boxes_overlap(const float* a, const float* b) {
     return ov;
 }
 
-// Sweep along x over the sorted boxes: count (pass 0) or write (pass 1) the
-// box-overlapping pairs (min, max) of each sorted position.
-__global__ void k_bp_sweep(int n, const int32_t* __restrict__ order, const float* __restrict__ box,
-                           const uint8_t* __restrict__ is_static, const int32_t* __restrict__ scene,
-                           const int32_t* __restrict__ off, int32_t* __restrict__ cnt, int32_t* __restrict__ out) {
+// Sweep along x over the sorted boxes, as ranges: the boxes that can overlap
+// sorted box u are the positions after u, in its scene, among the finite boxes,
+// up to the first whose lower x exceeds u's upper x (lower x is sorted, so
+// both ends are binary searches).  r[u] = the range's length.
+__global__ void k_bp_range(int n, const int32_t* __restrict__ order, const float* __restrict__ box,
+                           const unsigned long long* __restrict__ key_s, long long* __restrict__ r) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= n) return;
     const int p = order[u];
-    int c = 0;
-    if (p >= 0) {
-        const float* bp = box + 6 * (size_t)p;
-        int w = off ? off[u] : 0;
-        for (int v = u + 1; v < n; v++) {
-            const int q = order[v];
-            if (q < 0) break;  // the NaN boxes come last in a scene
-            if (scene[q] != scene[p]) break;
-            const float* bq = box + 6 * (size_t)q;
-            if (bq[0] > bp[3]) break;
-            if (is_static[p] && is_static[q]) continue;
-            if (!boxes_overlap(bp, bq)) continue;
-            if (out) {
-                out[2 * (size_t)w] = p < q ? p : q;
-                out[2 * (size_t)w + 1] = p < q ? q : p;
-                w++;
-            }
-            c++;
-        }
+    if (p < 0) {  // a NaN box overlaps nothing
+        r[u] = 0;
+        return;
     }
-    if (cnt) cnt[u] = c;
+    const unsigned long long lim = key_s[u] | 0xffffffffULL;  // the NaN-box key of this scene
+    int lo = u + 1, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (key_s[mid] < lim)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    const float hx = box[6 * (size_t)p + 3];
+    hi = lo;
+    lo = u + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (box[6 * (size_t)order[mid]] > hx)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    r[u] = lo - u - 1;
 }
 
 // The reference's swept-sphere filter of one candidate (i < j)
-// (broad_phase_embree.cpp:196-216); err on an invalid interpolation.
-__global__ void k_bp_filter(int n, const int32_t* __restrict__ cand, const uint8_t* __restrict__ is_static,
-                            const double* __restrict__ last, const double* __restrict__ cur,
-                            const double* __restrict__ radius, const double* __restrict__ geo_eps,
-                            const double* __restrict__ last_dt, unsigned long long* __restrict__ key,
-                            int32_t* __restrict__ flag, int32_t* __restrict__ err) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int i = cand[2 * (size_t)k], j = cand[2 * (size_t)k + 1];
+// (broad_phase_embree.cpp:196-216): 1 keep, 0 drop, -1 invalid interpolation.
+__device__ int bp_filter_one(int i, int j, const uint8_t* __restrict__ is_static, const double* __restrict__ last,
+                             const double* __restrict__ cur, const double* __restrict__ radius,
+                             const double* __restrict__ geo_eps, const double* __restrict__ last_dt) {
     State as = load_state(cur + 14 * (size_t)i), bs = load_state(cur + 14 * (size_t)j);
-    int f = 0;
-    bool ok = true;
     if (!is_static[i] && !is_static[j]) {
         State o;
         if (as.time < bs.time) {
-            ok = interpolate(bs, load_state(last + 14 * (size_t)j), as.time, o);
-            if (ok) bs = o;
+            if (!interpolate(bs, load_state(last + 14 * (size_t)j), as.time, o)) return -1;
+            bs = o;
         } else {
-            ok = interpolate(as, load_state(last + 14 * (size_t)i), bs.time, o);
-            if (ok) as = o;
+            if (!interpolate(as, load_state(last + 14 * (size_t)i), bs.time, o)) return -1;
+            as = o;
         }
     }
-    if (!ok) {
-        atomicExch(err, 1);
-    } else {
-        const double t = sphere_sphere_first_intersect(as.x, as.v, radius[i] + geo_eps[i], bs.x, bs.v,
-                                                       radius[j] + geo_eps[j]);
-        f = (t >= 0.0 && t < dmax(last_dt[i], last_dt[j])) ? 1 : 0;
-    }
-    flag[k] = f;
-    key[k] = ((unsigned long long)(uint32_t)i << 32) | (uint32_t)j;
+    const double t =
+        sphere_sphere_first_intersect(as.x, as.v, radius[i] + geo_eps[i], bs.x, bs.v, radius[j] + geo_eps[j]);
+    return (t >= 0.0 && t < dmax(last_dt[i], last_dt[j])) ? 1 : 0;
 }
 
-__global__ void k_bp_compact(int n, const int32_t* __restrict__ flag, const int32_t* __restrict__ off,
-                             const unsigned long long* __restrict__ key, unsigned long long* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n && flag[k]) out[off[k]] = key[k];
+// One thread per range element (grid-stride over the total read from
+// roff[n]): the box test of the two sorted positions, the static-static skip
+// and the swept-sphere filter; kept pairs append their key (i << 32 | j) at a
+// warp-aggregated counter (the keys are sorted afterwards, so the append
+// order does not matter).  Keys beyond cap are counted but not written.
+__global__ void k_bp_pairs(int n, const long long* __restrict__ roff, const int32_t* __restrict__ order,
+                           const float* __restrict__ box, const uint8_t* __restrict__ is_static,
+                           const double* __restrict__ last, const double* __restrict__ cur,
+                           const double* __restrict__ radius, const double* __restrict__ geo_eps,
+                           const double* __restrict__ last_dt, unsigned long long* __restrict__ out, int cap,
+                           int32_t* __restrict__ count, int32_t* __restrict__ err) {
+    const long long total = roff[n];
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long k = base + threadIdx.x;
+        bool keep = false;
+        unsigned long long key = 0;
+        if (k < total) {
+            int lo = 0, hi = n;  // roff[lo] <= k < roff[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (roff[mid] <= k)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const int p = order[lo], q = order[lo + 1 + (int)(k - roff[lo])];
+            if (!(is_static[p] && is_static[q]) && boxes_overlap(box + 6 * (size_t)p, box + 6 * (size_t)q)) {
+                const int i = p < q ? p : q, j = p < q ? q : p;
+                const int f = bp_filter_one(i, j, is_static, last, cur, radius, geo_eps, last_dt);
+                if (f < 0) atomicExch(err, 1);
+                keep = f > 0;
+                key = ((unsigned long long)(uint32_t)i << 32) | (uint32_t)j;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);  // base is uniform over the block
+        if (m) {
+            const int lead = __ffs(m) - 1;
+            int pos = 0;
+            if (lane == lead) pos = atomicAdd(count, __popc(m));
+            pos = __shfl_sync(0xffffffffu, pos, lead) + __popc(m & ((1u << lane) - 1u));
+            if (keep && pos < cap) out[pos] = key;
+        }
+    }
 }
 
 __global__ void k_bp_unpack(int n, const unsigned long long* __restrict__ key, int32_t* __restrict__ pairs) {
@@ -322,24 +354,51 @@ __global__ void k_cl_fill(int n_members, const int32_t* __restrict__ member_cid,
 }
 
 // Minimum current time, minimum last_dt and the sleeping flag of each
-// cluster over its moving members in order (separate_clusters.cpp:386-395).
+// cluster over its moving members in order (separate_clusters.cpp:386-395),
+// one warp per cluster.  The reference's running minimum from +inf keeps the
+// first of equal values and never takes a NaN; that is the leftmost minimum
+// over (value, member position), reduced with shuffles.
+__device__ __forceinline__ void lmin(double& v, int& i, double ov, int oi) {
+    if (ov < v || (ov == v && oi < i)) {
+        v = ov;
+        i = oi;
+    }
+}
 __global__ void k_cl_meta(int n_clusters, const int32_t* __restrict__ part_off, const int32_t* __restrict__ n_dyn,
                           const int32_t* __restrict__ parts, const double* __restrict__ cur,
                           const double* __restrict__ last_dt, const uint8_t* __restrict__ sleeping,
                           double* __restrict__ mct, double* __restrict__ step, int32_t* __restrict__ sleep) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_clusters) return;
-    double m = __longlong_as_double(0x7ff0000000000000LL), s = m;
-    int sl = 1;
-    for (int i = part_off[c]; i < part_off[c] + n_dyn[c]; i++) {
+    const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= n_clusters) return;  // uniform per warp
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    double m = inf, st = inf;
+    int mi = 0x7fffffff, si = 0x7fffffff;
+    bool awake = false;
+    const int i0 = part_off[c], i1 = part_off[c] + n_dyn[c];
+    for (int i = i0 + lane; i < i1; i += 32) {
         const int g = parts[i];
-        m = dmin(m, cur[14 * (size_t)g]);
-        s = dmin(s, last_dt[g]);
-        if (!sleeping[g]) sl = 0;
+        const double t = cur[14 * (size_t)g], l = last_dt[g];
+        if (t < m) {
+            m = t;
+            mi = i;
+        }
+        if (l < st) {
+            st = l;
+            si = i;
+        }
+        if (!sleeping[g]) awake = true;
     }
-    mct[c] = m;
-    step[c] = s;
-    sleep[c] = sl;
+    for (int o = 16; o > 0; o >>= 1) {
+        lmin(m, mi, __shfl_down_sync(0xffffffffu, m, o), __shfl_down_sync(0xffffffffu, mi, o));
+        lmin(st, si, __shfl_down_sync(0xffffffffu, st, o), __shfl_down_sync(0xffffffffu, si, o));
+    }
+    const bool any_awake = __any_sync(0xffffffffu, awake);
+    if (lane == 0) {
+        mct[c] = m;
+        step[c] = st;
+        sleep[c] = any_awake ? 0 : 1;
+    }
 }
 
 // separate_clusters.cpp:445-456: every moving body rolled back to its
@@ -431,42 +490,48 @@ int run_broad_phase(d2g_ctx* ctx, const float* d_aabb, int* n_out, int32_t* d_er
     RC(E.bp_key_s.ensure(n + 1));
     RC(E.bp_idx.ensure(n + 1));
     RC(E.bp_order.ensure(n + 1));
-    RC(E.bp_cnt.ensure(n + 1));
-    RC(E.bp_off.ensure(n + 1));
+    RC(E.bp_range.ensure(n + 1));
+    RC(E.bp_roff.ensure(n + 1));
+    RC(E.bp_count.ensure(1));
     BLAUNCH(k_bp_boxes, n, n, ctx->is_static.p, ctx->last.p, ctx->cur.p, ctx->fut.p, ctx->bounding_radius.p,
             ctx->geo_eps.p, d_aabb, ctx->scene.p, E.bp_box.p, E.bp_key.p, E.bp_idx.p);
     int scene_bits = 0;
     while (scene_bits < 31 && (1 << scene_bits) < ctx->n_scenes) scene_bits++;
     RC(sort_pairs(ctx, E.bp_key.p, E.bp_key_s.p, E.bp_idx.p, E.bp_order.p, n, 32 + scene_bits));
-    BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, ctx->scene.p, (const int32_t*)nullptr,
-            E.bp_cnt.p, (int32_t*)nullptr);
-    RC(bscan(ctx, E.bp_cnt.p, E.bp_off.p, n));
-    int n_cand = 0;
-    const int32_t* src = E.bp_off.p + n;
-    RC(read_ints(ctx, &src, 1, &n_cand));
-    RC(E.bp_cand.ensure(2 * (size_t)n_cand + 2));
-    RC(E.bp_flag.ensure(n_cand + 1));
-    RC(E.bp_foff.ensure(n_cand + 1));
-    RC(E.bp_pkey.ensure(n_cand + 1));
-    RC(E.bp_pkey2.ensure(n_cand + 1));
+    if (n > 0) BLAUNCH(k_bp_range, n, n, E.bp_order.p, E.bp_box.p, E.bp_key_s.p, E.bp_range.p);
+    // 64-bit exclusive scan of the range lengths: roff[n] = total range elements
+    D2G_CUDA(cudaMemsetAsync(E.bp_roff.p, 0, sizeof(long long), ctx->stream));
+    if (n > 0) {
+        size_t bytes = 0;
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, E.bp_range.p, E.bp_roff.p + 1, n, ctx->stream));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, E.bp_range.p, E.bp_roff.p + 1, n, ctx->stream));
+    }
+    // kept pairs: at most the previous capacity; on overflow grow and run again
+    RC(E.bp_pkey2.ensure(4 * (size_t)n + 1024));
+    int dev_sms = 0;
+    D2G_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int n_pairs = 0;
-    if (n_cand > 0) {
-        BLAUNCH(k_bp_sweep, n, n, E.bp_order.p, E.bp_box.p, ctx->is_static.p, ctx->scene.p, E.bp_off.p,
-                (int32_t*)nullptr, E.bp_cand.p);
-        BLAUNCH(k_bp_filter, n_cand, n_cand, E.bp_cand.p, ctx->is_static.p, ctx->last.p, ctx->cur.p,
-                ctx->bounding_radius.p, ctx->geo_eps.p, ctx->last_dt.p, E.bp_pkey.p, E.bp_flag.p, d_err);
-        RC(bscan(ctx, E.bp_flag.p, E.bp_foff.p, n_cand));
-        src = E.bp_foff.p + n_cand;
+    for (int pass = 0; pass < 2; pass++) {
+        const int cap = (int)std::min<size_t>(E.bp_pkey2.cap, (size_t)INT32_MAX);
+        D2G_CUDA(cudaMemsetAsync(E.bp_count.p, 0, sizeof(int32_t), ctx->stream));
+        k_bp_pairs<<<dev_sms * 8, 256, 0, ctx->stream>>>(
+            n, E.bp_roff.p, E.bp_order.p, E.bp_box.p, ctx->is_static.p, ctx->last.p, ctx->cur.p,
+            ctx->bounding_radius.p, ctx->geo_eps.p, ctx->last_dt.p, E.bp_pkey2.p, cap, E.bp_count.p, d_err);
+        ctx->eng.launches++;
+        const int32_t* src = E.bp_count.p;
         RC(read_ints(ctx, &src, 1, &n_pairs));
-        BLAUNCH(k_bp_compact, n_cand, n_cand, E.bp_flag.p, E.bp_foff.p, E.bp_pkey.p, E.bp_pkey2.p);
-        if (n_pairs > 0) {
-            size_t bytes = 0;
-            D2G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, bytes, E.bp_pkey2.p, E.bp_pkey.p, n_pairs, 0, 64,
-                                                    ctx->stream));
-            RC(E.cub_tmp.ensure(bytes + 16));
-            D2G_CUDA(cub::DeviceRadixSort::SortKeys(E.cub_tmp.p, bytes, E.bp_pkey2.p, E.bp_pkey.p, n_pairs, 0, 64,
-                                                    ctx->stream));
-        }
+        if (n_pairs <= cap) break;
+        RC(E.bp_pkey2.ensure((size_t)n_pairs + 1));
+    }
+    RC(E.bp_pkey.ensure(n_pairs + 1));
+    if (n_pairs > 0) {
+        size_t bytes = 0;
+        D2G_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, bytes, E.bp_pkey2.p, E.bp_pkey.p, n_pairs, 0, 64,
+                                                ctx->stream));
+        RC(E.cub_tmp.ensure(bytes + 16));
+        D2G_CUDA(cub::DeviceRadixSort::SortKeys(E.cub_tmp.p, bytes, E.bp_pkey2.p, E.bp_pkey.p, n_pairs, 0, 64,
+                                                ctx->stream));
     }
     RC(E.bp_pairs.ensure(2 * (size_t)n_pairs + 2));
     if (n_pairs > 0) BLAUNCH(k_bp_unpack, n_pairs, n_pairs, E.bp_pkey.p, E.bp_pairs.p);
@@ -566,7 +631,7 @@ int run_clusters(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int n_dyn_to
         RC(bscan(ctx, E.cl_n_all.p, E.cl_part_off.p, nc));
         BLAUNCH(k_cl_fill, m, n_dyn_total, member_cid, E.cl_member.p, E.cl_dyn_off.p, n_st, E.cl_st_key4.p,
                 E.cl_st_body4.p, E.cl_stat_off.p, E.cl_part_off.p, E.cl_n_dyn.p, E.cl_parts.p);
-        BLAUNCH(k_cl_meta, nc, nc, E.cl_part_off.p, E.cl_n_dyn.p, E.cl_parts.p, ctx->cur.p, ctx->last_dt.p,
+        BLAUNCH(k_cl_meta, 32LL * nc, nc, E.cl_part_off.p, E.cl_n_dyn.p, E.cl_parts.p, ctx->cur.p, ctx->last_dt.p,
                 ctx->sleeping.p, E.cl_mct.p, E.cl_step.p, E.cl_sleep.p);
         if (n_pairs > 0) BLAUNCH(k_cl_pair_count, n_pairs, n_pairs, E.cl_pair_cid.p, E.cl_pair_cnt.p);
         RC(bscan(ctx, E.cl_pair_cnt.p, E.cl_pair_off.p, nc));

@@ -152,7 +152,8 @@ struct Engine {
     // GPU broad phase (d2g_broadphase.cu)
     DBuf<float> bp_box;
     DBuf<unsigned long long> bp_key, bp_key_s;
-    DBuf<int32_t> bp_idx, bp_order, bp_cnt, bp_off, bp_cand, bp_flag, bp_foff, bp_pairs;
+    DBuf<int32_t> bp_idx, bp_order, bp_count, bp_pairs;
+    DBuf<long long> bp_range, bp_roff;
     DBuf<unsigned long long> bp_pkey, bp_pkey2;
     // GPU cluster separation (d2g_broadphase.cu)
     DBuf<int32_t> uf_parent, uf_root, uf_roff, cl_cid, cl_uidx, cl_member, cl_pair_cid, cl_piota, cl_porder,

@@ -112,51 +112,155 @@ __global__ void k_pair_new_dt(int n_pairs, const int32_t* __restrict__ pairs, co
     }
 }
 
+// Leftmost minimum of (value, index) over a block (all threads call it; the
+// result is returned to every thread).  red holds 2 * 32 words.
+__device__ void block_lmin(double& v, int& i, double* red_v, int* red_i) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, v, o);
+        const int oi = __shfl_down_sync(0xffffffffu, i, o);
+        if (ov < v || (ov == v && oi < i)) {
+            v = ov;
+            i = oi;
+        }
+    }
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        red_v[w] = v;
+        red_i[w] = i;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < nw; k++)
+            if (red_v[k] < v || (red_v[k] == v && red_i[k] < i)) {
+                v = red_v[k];
+                i = red_i[k];
+            }
+        red_v[0] = v;
+        red_i[0] = i;
+    }
+    __syncthreads();
+    v = red_v[0];
+    i = red_i[0];
+}
+
+constexpr int kStepsBlock = 256;
+constexpr int kStepsChunk = 1024;  // interactions staged per pass
+
 // The reference's order-dependent propagation over a cluster's interactions
-// (separate_clusters.cpp:555-598), one block per cluster: the moving bodies'
-// steps live in shared memory (loc maps a moving body to its slot), thread 0
-// walks the interactions in order.
-__global__ void k_cluster_steps(int n_clusters, const int32_t* __restrict__ cl_pair_off,
-                                const int32_t* __restrict__ cl_part_off, const int32_t* __restrict__ cl_parts,
-                                const int32_t* __restrict__ pairs, const double* __restrict__ new_dt,
-                                const int32_t* __restrict__ has, const uint8_t* __restrict__ is_static,
-                                const double* __restrict__ last_dt, int32_t* __restrict__ loc, double opt_dt,
-                                double* __restrict__ out, double* __restrict__ gstep) {
-    extern __shared__ double s_dyn[];
+// (separate_clusters.cpp:555-598), one block per cluster.  The moving bodies'
+// steps live in shared memory (loc maps a moving body to its slot).  Each
+// chunk of interactions is first staged by all threads as (slot a, slot b,
+// new step, step of the static side), then thread 0 walks the chunk in order
+// touching shared memory only.  The final running minimum is a leftmost-
+// minimum reduction when every value is non-negative (the fold is then
+// associative); otherwise thread 0 repeats the reference's fold.
+__global__ void __launch_bounds__(kStepsBlock)
+    k_cluster_steps(int n_clusters, const int32_t* __restrict__ cl_pair_off, const int32_t* __restrict__ cl_part_off,
+                    const int32_t* __restrict__ cl_parts, const int32_t* __restrict__ pairs,
+                    const double* __restrict__ new_dt, const int32_t* __restrict__ has,
+                    const uint8_t* __restrict__ is_static, const double* __restrict__ last_dt,
+                    int32_t* __restrict__ loc, double opt_dt, double* __restrict__ out, double* __restrict__ gstep,
+                    int n_step_slots, int chunk) {
+    extern __shared__ __align__(16) double s_dyn[];
+    __shared__ double red_v[32];
+    __shared__ int red_i[32];
     const int c = blockIdx.x;
     if (c >= n_clusters) return;
     const int p0 = cl_part_off[c], p1 = cl_part_off[c + 1];
     double* s_step = gstep ? gstep + p0 : s_dyn;  // global scratch for clusters too large for shared memory
+    double2* r_val = reinterpret_cast<double2*>(s_dyn + n_step_slots);
+    int2* r_slot = reinterpret_cast<int2*>(r_val + chunk);
     for (int i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
         const int g = cl_parts[i];
         s_step[i - p0] = last_dt[g];
         if (!is_static[g]) loc[g] = i - p0;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
+    const int q0 = cl_pair_off[c], q1 = cl_pair_off[c + 1];
+    for (int base = q0; base < q1; base += chunk) {
+        const int n = min(chunk, q1 - base);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const int i = base + j;
+            int sa = -1, sb = -1;
+            double nd = 0.0, sv = 0.0;
+            if (has[i]) {
+                const int a = pairs[2 * i], b = pairs[2 * i + 1];
+                const bool as = is_static[a], bs = is_static[b];
+                if (!(as && bs)) {  // two static sides write nothing
+                    sa = as ? -1 : loc[a];
+                    sb = bs ? -1 : loc[b];
+                    nd = new_dt[i];
+                    sv = as ? last_dt[a] : (bs ? last_dt[b] : 0.0);
+                }
+            }
+            r_slot[j] = make_int2(sa, sb);
+            r_val[j] = make_double2(nd, sv);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int j = 0; j < n; j++) {
+                const int2 sl = r_slot[j];
+                if ((sl.x & sl.y) < 0) continue;  // no contact, or both sides static
+                const double2 v = r_val[j];
+                const double va = sl.x >= 0 ? s_step[sl.x] : v.y;
+                const double vb = sl.y >= 0 ? s_step[sl.y] : v.y;
+                const double use = dmin_fast(v.x, dmin_fast(va, vb));
+                if (sl.x >= 0) s_step[sl.x] = use;
+                if (sl.y >= 0) s_step[sl.y] = use;
+            }
+        }
+        __syncthreads();
+    }
     auto step_of = [&](int g) { return is_static[g] ? last_dt[g] : s_step[loc[g]]; };
-    for (int i = cl_pair_off[c]; i < cl_pair_off[c + 1]; i++) {
-        if (!has[i]) continue;
+    // the first interaction with a moving side contributes the step of its
+    // first body, every later one the step of its moving (or first) body
+    double fv = 0.0;
+    int first = 0x7fffffff;
+    for (int i = q0 + threadIdx.x; i < q1; i += blockDim.x)
+        if (!(is_static[pairs[2 * i]] && is_static[pairs[2 * i + 1]])) {
+            first = i;
+            break;
+        }
+    block_lmin(fv, first, red_v, red_i);
+    double best = __longlong_as_double(0x7ff0000000000000LL);
+    int bi = 0x7fffffff;
+    bool irregular = false;
+    for (int i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
         const int a = pairs[2 * i], b = pairs[2 * i + 1];
-        const double use = dmin_fast(new_dt[i], dmin_fast(step_of(a), step_of(b)));
-        if (!is_static[a]) s_step[loc[a]] = use;
-        if (!is_static[b]) s_step[loc[b]] = use;
+        const bool as = is_static[a], bs = is_static[b];
+        if (as && bs) continue;
+        const double v = step_of(i == first || !as ? a : b);
+        if (!(v >= 0.0)) irregular = true;
+        if (v < best) {
+            best = v;
+            bi = i;
+        }
     }
+    irregular = __syncthreads_or(irregular);
+    block_lmin(best, bi, red_v, red_i);
+    if (threadIdx.x != 0) return;
     double cs = -1.0;
-    for (int i = cl_pair_off[c]; i < cl_pair_off[c + 1]; i++) {
-        const int a = pairs[2 * i], b = pairs[2 * i + 1];
-        int id;
-        if (!is_static[a] && !is_static[b])
-            id = a;
-        else if (is_static[a] && is_static[b])
-            continue;
-        else if (is_static[a])
-            id = b;
-        else
-            id = a;
-        cs = cs < 0.0 ? step_of(a) : dmin_fast(cs, step_of(id));
+    if (first == 0x7fffffff) {
+        cs = last_dt[cl_parts[p0]];
+    } else if (!irregular) {
+        cs = best;
+    } else {
+        for (int i = q0; i < q1; i++) {
+            const int a = pairs[2 * i], b = pairs[2 * i + 1];
+            int id;
+            if (!is_static[a] && !is_static[b])
+                id = a;
+            else if (is_static[a] && is_static[b])
+                continue;
+            else if (is_static[a])
+                id = b;
+            else
+                id = a;
+            cs = cs < 0.0 ? step_of(a) : dmin_fast(cs, step_of(id));
+        }
+        if (cs < 0.0) cs = last_dt[cl_parts[p0]];
     }
-    if (cs < 0.0) cs = last_dt[cl_parts[p0]];
     out[c] = dmax(1e-3, dmin(cs, opt_dt));
 }
 
@@ -534,19 +638,23 @@ int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const in
     if (n_clusters > 0) {
         RC(E.st_loc.ensure(ctx->n_bodies + 1));
         constexpr int kMaxSmemParts = 24 * 1024;  // 192 KB of steps
+        // staged interactions per pass: enough for a cluster's interactions
+        // (about twice its members), at most kStepsChunk
+        int chunk = 32;
+        while (chunk < kStepsChunk && chunk < 2 * max_cluster_parts) chunk *= 2;
         double* gstep = nullptr;
-        size_t smem = (size_t)max_cluster_parts * sizeof(double);
+        int n_slots = (max_cluster_parts + 1) & ~1;  // keeps the double2 records 16-byte aligned
         if (max_cluster_parts > kMaxSmemParts) {
             RC(E.st_step.ensure((size_t)n_parts + 1));
             gstep = E.st_step.p;
-            smem = 0;
-        } else if (smem > 48 * 1024) {
-            D2G_CUDA(cudaFuncSetAttribute(k_cluster_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(kMaxSmemParts * sizeof(double))));
+            n_slots = 0;
         }
-        k_cluster_steps<<<n_clusters, kBlock, smem, ctx->stream>>>(
+        const size_t smem = (size_t)n_slots * sizeof(double) + (size_t)chunk * (sizeof(double2) + sizeof(int2));
+        if (smem > 48 * 1024)
+            D2G_CUDA(cudaFuncSetAttribute(k_cluster_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_cluster_steps<<<n_clusters, kStepsBlock, smem, ctx->stream>>>(
             n_clusters, d_cl_pair_off, d_cl_part_off, d_cl_parts, d_pairs, E.st_new_dt.p, E.st_has.p,
-            ctx->is_static.p, ctx->last_dt.p, E.st_loc.p, opt_dt, d_out, gstep);
+            ctx->is_static.p, ctx->last_dt.p, E.st_loc.p, opt_dt, d_out, gstep, n_slots, chunk);
         ctx->eng.launches++;
     }
     D2G_CUDA(cudaGetLastError());
