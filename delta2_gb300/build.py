@@ -79,7 +79,7 @@ def build(force=False, verbose=False):
     for src in CPP_SOURCES:
         o = os.path.join(OBJ, os.path.basename(src).replace(".cpp", ".o"))
         jobs.append(["g++", "-c", os.path.join(CSRC, src), "-o", o, "-O2", "-std=c++17", "-fPIC",
-                     "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
+                     "-ffp-contract=off", "-fno-fast-math", "-pthread", "-Wall", "-Wno-unused-function",
                      "-I" + os.path.join(cuda, "include"), "-I" + CSRC])
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         outs = list(ex.map(_run, jobs))
@@ -89,7 +89,7 @@ def build(force=False, verbose=False):
                 print(o)
     objs = [j[j.index("-o") + 1] for j in jobs]
     tmp = LIB + ".tmp"
-    _run([nvcc, "-shared", ARCH, "-o", tmp] + objs + ["-Xcompiler=-fPIC"])
+    _run([nvcc, "-shared", ARCH, "-o", tmp] + objs + ["-Xcompiler=-fPIC,-pthread"])
     os.replace(tmp, LIB)
     with open(stamp, "w") as f:
         f.write(fp)

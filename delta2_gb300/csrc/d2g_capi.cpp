@@ -221,6 +221,9 @@ int d2g_ctx_create(int32_t device, d2g_ctx** out) {
     d2g_ctx* c = new d2g_ctx();
     c->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_pinned, 64 * sizeof(int32_t));
     if (e != cudaSuccess) {
         set_error(std::string("context creation: ") + cudaGetErrorString(e));
@@ -301,6 +304,7 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     E.d_pairs.release();
     E.d_max_time.release();
     E.cub_tmp.release();
+    E.cub_tmp2.release();
     E.scratch_i32.release();
     for (auto& p : E.pending) {
         cudaEventDestroy(p.e0);
@@ -308,6 +312,9 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     }
     for (auto ev : E.event_pool) cudaEventDestroy(ev);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

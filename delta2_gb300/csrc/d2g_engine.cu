@@ -89,27 +89,45 @@ __global__ void k_np_prep(int n, const int32_t* __restrict__ pairs, const double
 }
 
 // ------------------------------------------------------------ soup stage ---
-// Swept-box filter of every (node pair, a-triangle, b-triangle) slot
-// (continuous_comparison.h:804-812).
-__global__ void k_soup_filter(int n_slots, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
+// The swept-AABB prefilter of every (triangle of a, triangle of b) slot of a
+// soup node pair (continuous_comparison.h:804-812), one warp per node pair:
+// lanes 0-7 form the swept boxes of a's triangles, lanes 8-15 those of b's,
+// once each, and every lane then tests two of the 64 slots from shuffled
+// boxes.  flags[64 * entry + 8 * ta + tb] = 1 where the boxes overlap.
+__global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
                               const double* __restrict__ pm, const int32_t* __restrict__ ntris,
                               const double* __restrict__ tris, const double* __restrict__ geo_eps,
                               int32_t* __restrict__ flags) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_slots) return;
-    const Entry e = soup[i >> 6];
-    const int ta = (i >> 3) & 7, tb = i & 7;
-    int f = 0;
-    if (ta < ntris[e.na] && tb < ntris[e.nb]) {
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_soup) return;  // uniform per warp
+    const Entry e = soup[w];
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    const bool side_b = lane >= 8;
+    const int t = lane & 7;
+    Box bx;
+#pragma unroll
+    for (int k = 0; k < 3; k++) bx.lo[k] = bx.hi[k] = 0.0;
+    if (lane < 16 && t < (side_b ? nb : na)) {
         const double* M = pm + (size_t)PM_SIZE * e.pair;
-        const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
-        const Tri at = load_tri(tris + (size_t)e.na * 72 + ta * 9);
-        const Tri bt = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
-        const Box ba = swept_box(at, M + PM_AS, M + PM_AE, geo_eps[a]);
-        const Box bb = swept_box(bt, M + PM_BS, M + PM_BE, geo_eps[b]);
-        f = box_overlap(ba, bb) ? 1 : 0;
+        const int body = pairs[2 * e.pair + (side_b ? 1 : 0)];
+        const Tri tri = load_tri(tris + (size_t)(side_b ? e.nb : e.na) * 72 + t * 9);
+        bx = side_b ? swept_box(tri, M + PM_BS, M + PM_BE, geo_eps[body])
+                    : swept_box(tri, M + PM_AS, M + PM_AE, geo_eps[body]);
     }
-    flags[i] = f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+        Box A, B;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            A.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], ta);
+            A.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], ta);
+            B.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], 8 + tb);
+            B.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], 8 + tb);
+        }
+        flags[64 * (size_t)w + sl] = (ta < na && tb < nb && box_overlap(A, B)) ? 1 : 0;
+    }
 }
 
 __global__ void k_compact(int n, const int32_t* __restrict__ flags, const int32_t* __restrict__ off,
@@ -473,97 +491,284 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, c
     chit[item] = r.dist < (double)search[e.pair] ? 1 : 0;
 }
 
-__global__ void __launch_bounds__(kPrimBlock) k_prim_ee(int n_tp, int n_total, const int32_t* __restrict__ items,
-                                                        const Entry* __restrict__ soup, const Entry* __restrict__ conn,
-                                                        const int32_t* __restrict__ nn_off, int n_conn,
-                                                        const double* __restrict__ pm,
-                                                        const int32_t* __restrict__ ntris,
-                                                        const double* __restrict__ tris,
-                                                        const float* __restrict__ search,
-                                                        PrimResult* __restrict__ sub, PrimResult* __restrict__ cres,
-                                                        int32_t* __restrict__ chit, const int32_t* __restrict__ list,
-                                                        const int32_t* __restrict__ n_list) {
-    // work item list[kk] (every item when list is null)
-    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
-    if (kk >= n_total || (n_list && kk >= *n_list)) return;
-    const int j = list ? list[kk] : kk;
-    Entry e;
-    int aTri, aEdge, bTri, bEdge;
-    size_t item = 0;
-    int k = -1, s = 0;
-    if (j < 9 * n_tp) {
-        k = j / 9;
-        const int w = j % 9;
-        const int slot = items[k];
-        e = soup[slot >> 6];
-        aTri = (slot >> 3) & 7;
-        bTri = slot & 7;
-        aEdge = w / 3;
-        bEdge = w % 3;
-        s = 5 * aEdge + 2 + bEdge;
+// Edge-edge CCD in two kernels over the level's surviving tests.  GB300's
+// FP64 pipe takes one warp instruction per 64 cycles per SM sub-partition
+// (SMSP), dependent or not and whatever the number of active lanes (a
+// division costs ~9 such slots, a square root ~10), and a level has only a
+// few thousand surviving tests, so a warp's time is the instruction count of
+// its longest lane and the level's time that of its slowest warp.  62% of the
+// tests end within two Newton iterations and 20% run all ten, so:
+//   k_ee_first   one test per lane: edges, FP64 box-gap skip, the bisection
+//                (its cost is about two Newton iterations) or at most two
+//                Newton iterations; the tests still running are saved and
+//                listed.
+//   k_ee_rest4   the listed tests on four lanes each (below): the remaining
+//                iterations with about half the instructions per iteration,
+//                on few enough warps that each has an SMSP to itself.
+// Each test performs exactly the operations of edge_edge_ccd, in order.
+constexpr int kEeFirstIters = 2;
+constexpr int kEeRec = 34;  // saved test: 24 point coordinates, t, min_dist, P, Q, toc, iterations done
+struct EeArgs {
+    int n_tp, n_conn;
+    const int32_t* items;
+    const Entry* soup;
+    const Entry* conn;
+    const int32_t* nn_off;
+    const int32_t* ntris;
+    const float* search;
+    PrimResult* sub;
+    PrimResult* cres;
+    int32_t* chit;
+    double* rec;     // kEeRec per listed test
+    int32_t* out;    // the test's result slot: soup sub-result s >= 0, or leaf-pair item -1 - s
+    float* thr;      // the test's hit threshold (leaf-pair tests)
+    int32_t* count;  // [0] listed tests
+};
+
+__device__ __forceinline__ void ee_store_at(const EeArgs& a, int o, float thr, const Ccd& r) {
+    if (o < 0) {  // leaf-pair test: P and Q swapped (continuous_comparison.h:881-896)
+        store_prim(a.cres + (-1 - o), r.dist, r.Q, r.P, r.toc);
+        a.chit[-1 - o] = r.dist < (double)thr ? 1 : 0;
     } else {
-        const int jp = j - 9 * n_tp;
-        const int ei = find_entry(nn_off, n_conn, 9, jp);
-        e = conn[ei];
-        const int m = jp - 9 * nn_off[ei];
-        const int na = ntris[e.na], nb = ntris[e.nb];
-        const int ea = m / (3 * nb), eb = m % (3 * nb);
-        aTri = ea / 3;
-        aEdge = ea % 3;
-        bTri = eb / 3;
-        bEdge = eb % 3;
-        item = 15 * (size_t)nn_off[ei] + 6 * (size_t)na * nb + m;
+        store_prim(a.sub + o, r.dist, r.P, r.Q, r.toc);
     }
-    const double* M = pm + (size_t)PM_SIZE * e.pair;
-    const Edge ea = tedge(load_tri(tris + (size_t)e.na * 72 + aTri * 9), aEdge);
-    const Edge eb = tedge(load_tri(tris + (size_t)e.nb * 72 + bTri * 9), bEdge);
+}
+
+__global__ void __launch_bounds__(kPrimBlock) k_ee_first(int n_total, const int32_t* __restrict__ list,
+                                                         const int32_t* __restrict__ n_list,
+                                                         const double* __restrict__ pm,
+                                                         const double* __restrict__ tris, EeArgs a) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    bool keep = false;
+    int o = 0;
+    float thr = 0.f;
     Edge aS, aE, bS, bE;
-    aS.A = xform_rigid(ea.A, M + PM_AS);
-    aS.B = xform_rigid(ea.B, M + PM_AS);
-    aE.A = xform_rigid(ea.A, M + PM_AE);
-    aE.B = xform_rigid(ea.B, M + PM_AE);
-    bS.A = xform_rigid(eb.A, M + PM_BS);
-    bS.B = xform_rigid(eb.B, M + PM_BS);
-    bE.A = xform_rigid(eb.A, M + PM_BE);
-    bE.B = xform_rigid(eb.B, M + PM_BE);
-    // Every distance edgeEdgeCCD can return is between points of the two
-    // swept segments, which lie in the boxes of their four endpoint positions.
-    // A box gap beyond the search distance (plus 1e-7 m, far above FP64
-    // rounding at scene scale) means no hit, and such a sub-test can never be
-    // the best of a triangle pair that hits: skip it, recording +inf.
-    const double lim = (double)search[e.pair] + 1e-7;
-    double gap2 = 0.0;
-    {
-        const double ax[4] = {aS.A.x, aS.B.x, aE.A.x, aE.B.x}, ay[4] = {aS.A.y, aS.B.y, aE.A.y, aE.B.y},
-                     az[4] = {aS.A.z, aS.B.z, aE.A.z, aE.B.z};
-        const double bx[4] = {bS.A.x, bS.B.x, bE.A.x, bE.B.x}, by[4] = {bS.A.y, bS.B.y, bE.A.y, bE.B.y},
-                     bz[4] = {bS.A.z, bS.B.z, bE.A.z, bE.B.z};
-        const double* av[3] = {ax, ay, az};
-        const double* bv[3] = {bx, by, bz};
+    Ccd r;
+    double min_dist = DBL_MAX, t = 0.0;
+    int iters = 0;
+    if (kk < n_total && kk < *n_list) {
+        const int j = list[kk];
+        const EeWork w = decode_ee(j, a.n_tp, a.items, a.soup, a.conn, a.nn_off, a.n_conn, a.ntris, a.sub, a.cres,
+                                   a.chit);
+        o = w.hit ? -1 - (int)(w.out - a.cres) : (int)(w.out - a.sub);
+        thr = a.search[w.pair];
+        const double* M = pm + (size_t)PM_SIZE * w.pair;
+        const Edge ea = tedge(load_tri(tris + (size_t)w.na * 72 + w.aTri * 9), w.aEdge);
+        const Edge eb = tedge(load_tri(tris + (size_t)w.nb * 72 + w.bTri * 9), w.bEdge);
+        aS.A = xform_rigid(ea.A, M + PM_AS);
+        aS.B = xform_rigid(ea.B, M + PM_AS);
+        aE.A = xform_rigid(ea.A, M + PM_AE);
+        aE.B = xform_rigid(ea.B, M + PM_AE);
+        bS.A = xform_rigid(eb.A, M + PM_BS);
+        bS.B = xform_rigid(eb.B, M + PM_BS);
+        bE.A = xform_rigid(eb.A, M + PM_BE);
+        bE.B = xform_rigid(eb.B, M + PM_BE);
+        // Every distance edgeEdgeCCD can return is between points of the two
+        // swept segments, which lie in the boxes of their four endpoint
+        // positions.  A box gap beyond the search distance (plus 1e-7 m, far
+        // above FP64 rounding at scene scale) means no hit, and such a
+        // sub-test can never be the best of a triangle pair that hits: skip
+        // it, recording +inf.
+        const double lim = (double)thr + 1e-7;
+        double gap2 = 0.0;
+        {
+            const double ax[4] = {aS.A.x, aS.B.x, aE.A.x, aE.B.x}, ay[4] = {aS.A.y, aS.B.y, aE.A.y, aE.B.y},
+                         az[4] = {aS.A.z, aS.B.z, aE.A.z, aE.B.z};
+            const double bx[4] = {bS.A.x, bS.B.x, bE.A.x, bE.B.x}, by[4] = {bS.A.y, bS.B.y, bE.A.y, bE.B.y},
+                         bz[4] = {bS.A.z, bS.B.z, bE.A.z, bE.B.z};
+            const double* av[3] = {ax, ay, az};
+            const double* bv[3] = {bx, by, bz};
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-            const double alo = fmin(fmin(av[d][0], av[d][1]), fmin(av[d][2], av[d][3]));
-            const double ahi = fmax(fmax(av[d][0], av[d][1]), fmax(av[d][2], av[d][3]));
-            const double blo = fmin(fmin(bv[d][0], bv[d][1]), fmin(bv[d][2], bv[d][3]));
-            const double bhi = fmax(fmax(bv[d][0], bv[d][1]), fmax(bv[d][2], bv[d][3]));
-            const double g = fmax(blo - ahi, alo - bhi);
-            if (g > 0.0) gap2 = gap2 + g * g;
+            for (int d = 0; d < 3; d++) {
+                const double alo = fmin(fmin(av[d][0], av[d][1]), fmin(av[d][2], av[d][3]));
+                const double ahi = fmax(fmax(av[d][0], av[d][1]), fmax(av[d][2], av[d][3]));
+                const double blo = fmin(fmin(bv[d][0], bv[d][1]), fmin(bv[d][2], bv[d][3]));
+                const double bhi = fmax(fmax(bv[d][0], bv[d][1]), fmax(bv[d][2], bv[d][3]));
+                const double g = fmax(blo - ahi, alo - bhi);
+                if (g > 0.0) gap2 = gap2 + g * g;
+            }
+        }
+        if (gap2 > lim * lim) {
+            record_no_contact(w.out, w.hit);
+        } else {
+            r.P = mk(0, 0, 0);
+            r.Q = mk(0, 0, 0);
+            r.toc = 0.0;
+            const double dot_start = ee_coplanarity(aS, bS);
+            const double dot_end = ee_coplanarity(aE, bE);
+            bool bisected = false;
+            if (dot_start * dot_end < 0.0) {
+                min_dist = ee_bisect(aS, aE, bS, bE, dot_start, r);
+                bisected = true;
+            }
+            bool done = !(min_dist > 1e-8);
+            if (!done && !bisected) {
+                for (; iters < kEeFirstIters; iters++)
+                    if (ee_newton_iter(aS, aE, bS, bE, t, min_dist, r)) {
+                        done = true;
+                        break;
+                    }
+            }
+            if (done) {
+                r.dist = min_dist;
+                ee_store_at(a, o, thr, r);
+            } else {
+                keep = true;  // the remaining iterations run in k_ee_rest4
+            }
         }
     }
-    Ccd r;
-    if (gap2 > lim * lim) {
-        r.dist = 1.0 / 0.0;
-        r.P = mk(0, 0, 0);
-        r.Q = mk(0, 0, 0);
-        r.toc = 1.0;
-    } else {
-        r = edge_edge_ccd(aS, aE, bS, bE);
+    // warp-aggregated append of the tests still running
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (m) {
+        const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+        int base = 0;
+        if (lane == lead) base = atomicAdd(a.count, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, lead);
+        if (keep) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            double* R = a.rec + (size_t)kEeRec * slot;
+            const V3 v[8] = {aS.A, aS.B, aE.A, aE.B, bS.A, bS.B, bE.A, bE.B};
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                R[3 * k] = v[k].x;
+                R[3 * k + 1] = v[k].y;
+                R[3 * k + 2] = v[k].z;
+            }
+            const double tail[10] = {t, min_dist, r.P.x, r.P.y, r.P.z, r.Q.x, r.Q.y, r.Q.z, r.toc, (double)iters};
+#pragma unroll
+            for (int k = 0; k < 10; k++) R[24 + k] = tail[k];
+            a.out[slot] = o;
+            a.thr[slot] = thr;
+        }
     }
-    if (k >= 0) {
-        store_prim(sub + 15 * (size_t)k + s, r.dist, r.P, r.Q, r.toc);
-    } else {
-        store_prim(cres + item, r.dist, r.Q, r.P, r.toc);
-        chit[item] = r.dist < (double)search[e.pair] ? 1 : 0;
+}
+
+// ---- the Newton phase on four lanes per test ------------------------------
+// GB300 issues an FP64 warp instruction at the same cost whatever the number
+// of active lanes, and a level has far fewer surviving edge-edge tests than
+// the GPU has lanes, so a test's time is the number of FP64 instructions on
+// its path.  Here each test runs on a quad of lanes: lane c < 3 holds
+// component c of every point (lane 3 mirrors x), vector operations are one
+// instruction for all three components, a dot product is one multiply and the
+// two adds (x + y) + z of the reference's order, and independent divisions
+// share one instruction stream on different lanes.  Scalars are computed
+// identically on all four lanes, so every branch is uniform within a quad.
+// Every value is produced by the same operations, in the same order, as in
+// edge_edge_ccd.
+struct Quad {
+    unsigned m;  // the quad's lanes
+    int base;    // its first lane
+    int c;       // this lane's component (3: mirror of x)
+};
+__device__ __forceinline__ double q_at(const Quad& q, double v, int k) { return __shfl_sync(q.m, v, q.base + k); }
+__device__ __forceinline__ double q_dot(const Quad& q, double a, double b) {
+    const double p = a * b;
+    const double px = q_at(q, p, 0), py = q_at(q, p, 1), pz = q_at(q, p, 2);
+    return (px + py) + pz;
+}
+__device__ __forceinline__ double q_lerp(double A, double B, double t) {
+    const double u = 1 - t;
+    return A * u + B * t;
+}
+// components differ anywhere (vne)
+__device__ __forceinline__ bool q_ne(const Quad& q, double a, double b) {
+    const unsigned bal = __ballot_sync(q.m, q.c < 3 && a != b);
+    return ((bal >> q.base) & 7u) != 0u;
+}
+// edge_constrain(A, B, pos)
+__device__ __forceinline__ double q_constrain(const Quad& q, double A, double B, double pos) {
+    const double ba = B - A;
+    const double t = q_dot(q, pos - A, ba) / q_dot(q, ba, ba);
+    return q_lerp(A, B, clamp01(t));
+}
+// edge_closest(SA, SB, EA, EB, P, Q): one component per lane
+__device__ __forceinline__ double q_edge_closest(const Quad& q, double SA, double SB, double EA, double EB, double& P,
+                                                 double& Qo) {
+    const double segDC = EB - EA;
+    const double lineDirSqrMag = q_dot(q, segDC, segDC);
+    const double segAC = SA - EA;
+    const double segBC = SB - EA;
+    const double nA = q_dot(q, segAC, segDC), nB = q_dot(q, segBC, segDC);
+    const double s2 = ((q.c & 1) ? nB : nA) / lineDirSqrMag;  // lanes 0, 2: A; 1, 3: B
+    const double sA = q_at(q, s2, 0), sB = q_at(q, s2, 1);
+    const double inPlaneA = SA - sA * segDC;
+    const double inPlaneB = SB - sB * segDC;
+    const double inPlaneBA = inPlaneB - inPlaneA;
+    double t = q_dot(q, EA - inPlaneA, inPlaneBA) / q_dot(q, inPlaneBA, inPlaneBA);
+    t = q_ne(q, inPlaneA, inPlaneB) ? t : 0.0;
+    const double segABtoLineCD = q_lerp(SA, SB, clamp01(t));
+    const double segCDtoSegAB = q_constrain(q, EA, EB, segABtoLineCD);
+    const double segABtoSegCD = q_constrain(q, SA, SB, segCDtoSegAB);
+    Qo = segCDtoSegAB;
+    P = segABtoSegCD;
+    const double d = Qo - P;
+    return sqrt(q_dot(q, d, d));
+}
+
+__global__ void __launch_bounds__(kBlock) k_ee_rest4(EeArgs a) {
+    const int n = a.count[0];
+    Quad q;
+    q.m = 0xFu << (threadIdx.x & 28);
+    q.base = threadIdx.x & 28;
+    q.c = threadIdx.x & 3;
+    const int comp = q.c < 3 ? q.c : 0;
+    const int n_quads = (gridDim.x * blockDim.x) >> 2;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < n; i += n_quads) {
+        const double* R = a.rec + (size_t)kEeRec * i;
+        // aS.A, aS.B, aE.A, aE.B, bS.A, bS.B, bE.A, bE.B (this lane's component)
+        const double aSA = R[comp], aSB = R[3 + comp], aEA = R[6 + comp], aEB = R[9 + comp];
+        const double bSA = R[12 + comp], bSB = R[15 + comp], bEA = R[18 + comp], bEB = R[21 + comp];
+        double t = R[24], min_dist = R[25];
+        double rP = R[26 + comp], rQ = R[29 + comp], toc = R[32];
+        for (int iter = (int)R[33]; iter < kEeNewtonIters; iter++) {
+            const double atA = q_lerp(aSA, aEA, t), atB = q_lerp(aSB, aEB, t);
+            const double btA = q_lerp(bSA, bEA, t), btB = q_lerp(bSB, bEB, t);
+            double P, Qv;
+            const double dist = q_edge_closest(q, atA, atB, btA, btB, P, Qv);
+            if (dist < min_dist) {
+                min_dist = dist;
+                rP = P;
+                rQ = Qv;
+                toc = t;
+            }
+            // edge_project(atA, atB, P) and edge_project(btA, btB, Q), divided on lanes 0 / 1
+            const double AB = atB - atA, CD = btB - btA;
+            const double na = q_dot(q, P - atA, AB), da = q_dot(q, AB, AB);
+            const double nb = q_dot(q, Qv - btA, CD), db = q_dot(q, CD, CD);
+            const double pr = ((q.c & 1) ? nb : na) / ((q.c & 1) ? db : da);
+            const double pa = q_at(q, pr, 0), pb = q_at(q, pr, 1);
+            // ee_newton_terms, component per lane
+            const double omt = 1 - t, ompa = 1 - pa, ompb = 1 - pb, pbm1 = pb - 1;
+            const double f = ((pa * (aEB + aSB * omt) - pb * (bEB + bSB * omt)) + ompa * (aEA * t + aSA * omt)) -
+                             ompb * (bEA * t + bSA * omt);
+            const double g = ((-2 * aSB * pa + 2 * bSB * pb) + 2 * ompa * (aEA - aSA)) + 2 * (bEA - bSA) * pbm1;
+            const double h = ((-aSB * pa / 2 + bSB * pb / 2) + ompa * (aEA - aSA) / 2) + (bEA - bSA) * pbm1 / 2;
+            const double gf2 = g * f / 2, gh = g * h, ff = f * f;
+            const double gf = (q_at(q, gf2, 0) + q_at(q, gf2, 1)) + q_at(q, gf2, 2);
+            const double S = (q_at(q, ff, 0) + q_at(q, ff, 1)) + q_at(q, ff, 2);
+            const double GH = (q_at(q, gh, 0) + q_at(q, gh, 1)) + q_at(q, gh, 2);
+            const double sS = sqrt(S);
+            // gf / sS, GH / sS and (-gf * gf) / pow15(S) on lanes 0, 1, 2
+            const double num = q.c == 1 ? GH : (q.c == 2 ? (-gf) * gf : gf);
+            const double den = q.c == 2 ? m_pow15(S) : sS;
+            const double quo = num / den;
+            const double t_diff = q_at(q, quo, 0);
+            const double t_diff2 = q_at(q, quo, 1) + q_at(q, quo, 2);
+            const double t_prev = t;
+            t = t - t_diff / t_diff2;
+            t = clamp01(t);
+            if (t == t_prev || t != t) break;
+        }
+        const double Px = q_at(q, rP, 0), Py = q_at(q, rP, 1), Pz = q_at(q, rP, 2);
+        const double Qx = q_at(q, rQ, 0), Qy = q_at(q, rQ, 1), Qz = q_at(q, rQ, 2);
+        if (q.c == 0) {
+            Ccd r;
+            r.dist = min_dist;
+            r.P = mk(Px, Py, Pz);
+            r.Q = mk(Qx, Qy, Qz);
+            r.toc = toc;
+            ee_store_at(a, a.out[i], a.thr[i], r);
+        }
     }
 }
 
@@ -917,7 +1122,7 @@ __global__ void k_fill(int n, int32_t* __restrict__ v, int32_t x) {
 
 // Profiling mode: an event pair around a dominant kernel's launch; the
 // elapsed times are collected at the next stream synchronisation.
-int prof_begin(d2g_ctx* ctx, int kind, long long items) {
+int prof_begin(d2g_ctx* ctx, int kind, long long items, cudaStream_t st = nullptr) {
     Engine& E = ctx->eng;
     if (!E.profiling) return -1;
     cudaEvent_t ev[2];
@@ -929,12 +1134,12 @@ int prof_begin(d2g_ctx* ctx, int kind, long long items) {
             return -1;
         }
     }
-    cudaEventRecord(ev[0], ctx->stream);
+    cudaEventRecord(ev[0], st ? st : ctx->stream);
     E.pending.push_back(Engine::Pending{kind, ev[0], ev[1], items});
     return (int)E.pending.size() - 1;
 }
-void prof_end(d2g_ctx* ctx, int idx) {
-    if (idx >= 0) cudaEventRecord(ctx->eng.pending[idx].e1, ctx->stream);
+void prof_end(d2g_ctx* ctx, int idx, cudaStream_t st = nullptr) {
+    if (idx >= 0) cudaEventRecord(ctx->eng.pending[idx].e1, st ? st : ctx->stream);
 }
 // Call only after the stream has been synchronised.
 void prof_collect(d2g_ctx* ctx) {
@@ -953,15 +1158,17 @@ void prof_collect(d2g_ctx* ctx) {
 }
 
 // Exclusive prefix sum of in[0..n) into out[0..n], out[n] = total.
-int scan(d2g_ctx* ctx, const int32_t* in, int32_t* out, int n) {
-    Engine& E = ctx->eng;
-    D2G_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), ctx->stream));
+int scan_on(cudaStream_t st, DBuf<uint8_t>& tmp, const int32_t* in, int32_t* out, int n) {
+    D2G_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), st));
     if (n == 0) return D2G_OK;
     size_t bytes = 0;
-    D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out + 1, n, ctx->stream));
-    if (int rc = E.cub_tmp.ensure(bytes + 16)) return rc;
-    D2G_CUDA(cub::DeviceScan::InclusiveSum(E.cub_tmp.p, bytes, in, out + 1, n, ctx->stream));
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out + 1, n, st));
+    if (int rc = tmp.ensure(bytes + 16)) return rc;
+    D2G_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, bytes, in, out + 1, n, st));
     return D2G_OK;
+}
+int scan(d2g_ctx* ctx, const int32_t* in, int32_t* out, int n) {
+    return scan_on(ctx->stream, ctx->eng.cub_tmp, in, out, n);
 }
 
 // Read k device int32 scalars (after the stream's pending work).
@@ -1050,6 +1257,21 @@ void emit_records(d2g_ctx* ctx, int n, const int32_t* flags, const int32_t* off,
            E.rec.p, E.rec_pair.p, base);
 }
 
+// Grid of k_ee_rest4: it reads its list size from device memory, so the grid
+// is fixed (every block resident, grid-stride; the first quads take the
+// tests, so a short list occupies the first blocks, one warp per SMSP).
+int ee_grid_size(d2g_ctx* ctx, int* grid) {
+    Engine& E = ctx->eng;
+    if (E.ee_grid == 0) {
+        int dev_sms = 0, per_sm = 0;
+        D2G_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+        D2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ee_rest4, kBlock, 0));
+        E.ee_grid = std::max(1, dev_sms * std::max(1, per_sm));
+    }
+    *grid = E.ee_grid;
+    return D2G_OK;
+}
+
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters) {
     Engine& E = ctx->eng;
@@ -1059,6 +1281,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     RC(E.pfut.ensure(28 * (size_t)n_pairs + 1));
     RC(E.search.ensure(n_pairs + 1));
     RC(E.soup.ensure(n_pairs + 1));
+    int ee_grid = 0;
+    RC(ee_grid_size(ctx, &ee_grid));
     int n_rec = 0;
     if (n_pairs > 0)
         LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
@@ -1080,7 +1304,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         if (n_soup > 0) {
             D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
             const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
-            LAUNCH(k_soup_filter, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
+            LAUNCH(k_soup_filter, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
                    ctx->geo_eps.p, E.flags.p);
             prof_end(ctx, pff);
         }
@@ -1091,6 +1315,11 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         const int32_t* src1[2] = {E.flag_off.p + n_slots, E.nn_off.p + n_conn};
         RC(read_scalars(ctx, src1, 2, tot1));
         const int K = tot1[0], P = tot1[1];  // soup triangle pairs, leaf-pair triangle pairs
+        if (15LL * K + 15LL * P > (long long)INT32_MAX) {  // test indices are 32-bit
+            set_error("CCD level with " + std::to_string(K) + " + " + std::to_string(P) +
+                      " triangle pairs exceeds the 32-bit test index range");
+            return D2G_ERR_INVALID;
+        }
         c_tri += (int64_t)K + 15 * (int64_t)P;
         // (2) all primitive tests of the level
         RC(E.items.ensure(K + 1));
@@ -1122,6 +1351,52 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             if (level_pm32 == 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);
             level_pm32 = 1;
         }
+        if (n_ee > 0) {
+            RC(E.ee_rec.ensure((size_t)kEeRec * n_ee));
+            RC(E.ee_out.ensure(n_ee));
+            RC(E.ee_thr.ensure(n_ee));
+            RC(E.ee_count.ensure(1));
+        }
+        // The point-triangle and edge-edge chains touch disjoint outputs: the
+        // edge-edge chain runs on the second stream beside the other.
+        const bool fork = n_pt > 0 && n_ee > 0;
+        cudaStream_t s_ee = fork ? ctx->stream2 : s;
+        if (fork) {
+            D2G_CUDA(cudaEventRecord(ctx->ev_fork, s));
+            D2G_CUDA(cudaStreamWaitEvent(s_ee, ctx->ev_fork, 0));
+        }
+        if (n_ee > 0) {
+            k_ccd_mask_ee<<<nblocks(n_ee), kBlock, 0, s_ee>>>(K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p,
+                                                            n_conn, E.pm32c.p, ctx->ntris.p, ctx->tri32.p,
+                                                            E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee,
+                                                            cnt_ee, E.fp32_bounds ? 1 : 0);
+            RC(scan_on(s_ee, fork ? E.cub_tmp2 : E.cub_tmp, cnt_ee, off_ee, w_ee));
+            k_np_items<<<nblocks(n_ee), kBlock, 0, s_ee>>>(n_ee, mask_ee, off_ee, list_ee);
+            const int pf = prof_begin(ctx, PROF_CONN, n_ee, s_ee);
+            EeArgs ea;
+            ea.n_tp = K;
+            ea.n_conn = n_conn;
+            ea.items = E.items.p;
+            ea.soup = E.soup.p;
+            ea.conn = E.conn.p;
+            ea.nn_off = E.nn_off.p;
+            ea.ntris = ctx->ntris.p;
+            ea.search = E.search.p;
+            ea.sub = E.sub.p;
+            ea.cres = E.cres.p;
+            ea.chit = E.chit.p;
+            ea.rec = E.ee_rec.p;
+            ea.out = E.ee_out.p;
+            ea.thr = E.ee_thr.p;
+            ea.count = E.ee_count.p;
+            D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
+            k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, off_ee + w_ee, E.pm.p,
+                                                                          ctx->tris.p, ea);
+            k_ee_rest4<<<ee_grid, kBlock, 0, s_ee>>>(ea);
+            ctx->eng.launches += 2;
+            prof_end(ctx, pf, s_ee);
+            ctx->eng.launches += 2;  // mask, items
+        }
         if (n_pt > 0) {
             LAUNCH(k_ccd_mask_pt, n_pt, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
                    ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_pt, cnt_pt,
@@ -1133,16 +1408,9 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
                     ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_pt, off_pt + w_pt);
             prof_end(ctx, pf);
         }
-        if (n_ee > 0) {
-            LAUNCH(k_ccd_mask_ee, n_ee, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
-                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee, cnt_ee,
-                   E.fp32_bounds ? 1 : 0);
-            RC(scan(ctx, cnt_ee, off_ee, w_ee));
-            LAUNCH(k_np_items, n_ee, n_ee, mask_ee, off_ee, list_ee);
-            const int pf = prof_begin(ctx, PROF_CONN, n_ee);
-            LAUNCHB(k_prim_ee, n_ee, kPrimBlock, K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
-                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_ee, off_ee + w_ee);
-            prof_end(ctx, pf);
+        if (fork) {
+            D2G_CUDA(cudaEventRecord(ctx->ev_join, s_ee));
+            D2G_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
         }
         // (3) soup fold and finals, leaf-pair finals, expansion; one synchronisation
         if (K > 0) {

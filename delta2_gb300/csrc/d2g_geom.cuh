@@ -599,67 +599,86 @@ D2G_HD void ee_newton_terms(const Edge& aS, const Edge& aE, const Edge& bS, cons
     t_diff2 = GH / sS + ((-gf) * gf) / m_pow15(S);
 }
 
+// The pieces of collision_detection/continuous_comparison.h:565-673
+// edgeEdgeCCD, shared by edge_edge_ccd below and the phased kernels.
+// Coplanarity triple product of two edges (:570-573).
+D2G_HD double ee_coplanarity(const Edge& a, const Edge& b) {
+    const V3 n = cross(a.B - a.A, b.A - a.A);
+    return dot(b.B - a.A, n);
+}
+
+// The bisection on a sign change of the triple product (:574-607): 20 halvings,
+// then the closest points at the middle time.  Returns the distance.
+D2G_HD double ee_bisect(const Edge& aS, const Edge& aE, const Edge& bS, const Edge& bE, double dot_start, Ccd& r) {
+    double t_lower = 0.0, t_upper = 1.0;
+    for (int iter = 0; iter < 20; iter++) {
+        const double t_mid = (t_lower + t_upper) / 2.0;
+        const V3 atA = lerp(aS.A, aE.A, t_mid), atB = lerp(aS.B, aE.B, t_mid);
+        const V3 btA = lerp(bS.A, bE.A, t_mid), btB = lerp(bS.B, bE.B, t_mid);
+        const V3 n_mid = cross(atB - atA, btA - atA);
+        const double dot_mid = dot(btB - atA, n_mid);
+        if (fabs(dot_mid) < 1e-8) {
+            t_lower = t_mid;
+            t_upper = t_mid;
+            break;
+        } else if (dot_start * dot_mid < 0.0) {
+            t_upper = t_mid;
+        } else {
+            t_lower = t_mid;
+        }
+    }
+    const double t_mid = (t_lower + t_upper) / 2.0;
+    const V3 atA = lerp(aS.A, aE.A, t_mid), atB = lerp(aS.B, aE.B, t_mid);
+    const V3 btA = lerp(bS.A, bE.A, t_mid), btB = lerp(bS.B, bE.B, t_mid);
+    const double d = edge_closest(atA, atB, btA, btB, r.P, r.Q);
+    r.toc = t_mid;
+    return d;
+}
+
+// One Newton iteration from time t (:609-637): the closest points at t update
+// the best (min_dist, r), then t moves by -f'/f'' and is clamped to [0, 1].
+// Returns true when the iteration loop ends here: each iteration is a
+// function of t alone, so once t repeats (or is NaN) the remaining iterations
+// recompute the same distance, which cannot lower min_dist, and stopping
+// gives the same result.
+D2G_HD bool ee_newton_iter(const Edge& aS, const Edge& aE, const Edge& bS, const Edge& bE, double& t,
+                           double& min_dist, Ccd& r) {
+    const V3 atA = lerp(aS.A, aE.A, t), atB = lerp(aS.B, aE.B, t);
+    const V3 btA = lerp(bS.A, bE.A, t), btB = lerp(bS.B, bE.B, t);
+    V3 P, Q;
+    const double dist = edge_closest(atA, atB, btA, btB, P, Q);
+    if (dist < min_dist) {
+        min_dist = dist;
+        r.P = P;
+        r.Q = Q;
+        r.toc = t;
+    }
+    const double pa = edge_project(atA, atB, P);
+    const double pb = edge_project(btA, btB, Q);
+    double td, td2;
+    ee_newton_terms(aS, aE, bS, bE, pa, pb, t, td, td2);
+    const double t_prev = t;
+    t = t - td / td2;
+    t = clamp01(t);
+    return t == t_prev || t != t;
+}
+
+constexpr int kEeNewtonIters = 10;
+
 // collision_detection/continuous_comparison.h:565-673 edgeEdgeCCD.
-// iters_out (optional) receives the number of bisection + Newton iterations.
 D2G_HD Ccd edge_edge_ccd(const Edge& aS, const Edge& aE, const Edge& bS, const Edge& bE) {
     Ccd r;
     r.P = mk(0, 0, 0);
     r.Q = mk(0, 0, 0);
     r.toc = 0.0;
     double min_dist = DBL_MAX;
-    const V3 n_start = cross(aS.B - aS.A, bS.A - aS.A);
-    const double dot_start = dot(bS.B - aS.A, n_start);
-    const V3 n_end = cross(aE.B - aE.A, bE.A - aE.A);
-    const double dot_end = dot(bE.B - aE.A, n_end);
-    if (dot_start * dot_end < 0.0) {
-        double t_lower = 0.0, t_upper = 1.0;
-        for (int iter = 0; iter < 20; iter++) {
-            const double t_mid = (t_lower + t_upper) / 2.0;
-            const V3 atA = lerp(aS.A, aE.A, t_mid), atB = lerp(aS.B, aE.B, t_mid);
-            const V3 btA = lerp(bS.A, bE.A, t_mid), btB = lerp(bS.B, bE.B, t_mid);
-            const V3 n_mid = cross(atB - atA, btA - atA);
-            const double dot_mid = dot(btB - atA, n_mid);
-            if (fabs(dot_mid) < 1e-8) {
-                t_lower = t_mid;
-                t_upper = t_mid;
-                break;
-            } else if (dot_start * dot_mid < 0.0) {
-                t_upper = t_mid;
-            } else {
-                t_lower = t_mid;
-            }
-        }
-        const double t_mid = (t_lower + t_upper) / 2.0;
-        const V3 atA = lerp(aS.A, aE.A, t_mid), atB = lerp(aS.B, aE.B, t_mid);
-        const V3 btA = lerp(bS.A, bE.A, t_mid), btB = lerp(bS.B, bE.B, t_mid);
-        min_dist = edge_closest(atA, atB, btA, btB, r.P, r.Q);
-        r.toc = t_mid;
-    }
+    const double dot_start = ee_coplanarity(aS, bS);
+    const double dot_end = ee_coplanarity(aE, bE);
+    if (dot_start * dot_end < 0.0) min_dist = ee_bisect(aS, aE, bS, bE, dot_start, r);
     if (min_dist > 1e-8) {
         double t = 0.0;
-        for (int iter = 0; iter < 10; iter++) {
-            const V3 atA = lerp(aS.A, aE.A, t), atB = lerp(aS.B, aE.B, t);
-            const V3 btA = lerp(bS.A, bE.A, t), btB = lerp(bS.B, bE.B, t);
-            V3 P, Q;
-            const double dist = edge_closest(atA, atB, btA, btB, P, Q);
-            if (dist < min_dist) {
-                min_dist = dist;
-                r.P = P;
-                r.Q = Q;
-                r.toc = t;
-            }
-            const double pa = edge_project(atA, atB, P);
-            const double pb = edge_project(btA, btB, Q);
-            double td, td2;
-            ee_newton_terms(aS, aE, bS, bE, pa, pb, t, td, td2);
-            const double t_prev = t;
-            t = t - td / td2;
-            t = clamp01(t);
-            // Each iteration is a function of t alone: once t repeats (or is
-            // NaN) the remaining iterations recompute the same distance, which
-            // cannot lower min_dist, so stopping gives the same result.
-            if (t == t_prev || t != t) break;
-        }
+        for (int iter = 0; iter < kEeNewtonIters; iter++)
+            if (ee_newton_iter(aS, aE, bS, bE, t, min_dist, r)) break;
     }
     r.dist = min_dist;
     return r;

@@ -177,7 +177,13 @@ struct Engine {
     DBuf<int32_t> rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted, out_off, pair_cnt;
     DBuf<int32_t> d_pairs;
     DBuf<double> d_max_time;
-    DBuf<uint8_t> cub_tmp;
+    DBuf<uint8_t> cub_tmp, cub_tmp2;
+    // phased edge-edge CCD (d2g_engine.cu)
+    DBuf<double> ee_rec;
+    DBuf<int32_t> ee_out, ee_count;
+    DBuf<float> ee_thr;
+    int ee_grid = 0;  // k_ee_rest4 grid (every block resident)
+  // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing
     long long launches = 0;
@@ -200,6 +206,10 @@ struct Engine {
 struct d2g_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a second stream for independent work within a call (forked from and
+    // joined back into `stream` by the two events)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // trees
     int n_meshes = 0, n_nodes = 0;
     d2g::DBuf<int32_t> mesh_node_off, ntris;

@@ -4,11 +4,13 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <deque>
 #include <limits>
 #include <map>
 #include <set>
+#include <thread>
 #include <tuple>
 #include <utility>
 
@@ -423,6 +425,20 @@ Mesh make_plane(double width) {
     return m;
 }
 
+// A box open at the top: floor [-w/2, w/2]^2 at z = 0 and four walls of
+// height h, ten triangles wound so that their normals face the inside.
+Mesh make_open_box(double w, double h) {
+    Mesh m;
+    const double a = w / 2.0;
+    m.V = {-a, -a, 0.0, a, -a, 0.0, a, a, 0.0, -a, a, 0.0, -a, -a, h, a, -a, h, a, a, h, -a, a, h};
+    m.F = {0, 1, 2, 0, 2, 3,   // floor (+z)
+           0, 5, 1, 0, 4, 5,   // y = -a (+y)
+           1, 6, 2, 1, 5, 6,   // x = +a (-x)
+           2, 7, 3, 2, 6, 7,   // y = +a (-y)
+           3, 4, 0, 3, 7, 4};  // x = -a (+x)
+    return m;
+}
+
 Mesh make_icosphere(int subdiv, double radius, double noise, Pcg32* rng) {
     const double t = (1.0 + std::sqrt(5.0)) / 2.0;
     std::vector<P3> V = {{-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0}, {0, -1, t}, {0, 1, t},
@@ -685,6 +701,10 @@ bool build_tree(const Mesh& m, Pcg32& rng, Tree& out, std::string* err) {
 int scene_add_mesh(Scene& s, const Mesh& m, Pcg32& tree_rng, std::string* err) {
     Tree t;
     if (!build_tree(m, tree_rng, t, err)) return -1;
+    return scene_add_tree(s, t, m.nf());
+}
+
+int scene_add_tree(Scene& s, const Tree& t, int n_faces) {
     if (s.mesh_node_off.empty()) s.mesh_node_off.push_back(0);
     const int base = s.mesh_node_off.back();
     for (int i = 0; i < t.n(); i++) {
@@ -699,8 +719,41 @@ int scene_add_mesh(Scene& s, const Mesh& m, Pcg32& tree_rng, std::string* err) {
     s.eps.insert(s.eps.end(), t.eps.begin(), t.eps.end());
     s.inner_eps.insert(s.inner_eps.end(), t.inner_eps.begin(), t.inner_eps.end());
     s.mesh_node_off.push_back(base + t.n());
-    s.mesh_ntris.push_back(m.nf());
+    s.mesh_ntris.push_back(n_faces);
     return (int)s.mesh_node_off.size() - 2;
+}
+
+// Trees of many meshes on all host cores; mesh k's tree draws from its own
+// PCG32 stream (42, stream0 + k), so the trees do not depend on the order in
+// which the threads build them.
+bool build_trees_parallel(const std::vector<Mesh>& meshes, uint64_t stream0, std::vector<Tree>& out,
+                          std::string* err) {
+    const int n = (int)meshes.size();
+    out.assign(n, Tree());
+    std::vector<std::string> errs(n);
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto work = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= n || failed.load()) break;
+            Pcg32 r;
+            r.seed(42u, stream0 + (uint64_t)k);
+            if (!build_tree(meshes[k], r, out[k], &errs[k])) failed.store(true);
+        }
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = (int)std::max(1u, std::min(64u, std::min(hw ? hw : 1u, (unsigned)std::max(n, 1))));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nt; i++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    for (int k = 0; k < n; k++)
+        if (!errs[k].empty()) {
+            if (err) *err = errs[k];
+            return false;
+        }
+    return !failed.load();
 }
 
 namespace {
@@ -811,13 +864,27 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
     s.opt_dt = dt;
     s.gravity_z = o.gravity_z;
 
-    // Ground plane: static, surface mass model (model/mesh.cpp:93-130).
-    Mesh g = make_plane(ground_w);
-    const MassProps gmp = mass_surface(g, 0.01);
-    const int gm = scene_add_mesh(s, g, tree_rng, err);
-    if (gm < 0) return false;
+    // Ground plane: static, surface mass model (model/mesh.cpp:93-130).  The
+    // noisy-icosphere configuration pours its bodies into a static open box
+    // (40 x 40 m floor, 20 m walls) instead, centred at its centre of mass
+    // like every other mesh.
     const double zero3[3] = {0, 0, 0}, ident[4] = {1, 0, 0, 0};
-    add_body(s, gm, g, gmp, true, density, geo_eps, mu, zero3, ident, zero3, dt);
+    {
+        Mesh g = o.config == 5 ? make_open_box(40.0, 20.0) : make_plane(ground_w);
+        MassProps gmp = mass_surface(g, 0.01);
+        double at[3] = {0, 0, 0};
+        if (o.config == 5) {
+            for (int k = 0; k < 3; k++) at[k] = gmp.com[k];
+            shift_vertices(g, gmp.com);
+            gmp.com[0] = gmp.com[1] = gmp.com[2] = 0.0;
+        }
+        const int gm = scene_add_mesh(s, g, tree_rng, err);
+        if (gm < 0) return false;
+        add_body(s, gm, g, gmp, true, density, geo_eps, mu, at, ident, zero3, dt);
+    }
+    // noisy icospheres: every body has its own mesh; the trees are built
+    // afterwards on all host cores (mesh ids follow the box's)
+    std::vector<Mesh> pending;
 
     int shared_mesh = -1;
     Mesh shared;
@@ -864,8 +931,13 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
                         mp = mass_volume(m);
                         shift_vertices(m, mp.com);
                         mp.com[0] = mp.com[1] = mp.com[2] = 0.0;
-                        mesh_id = scene_add_mesh(s, m, tree_rng, err);
-                        if (mesh_id < 0) return false;
+                        if (o.config == 5) {
+                            mesh_id = 1 + (int)pending.size();
+                            pending.push_back(m);
+                        } else {
+                            mesh_id = scene_add_mesh(s, m, tree_rng, err);
+                            if (mesh_id < 0) return false;
+                        }
                         if (o.config == 3) {
                             mix_mesh[slot] = mesh_id;
                             mix_geom[slot] = m;
@@ -890,6 +962,15 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
                 for (int k = 0; k < 3; k++) v[k] = sigma * normal(rng);
                 add_body(s, mesh_id, m, mp, false, density, geo_eps, mu, x, q, v, dt);
             }
+    if (!pending.empty()) {
+        std::vector<Tree> trees;
+        if (!build_trees_parallel(pending, 55u, trees, err)) return false;
+        for (size_t k = 0; k < trees.size(); k++)
+            if (scene_add_tree(s, trees[k], pending[k].nf()) != (int)k + 1) {
+                if (err) *err = "mesh numbering";
+                return false;
+            }
+    }
     return true;
 }
 

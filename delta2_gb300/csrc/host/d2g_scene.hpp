@@ -31,6 +31,7 @@ struct Mesh {
 
 Mesh make_cube(double half_extent);         // common/primitive_geo.cpp:6-31 scaled by half_extent
 Mesh make_plane(double width);              // common/primitive_geo.cpp:76-89
+Mesh make_open_box(double w, double h);     // floor w x w at z = 0, walls of height h, open top
 Mesh make_icosphere(int subdiv, double radius, double noise, Pcg32* rng);
 Mesh make_hull(int npts, double radius, Pcg32& rng);  // convex hull of points uniform in a ball
 
@@ -73,7 +74,7 @@ struct Scene {
 };
 
 struct SceneOpts {
-    int config = 1;          // 1: cubes, 2: convex hulls, 3: mixed shapes, 5: noisy icospheres
+    int config = 1;          // 1: cubes, 2: convex hulls, 3: mixed shapes, 5: noisy icospheres in an open box
     int nx = 0, ny = 0, nz = 0;
     double spacing = 0;
     double speed_sigma = -1;  // per-axis initial velocity std-dev
@@ -88,5 +89,7 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err);
 
 // Adds one mesh (tree built with rng) and returns its mesh id.
 int scene_add_mesh(Scene& s, const Mesh& m, Pcg32& tree_rng, std::string* err);
+// Adds a built tree of a mesh with n_faces triangles; returns its mesh id.
+int scene_add_tree(Scene& s, const Tree& t, int n_faces);
 
 }  // namespace d2g

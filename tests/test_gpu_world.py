@@ -170,6 +170,22 @@ def test_fp32_bounds_do_not_change_results(ctx):
     assert len(out[True][0]) > 0 and len(out[True][3]) > 0
 
 
+def test_world_noisy_icospheres_in_open_box(ctx):
+    # The noisy-icosphere configuration at small size: four non-convex bodies
+    # (icospheres of 1,280 triangles with radial noise) in the static open
+    # box; two start beside opposite walls moving towards them, two beside
+    # each other, all just above the floor.
+    s = D.make_scene(5, nx=2, ny=2, nz=1)
+    assert s.n_bodies == 5 and s.is_static[0] == 1 and s.ntris[s.mesh_node_off[1]:].max() <= 8
+    br = s.bounding_radius
+    s.cur[1, 8], s.cur[1, 11] = -20.0 + br[1] + 0.05, -0.5
+    s.cur[2, 8], s.cur[2, 11] = 20.0 - br[2] - 0.05, 0.5
+    st = run_world(ctx, s, 60)
+    assert st["np_contacts"] > 0
+    got = ctx.get_bodies(s.copy())
+    assert np.isfinite(got.cur).all()
+
+
 def test_world_cube_pile_grid_solve(ctx):
     # the 64-cube configuration: one cluster whose contacts grow past the
     # threshold where the solve runs as a cooperative grid over the SMs
