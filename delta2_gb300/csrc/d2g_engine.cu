@@ -38,28 +38,48 @@ __device__ __forceinline__ int4 ld_node(const int4* nodes, int g) { return nodes
 // ------------------------------------------------------------- CCD prep ----
 // Projects both futures over the pair's max_time (model/state.cpp:90-102,
 // full_tree_comparison.h:78-79) and forms the pose matrices.
+// Per pair: the futures over max_time, the pose matrices (pair_mats) and the
+// root frontier entry.  Four lanes per pair: lanes 1 and 3 extrapolate a and
+// b, lane k forms transform k (a start, a end, b start, b end) and then the
+// product inverse(transform k^2) * transform k, so the four 4x4 inverses and
+// products run side by side.
 __global__ void k_ccd_prep(int n, const int32_t* __restrict__ pairs, const double* __restrict__ max_time,
                            const double* __restrict__ cur, const double* __restrict__ ii,
                            const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
                            const double* __restrict__ geo_eps, double* __restrict__ pm, double* __restrict__ pfut,
                            float* __restrict__ search, Entry* __restrict__ soup) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const int a = pairs[2 * p], b = pairs[2 * p + 1];
-    const double mt = max_time[p];
-    const State ca = load_state(cur + 14 * (size_t)a);
-    const State cb = load_state(cur + 14 * (size_t)b);
-    const State fa = extrapolate(ca, mt, ii + 9 * (size_t)a);
-    const State fb = extrapolate(cb, mt, ii + 9 * (size_t)b);
-    pair_mats(ca, fa, cb, fb, pm + (size_t)PM_SIZE * p);
-    store_state(pfut + 28 * (size_t)p, fa);
-    store_state(pfut + 28 * (size_t)p + 14, fb);
-    search[p] = (float)(geo_eps[a] + geo_eps[b]);
-    Entry e;
-    e.pair = p;
-    e.na = mesh_node_off[mesh[a]];
-    e.nb = mesh_node_off[mesh[b]];
-    soup[p] = e;
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 2);
+    const int k = threadIdx.x & 3;
+    if (p >= n) return;  // uniform per quad
+    const unsigned qm = 0xFu << (threadIdx.x & 28);
+    const int body = pairs[2 * p + (k >> 1)];
+    const State c = load_state(cur + 14 * (size_t)body);
+    State st = c;
+    if (k & 1) {
+        st = extrapolate(c, max_time[p], ii + 9 * (size_t)body);
+        store_state(pfut + 28 * (size_t)p + 14 * (k >> 1), st);
+    }
+    double* M = pm + (size_t)PM_SIZE * p;
+    double T[16], O[16], inv[16], R[16];
+    transformation(st.q, st.x, T);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        M[16 * k + i] = T[i];
+        O[i] = __shfl_xor_sync(qm, T[i], 2);
+    }
+    mat_inverse(O, inv);
+    mat_mul(inv, T, R);
+#pragma unroll
+    for (int i = 0; i < 16; i++) M[PM_ABS + 16 * k + i] = R[i];
+    if (k == 0) {
+        const int a = pairs[2 * p], b = pairs[2 * p + 1];
+        search[p] = (float)(geo_eps[a] + geo_eps[b]);
+        Entry e;
+        e.pair = p;
+        e.na = mesh_node_off[mesh[a]];
+        e.nb = mesh_node_off[mesh[b]];
+        soup[p] = e;
+    }
 }
 
 // Discrete narrow phase prep: future transforms of a and b (comparison_dist.h:225,229).
@@ -1158,9 +1178,80 @@ void prof_collect(d2g_ctx* ctx) {
 }
 
 // Exclusive prefix sum of in[0..n) into out[0..n], out[n] = total.
+// Exclusive prefix sums of up to two small int32 arrays in one launch, one
+// 1024-thread block per array: out[0..n] with out[n] = total.  The array is
+// staged in shared memory in chunks of kScanChunk (coalesced), each thread
+// sums its kScanPer contiguous elements, and a shuffle scan over the thread
+// sums gives every thread its offset.
+constexpr int kScanThreads = 1024, kScanPer = 8, kScanChunk = kScanThreads * kScanPer;
+static_assert(kScanThreads == 32 * 32, "the warp-sum scan assumes 32 warps");
+constexpr int kScanOneBlock = 4 * kScanChunk;  // larger arrays go to cub
+struct ScanSeg {
+    const int32_t* in[2];
+    int32_t* out[2];
+    int n[2];
+};
+__global__ void __launch_bounds__(kScanThreads) k_scan1(ScanSeg sg) {
+    __shared__ int32_t buf[kScanChunk];
+    __shared__ int32_t wsum[32];
+    const int32_t* in = sg.in[blockIdx.x];
+    int32_t* out = sg.out[blockIdx.x];
+    const int n = sg.n[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    int carry = 0;
+    for (int base = 0; base < n; base += kScanChunk) {
+        const int m = min(kScanChunk, n - base);
+        for (int i = tid; i < kScanChunk; i += kScanThreads) buf[i] = i < m ? in[base + i] : 0;
+        __syncthreads();
+        int v[kScanPer], sum = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            v[k] = buf[tid * kScanPer + k];
+            sum += v[k];
+        }
+        int x = sum;  // inclusive warp scan of the thread sums
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int z = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z;  // inclusive over warps
+        }
+        __syncthreads();
+        int run = carry + (w > 0 ? wsum[w - 1] : 0) + (x - sum);
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            buf[tid * kScanPer + k] = run;
+            run += v[k];
+        }
+        const int chunk_total = wsum[31];
+        __syncthreads();
+        for (int i = tid; i < m; i += kScanThreads) out[base + i] = buf[i];
+        carry += chunk_total;
+        __syncthreads();
+    }
+    if (tid == 0) out[n] = carry;
+}
+
 int scan_on(cudaStream_t st, DBuf<uint8_t>& tmp, const int32_t* in, int32_t* out, int n) {
+    if (n <= kScanOneBlock) {
+        ScanSeg sg;
+        sg.in[0] = sg.in[1] = in;
+        sg.out[0] = sg.out[1] = out;
+        sg.n[0] = sg.n[1] = n;
+        k_scan1<<<1, kScanThreads, 0, st>>>(sg);
+        return D2G_OK;
+    }
     D2G_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), st));
-    if (n == 0) return D2G_OK;
     size_t bytes = 0;
     D2G_CUDA(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out + 1, n, st));
     if (int rc = tmp.ensure(bytes + 16)) return rc;
@@ -1169,6 +1260,22 @@ int scan_on(cudaStream_t st, DBuf<uint8_t>& tmp, const int32_t* in, int32_t* out
 }
 int scan(d2g_ctx* ctx, const int32_t* in, int32_t* out, int n) {
     return scan_on(ctx->stream, ctx->eng.cub_tmp, in, out, n);
+}
+// Two independent scans on the context's stream (one launch when both are small).
+int scan2(d2g_ctx* ctx, const int32_t* in0, int32_t* out0, int n0, const int32_t* in1, int32_t* out1, int n1) {
+    if (n0 <= kScanOneBlock && n1 <= kScanOneBlock) {
+        ScanSeg sg;
+        sg.in[0] = in0;
+        sg.out[0] = out0;
+        sg.n[0] = n0;
+        sg.in[1] = in1;
+        sg.out[1] = out1;
+        sg.n[1] = n1;
+        k_scan1<<<2, kScanThreads, 0, ctx->stream>>>(sg);
+        return D2G_OK;
+    }
+    if (int rc = scan(ctx, in0, out0, n0)) return rc;
+    return scan(ctx, in1, out1, n1);
 }
 
 // Read k device int32 scalars (after the stream's pending work).
@@ -1285,7 +1392,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     RC(ee_grid_size(ctx, &ee_grid));
     int n_rec = 0;
     if (n_pairs > 0)
-        LAUNCH(k_ccd_prep, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
+        LAUNCH(k_ccd_prep, 4LL * n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
     int n_soup = n_pairs, n_conn = 0;
     int level_pm32 = 0;  // FP32 poses made once per call
@@ -1417,16 +1524,14 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             LAUNCH(k_soup_fold, K, K, E.items.p, E.soup.p, E.sub.p, E.search.p, E.res.p, E.hit.p, E.entry_hits.p);
             LAUNCH(k_final_flags, K, K, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p, E.flags.p);
         }
-        RC(scan(ctx, E.flags.p, E.flag_off.p, K));
-        RC(scan(ctx, E.chit.p, E.cflag_off.p, 15 * P));
+        RC(scan2(ctx, E.flags.p, E.flag_off.p, K, E.chit.p, E.cflag_off.p, 15 * P));
         RC(E.cnt_a.ensure(n_soup + 1));
         RC(E.cnt_b.ensure(n_soup + 1));
         RC(E.off_a.ensure(n_soup + 1));
         RC(E.off_b.ensure(n_soup + 1));
         if (n_soup > 0)
             LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1, E.cnt_a.p, E.cnt_b.p);
-        RC(scan(ctx, E.cnt_a.p, E.off_a.p, n_soup));
-        RC(scan(ctx, E.cnt_b.p, E.off_b.p, n_soup));
+        RC(scan2(ctx, E.cnt_a.p, E.off_a.p, n_soup, E.cnt_b.p, E.off_b.p, n_soup));
         int32_t tot2[4];
         const int32_t* src2[4] = {E.flag_off.p + K, E.cflag_off.p + 15 * P, E.off_a.p + n_soup, E.off_b.p + n_soup};
         RC(read_scalars(ctx, src2, 4, tot2));
