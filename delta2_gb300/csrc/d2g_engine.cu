@@ -822,10 +822,12 @@ __global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entr
 // hit test dist < float(search) + eps_a + eps_b (comparison_dist.h:223-236).
 // Candidate slots of the discrete narrow phase.  A (node pair, ta, tb) slot
 // can only hit (comparison_dist.h:231-233) when the triangles are closer than
-// thr = search + eps_a + eps_b.  Two lower bounds on that distance: the
-// bounding spheres' |c_a - c_b| - r_a - r_b (centroid, radius rounded up) and
-// the gap between the boxes of the transformed triangles.  The larger is
-// evaluated in FP32 and a slot is dropped only when it exceeds thr by a margin
+// thr = search + eps_a + eps_b.  Lower bounds on that distance: the bounding
+// spheres' |c_a - c_b| - r_a - r_b (centroid, radius rounded up), the gap
+// between the boxes of the transformed triangles and, for slots those keep,
+// the gaps along the eleven separating axes (two face normals, nine edge-edge
+// cross products).  The largest is evaluated in FP32 and a slot is dropped
+// only when it exceeds thr by a margin
 // (1 mm plus 4e-6 of the magnitudes involved) far above the FP32 rounding of
 // the bound and the FP64 rounding of the exact test, so every slot that hits
 // survives.  Dropped slots produce nothing in the reference
@@ -862,26 +864,69 @@ __global__ void __launch_bounds__(kBlock) k_np_mask(int n_slots, const Entry* __
             // the gap between the transformed triangles' boxes is a second lower bound
             const float* va = tri32 + ((size_t)e.na * 8 + ta) * 9;
             const float* vb = tri32 + ((size_t)e.nb * 8 + tb) * 9;
+            float wa[3][3], wb[3][3];  // [vertex][axis]
+#pragma unroll
+            for (int v = 0; v < 3; v++)
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+                    wa[v][r] = A[4 * r] * va[3 * v] + A[4 * r + 1] * va[3 * v + 1] + A[4 * r + 2] * va[3 * v + 2] +
+                               A[4 * r + 3];
+                    wb[v][r] = B[4 * r] * vb[3 * v] + B[4 * r + 1] * vb[3 * v + 1] + B[4 * r + 2] * vb[3 * v + 2] +
+                               B[4 * r + 3];
+                }
             float gap2 = 0.f;
 #pragma unroll
             for (int r = 0; r < 3; r++) {
-                float alo = 3.4e38f, ahi = -3.4e38f, blo = 3.4e38f, bhi = -3.4e38f;
-#pragma unroll
-                for (int v = 0; v < 3; v++) {
-                    const float wa = A[4 * r] * va[3 * v] + A[4 * r + 1] * va[3 * v + 1] + A[4 * r + 2] * va[3 * v + 2] +
-                                     A[4 * r + 3];
-                    const float wb = B[4 * r] * vb[3 * v] + B[4 * r + 1] * vb[3 * v + 1] + B[4 * r + 2] * vb[3 * v + 2] +
-                                     B[4 * r + 3];
-                    alo = fminf(alo, wa);
-                    ahi = fmaxf(ahi, wa);
-                    blo = fminf(blo, wb);
-                    bhi = fmaxf(bhi, wb);
-                }
+                const float alo = fminf(fminf(wa[0][r], wa[1][r]), wa[2][r]);
+                const float ahi = fmaxf(fmaxf(wa[0][r], wa[1][r]), wa[2][r]);
+                const float blo = fminf(fminf(wb[0][r], wb[1][r]), wb[2][r]);
+                const float bhi = fmaxf(fmaxf(wb[0][r], wb[1][r]), wb[2][r]);
                 const float g = fmaxf(blo - ahi, alo - bhi);
                 if (g > 0.f) gap2 += g * g;
             }
             lb = fmaxf(lb, sqrtf(gap2));
-            keep = !use_bounds || !(lb > thr + (1e-3f + 4e-6f * mag));  // NaN keeps the slot
+            const float lim = thr + (1e-3f + 4e-6f * mag);
+            if (!(lb > lim)) {
+                // Separating axes: along any direction n the distance is at
+                // least the gap between the projections divided by |n|,
+                // whatever n is, so n computed in FP32 still bounds; the two
+                // face normals and the nine edge-edge cross products.
+                auto axis_gap = [&](float nx, float ny, float nz) {
+                    const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
+                    if (!(nn > 1e-20f)) return 0.f;
+                    float a0 = 3.4e38f, a1 = -3.4e38f, b0 = 3.4e38f, b1 = -3.4e38f;
+#pragma unroll
+                    for (int v = 0; v < 3; v++) {
+                        const float pa = wa[v][0] * nx + wa[v][1] * ny + wa[v][2] * nz;
+                        const float pb = wb[v][0] * nx + wb[v][1] * ny + wb[v][2] * nz;
+                        a0 = fminf(a0, pa);
+                        a1 = fmaxf(a1, pa);
+                        b0 = fminf(b0, pb);
+                        b1 = fmaxf(b1, pb);
+                    }
+                    return fmaxf(b0 - a1, a0 - b1) / nn;
+                };
+                float ea[3][3], eb[3][3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int r = 0; r < 3; r++) {
+                        ea[k][r] = wa[(k + 1) % 3][r] - wa[k][r];
+                        eb[k][r] = wb[(k + 1) % 3][r] - wb[k][r];
+                    }
+                lb = fmaxf(lb, axis_gap(ea[0][1] * ea[1][2] - ea[0][2] * ea[1][1], ea[0][2] * ea[1][0] - ea[0][0] * ea[1][2],
+                                        ea[0][0] * ea[1][1] - ea[0][1] * ea[1][0]));
+                lb = fmaxf(lb, axis_gap(eb[0][1] * eb[1][2] - eb[0][2] * eb[1][1], eb[0][2] * eb[1][0] - eb[0][0] * eb[1][2],
+                                        eb[0][0] * eb[1][1] - eb[0][1] * eb[1][0]));
+#pragma unroll
+                for (int x = 0; x < 3; x++)
+#pragma unroll
+                    for (int y = 0; y < 3; y++)
+                        lb = fmaxf(lb, axis_gap(ea[x][1] * eb[y][2] - ea[x][2] * eb[y][1],
+                                                ea[x][2] * eb[y][0] - ea[x][0] * eb[y][2],
+                                                ea[x][0] * eb[y][1] - ea[x][1] * eb[y][0]));
+            }
+            keep = !use_bounds || !(lb > lim);  // NaN keeps the slot
         }
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
