@@ -1338,27 +1338,6 @@ int read_scalars(d2g_ctx* ctx, const int32_t* const* src, int k, int32_t* dst) {
         if (int rc_ = (x)) return rc_; \
     } while (0)
 
-// Append the flagged results of a stage to the record buffer.
-int append_records(d2g_ctx* ctx, int n, const int32_t* flags, const int32_t* items, int slot_shift,
-                   const Entry* front, const int32_t* conn_off, int n_conn, const int32_t* d_pairs,
-                   const double* res_eps, int& n_rec) {
-    Engine& E = ctx->eng;
-    RC(E.flag_off.ensure(n + 1));
-    RC(scan(ctx, flags, E.flag_off.p, n));
-    int32_t tot;
-    const int32_t* src = E.flag_off.p + n;
-    RC(read_scalars(ctx, &src, 1, &tot));
-    if (tot == 0) return D2G_OK;
-    // records accumulate across levels and stages: grow without losing them
-    RC(E.rec.ensure_keep(14 * (size_t)(n_rec + tot), 14 * (size_t)n_rec, ctx->stream));
-    RC(E.rec_pair.ensure_keep((size_t)(n_rec + tot), (size_t)n_rec, ctx->stream));
-    LAUNCH(k_emit, n, n, flags, E.flag_off.p, items, slot_shift, front, conn_off, n_conn,
-                                                   d_pairs, E.res.p, res_eps, ctx->geo_eps.p, E.rec.p,
-                                                   E.rec_pair.p, n_rec);
-    n_rec += tot;
-    return D2G_OK;
-}
-
 // Sort records by pair (stable) into rec_sorted and write offsets [n_pairs+1].
 int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
     Engine& E = ctx->eng;
@@ -1654,14 +1633,28 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
                E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p, E.fp32_bounds ? 1 : 0);
         RC(scan(ctx, E.np_cnt.p, E.np_off.p, n_words));
         LAUNCH(k_np_items, n_slots, n_slots, E.np_mask.p, E.np_off.p, E.items.p);
-        const int pf = prof_begin(ctx, PROF_NP, n_slots);
-        LAUNCH(k_np, n_slots, n_slots, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
-                                                 ctx->eps.p, ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p,
-                                                 res_eps.p, E.hit.p, E.entry_hits.p, E.items.p, E.np_off.p + n_words);
-        prof_end(ctx, pf);
-        LAUNCH(k_final_flags, n_slots, n_slots, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p,
-                                                          E.flags.p);
-        RC(append_records(ctx, n_slots, E.flags.p, E.items.p, 6, E.soup.p, nullptr, 0, d_pairs, res_eps.p, n_rec));
+        // the survivors' count sizes every later kernel of the level
+        int32_t n_items = 0;
+        {
+            const int32_t* src = E.np_off.p + n_words;
+            RC(read_scalars(ctx, &src, 1, &n_items));
+        }
+        if (n_items > 0) {
+            const int pf = prof_begin(ctx, PROF_NP, n_slots);
+            LAUNCH(k_np, n_items, n_items, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p, ctx->eps.p,
+                   ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p, res_eps.p, E.hit.p, E.entry_hits.p,
+                   E.items.p, (const int32_t*)nullptr);
+            prof_end(ctx, pf);
+            LAUNCH(k_final_flags, n_items, n_items, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p, E.flags.p);
+        }
+        // final contacts: compacted now, counted with the level-end read
+        RC(E.flag_off.ensure(n_items + 1));
+        RC(scan(ctx, E.flags.p, E.flag_off.p, n_items));
+        RC(E.rec.ensure_keep(14 * (size_t)(n_rec + n_items + 1), 14 * (size_t)n_rec, s));
+        RC(E.rec_pair.ensure_keep((size_t)(n_rec + n_items + 1), (size_t)n_rec, s));
+        if (n_items > 0)
+            LAUNCH(k_emit, n_items, n_items, E.flags.p, E.flag_off.p, E.items.p, 6, E.soup.p, (const int32_t*)nullptr,
+                   0, d_pairs, E.res.p, res_eps.p, ctx->geo_eps.p, E.rec.p, E.rec_pair.p, n_rec);
         RC(E.cnt_a.ensure(n));
         RC(E.cnt_b.ensure(n));
         RC(E.off_a.ensure(n + 1));
@@ -1670,11 +1663,12 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
                                                      E.cnt_b.p);
         RC(scan(ctx, E.cnt_a.p, E.off_a.p, n));
         D2G_CUDA(cudaMemsetAsync(E.off_b.p, 0, sizeof(int32_t) * (n + 1), s));
-        int32_t vals[2];
-        const int32_t* srcs[2] = {E.off_a.p + n, E.np_tri.p};
-        RC(read_scalars(ctx, srcs, 2, vals));
+        int32_t vals[3];
+        const int32_t* srcs[3] = {E.off_a.p + n, E.np_tri.p, E.flag_off.p + n_items};
+        RC(read_scalars(ctx, srcs, 3, vals));
         const int32_t tot = vals[0];
         c_tri = vals[1];
+        n_rec += vals[2];
         RC(E.soup_next.ensure(tot + 1));
         LAUNCH(k_expand_write, n, n, E.soup.p, E.entry_hits.p, ctx->nodes.p, 0, E.off_a.p,
                                                      E.off_b.p, E.soup_next.p, E.conn_next.p);
