@@ -702,7 +702,7 @@ int d2g_solve_clusters(d2g_ctx* c, int32_t n_clusters, const int32_t* particle_o
     RC(E.up_ab.ensure(2 * (size_t)n + 2));
     RC(d2g::run_solve(c, n_clusters, E.up_part_off.p, E.up_parts.p, np, E.up_con_off.p, n, E.up_rec.p, E.up_cnt.p,
                       E.up_warm.p, E.up_step.p, gravity_z, E.up_status.p, E.up_iters.p, E.up_imp.p, E.up_ab.p, nullptr,
-                      nullptr, contact_off));
+                      nullptr, contact_off, particle_off));
     RC(download(c, status, E.up_status, (size_t)n_clusters));
     if (iterations) RC(download(c, iterations, E.up_iters, 2 * (size_t)n_clusters));
     if (impulse_out) RC(download(c, impulse_out, E.up_imp, (size_t)n));

@@ -109,47 +109,6 @@ __global__ void k_np_prep(int n, const int32_t* __restrict__ pairs, const double
 }
 
 // ------------------------------------------------------------ soup stage ---
-// The swept-AABB prefilter of every (triangle of a, triangle of b) slot of a
-// soup node pair (continuous_comparison.h:804-812), one warp per node pair:
-// lanes 0-7 form the swept boxes of a's triangles, lanes 8-15 those of b's,
-// once each, and every lane then tests two of the 64 slots from shuffled
-// boxes.  flags[64 * entry + 8 * ta + tb] = 1 where the boxes overlap.
-__global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
-                              const double* __restrict__ pm, const int32_t* __restrict__ ntris,
-                              const double* __restrict__ tris, const double* __restrict__ geo_eps,
-                              int32_t* __restrict__ flags) {
-    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (w >= n_soup) return;  // uniform per warp
-    const Entry e = soup[w];
-    const int na = ntris[e.na], nb = ntris[e.nb];
-    const bool side_b = lane >= 8;
-    const int t = lane & 7;
-    Box bx;
-#pragma unroll
-    for (int k = 0; k < 3; k++) bx.lo[k] = bx.hi[k] = 0.0;
-    if (lane < 16 && t < (side_b ? nb : na)) {
-        const double* M = pm + (size_t)PM_SIZE * e.pair;
-        const int body = pairs[2 * e.pair + (side_b ? 1 : 0)];
-        const Tri tri = load_tri(tris + (size_t)(side_b ? e.nb : e.na) * 72 + t * 9);
-        bx = side_b ? swept_box(tri, M + PM_BS, M + PM_BE, geo_eps[body])
-                    : swept_box(tri, M + PM_AS, M + PM_AE, geo_eps[body]);
-    }
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
-        Box A, B;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            A.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], ta);
-            A.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], ta);
-            B.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], 8 + tb);
-            B.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], 8 + tb);
-        }
-        flags[64 * (size_t)w + sl] = (ta < na && tb < nb && box_overlap(A, B)) ? 1 : 0;
-    }
-}
-
 __global__ void k_compact(int n, const int32_t* __restrict__ flags, const int32_t* __restrict__ off,
                           int32_t* __restrict__ items) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -269,6 +228,107 @@ __global__ void k_ccd_pm32(int n, const double* __restrict__ pm, float* __restri
     const int p = i / 96, w = (i % 96) / 12, r = i % 12;
     pm32[i] = (float)pm[(size_t)PM_SIZE * p + 16 * w + r];
 }
+
+// The swept-AABB prefilter of every (triangle of a, triangle of b) slot of a
+// soup node pair (continuous_comparison.h:804-812), one warp per node pair:
+// lanes 0-7 form the swept boxes of a's triangles, lanes 8-15 those of b's,
+// once each, and every lane then tests two of the 64 slots from shuffled
+// boxes.  flags[64 * entry + 8 * ta + tb] = 1 where the boxes overlap.  The
+// boxes are first formed in FP32 (FP32 poses and triangles): a slot whose
+// boxes are apart, or overlap, by more than a margin (1e-4 m plus 4e-6 of the
+// largest coordinate, far above the FP32 rounding of the box edges) has the
+// answer the FP64 boxes give; a warp with any slot inside the margin (or a
+// NaN) forms the FP64 boxes and decides those slots exactly.
+__global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
+                              const double* __restrict__ pm, const float* __restrict__ pm32,
+                              const int32_t* __restrict__ ntris, const double* __restrict__ tris,
+                              const float* __restrict__ tri32, const double* __restrict__ geo_eps,
+                              int32_t* __restrict__ flags) {
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_soup) return;  // uniform per warp
+    const Entry e = soup[w];
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    const bool side_b = lane >= 8;
+    const int t = lane & 7;
+    const bool own = lane < 16 && t < (side_b ? nb : na);
+    const int body = pairs[2 * e.pair + (side_b ? 1 : 0)];
+    const int node = side_b ? e.nb : e.na;
+    Box32 b32;
+    box_init(b32);
+    float mag = 0.f;
+    if (own) {
+        const float* tv = tri32 + ((size_t)node * 8 + t) * 9;
+        const float* MS = pm32_of(pm32, e.pair, side_b ? P32_BS : P32_AS);
+        const float* ME = pm32_of(pm32, e.pair, side_b ? P32_BE : P32_AE);
+        float o[3];
+#pragma unroll
+        for (int v = 0; v < 3; v++) {
+            box_add(b32, MS, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+            box_add(b32, ME, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+        }
+        const float e32 = (float)geo_eps[body];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            b32.lo[k] -= e32;
+            b32.hi[k] += e32;
+        }
+        mag += e32;
+    }
+    int res[2];
+    bool border = false;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+        float alo[3], ahi[3], blo[3], bhi[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            alo[k] = __shfl_sync(0xffffffffu, b32.lo[k], ta);
+            ahi[k] = __shfl_sync(0xffffffffu, b32.hi[k], ta);
+            blo[k] = __shfl_sync(0xffffffffu, b32.lo[k], 8 + tb);
+            bhi[k] = __shfl_sync(0xffffffffu, b32.hi[k], 8 + tb);
+        }
+        const float m = 1e-4f + 4e-6f * fmaxf(__shfl_sync(0xffffffffu, mag, ta), __shfl_sync(0xffffffffu, mag, 8 + tb));
+        res[h] = 0;
+        if (ta < na && tb < nb) {
+            bool apart = false, over = true;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                apart = apart || blo[k] > ahi[k] + m || alo[k] > bhi[k] + m;
+                over = over && blo[k] < ahi[k] - m && alo[k] < bhi[k] - m;
+            }
+            res[h] = apart ? 0 : (over ? 1 : 2);
+            border = border || res[h] == 2;
+        }
+    }
+    if (__any_sync(0xffffffffu, border)) {
+        Box bx;
+#pragma unroll
+        for (int k = 0; k < 3; k++) bx.lo[k] = bx.hi[k] = 0.0;
+        if (own) {
+            const double* M = pm + (size_t)PM_SIZE * e.pair;
+            const Tri tri = load_tri(tris + (size_t)node * 72 + t * 9);
+            bx = side_b ? swept_box(tri, M + PM_BS, M + PM_BE, geo_eps[body])
+                        : swept_box(tri, M + PM_AS, M + PM_AE, geo_eps[body]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+            Box A, B;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                A.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], ta);
+                A.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], ta);
+                B.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], 8 + tb);
+                B.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], 8 + tb);
+            }
+            if (res[h] == 2) res[h] = box_overlap(A, B) ? 1 : 0;
+        }
+    }
+    flags[64 * (size_t)w + lane] = res[0];
+    flags[64 * (size_t)w + lane + 32] = res[1];
+}
+
 
 // Point-triangle work item j (the decoding of k_prim_pt): which pair, which
 // point (body-local), which triangle (body-local) and which transforms.
@@ -1419,7 +1479,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         LAUNCH(k_ccd_prep, 4LL * n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
     int n_soup = n_pairs, n_conn = 0;
-    int level_pm32 = 0;  // FP32 poses made once per call
+    RC(E.pm32c.ensure((size_t)96 * n_pairs + 1));
+    if (n_pairs > 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);  // FP32 poses, once per call
     while (n_soup > 0 || n_conn > 0) {
         c_levels++;
         c_node += n_soup + n_conn;
@@ -1435,8 +1496,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         if (n_soup > 0) {
             D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
             const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
-            LAUNCH(k_soup_filter, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, ctx->ntris.p, ctx->tris.p,
-                   ctx->geo_eps.p, E.flags.p);
+            LAUNCH(k_soup_filter, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, E.pm32c.p, ctx->ntris.p,
+                   ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, E.flags.p);
             prof_end(ctx, pff);
         }
         RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
@@ -1477,11 +1538,6 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         int32_t* off_ee = E.ccd_off.p + w_pt + 1;
         int32_t* list_pt = E.ccd_list.p;
         int32_t* list_ee = E.ccd_list.p + n_pt;
-        if (n_pt > 0 || n_ee > 0) {
-            RC(E.pm32c.ensure((size_t)96 * n_pairs + 1));
-            if (level_pm32 == 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);
-            level_pm32 = 1;
-        }
         if (n_ee > 0) {
             RC(E.ee_rec.ensure((size_t)kEeRec * n_ee));
             RC(E.ee_out.ensure(n_ee));

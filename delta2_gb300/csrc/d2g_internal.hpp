@@ -278,5 +278,5 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
               const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
               const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
               double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm,
-              const int32_t* h_con_off = nullptr);
+              const int32_t* h_con_off = nullptr, const int32_t* h_part_off = nullptr);
 }  // namespace d2g

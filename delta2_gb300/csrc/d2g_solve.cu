@@ -30,6 +30,7 @@ constexpr int kBlock = 128;
 constexpr int kSolveBlock = 256;
 constexpr int kGridMinContacts = 128;  // a cluster this large may take a cooperative grid
 constexpr int kGridMaxClusters = 8;    // ... when the call has at most this many clusters
+constexpr int kGridMinParts = 128;     // ... and its waves can be wider than one block takes at once
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -764,7 +765,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
               const int32_t* d_con_off, int n_con, const double* d_rec, const int32_t* d_pair_cnt,
               const double* d_warm, const double* d_step, double gravity_z, int32_t* d_status, int32_t* d_iters,
               double* d_out_impulse, int32_t* d_out_ab, const int32_t* d_con_pair, double* d_pair_warm,
-              const int32_t* h_con_off) {
+              const int32_t* h_con_off, const int32_t* h_part_off) {
     Engine& E = ctx->eng;
     cudaStream_t s = ctx->stream;
     RC(E.sv_scon.ensure(n_con + 1));
@@ -824,11 +825,16 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
         a.con_pair = d_con_pair;
         a.pair_warm = d_pair_warm;
         // A large cluster among few is solved by a cooperative grid over the
-        // SMs; the others one block each.
+        // SMs; the others one block each.  A wave holds at most one contact
+        // per moving body, so a cluster of at most kGridMinParts parts never
+        // has waves much wider than the kSolveBlock / 4 contacts one block
+        // takes at once, and the grid would only add its barriers.
         std::vector<int32_t> small, big;
         for (int c = 0; c < n_clusters; c++) {
             const int nck = h_con_off ? h_con_off[c + 1] - h_con_off[c] : 0;
-            if (h_con_off && n_clusters <= kGridMaxClusters && nck >= kGridMinContacts)
+            const int npc = h_part_off ? h_part_off[c + 1] - h_part_off[c] : 0;
+            if (h_con_off && h_part_off && n_clusters <= kGridMaxClusters && nck >= kGridMinContacts &&
+                npc > kGridMinParts)
                 big.push_back(c);
             else
                 small.push_back(c);

@@ -271,7 +271,7 @@ int pde_round(d2g_ctx* c, WorldState& W, const std::vector<HostCluster>& cls, co
     D2G_CUDA(cudaStreamSynchronize(s));
     RC(run_solve(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), (int)parts.size(), W.con_off.p, n_kept,
                  E.flt.p, W.con_cnt.p, W.con_warm.p, W.step_a.p, W.gravity_z, W.status.p, W.iters.p, W.con_imp.p,
-                 W.con_ab.p, W.con_pair.p, W.pair_warm.p, h_con_off));
+                 W.con_ab.p, W.con_pair.p, W.pair_warm.p, h_con_off, part_off.data()));
     RC(run_pde_finish(c, nA, W.pk_batch.ptr(i_poff), W.pk_batch.ptr(i_parts), W.step_a.p, W.status.p,
                       W.will_sleep.p));
     // results back: status, iterations, will_sleep, kept counts (int); step, pair warm (double)

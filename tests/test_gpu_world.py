@@ -97,12 +97,10 @@ def test_filter_matches_oracle(ctx):
         assert np.array_equal(bits(got), bits(np.asarray(ref).reshape(-1, 14))), p
 
 
-def test_solve_matches_oracle(ctx):
-    # a state with many contacts: the cube scene after 120 oracle steps
-    s = D.make_scene(1, nx=2, ny=2, nz=2)
-    w = O.World(s.copy(), s.opt_dt, s.gravity_z)
-    w.step(120)
-    base = w.get_bodies().copy()
+def solve_against_oracle(ctx, base, s, min_contacts=1):
+    """Solve every cluster of state `base` (contacts from the oracle's narrow
+    phase and filter) on the GPU in one call and with the oracle cluster by
+    cluster; compare statuses, iterations, future states and the warm store."""
     pairs = D.broad_phase(base)
     clusters = separate(pairs, base.is_static, base.n_bodies)
     flat = np.array([p for _, inter in clusters for p in inter], dtype=np.int32).reshape(-1, 2)
@@ -115,7 +113,7 @@ def test_solve_matches_oracle(ctx):
             cl.append(f)
             k += 1
         hits.append(np.concatenate(cl) if cl else np.zeros((0, 14)))
-    assert sum(len(h) for h in hits) > 0
+    assert sum(len(h) for h in hits) >= min_contacts
     step = float(np.float32(s.opt_dt))
     # oracle: one cluster after another, its warm store empty
     ref_world = O.World(base.copy(), s.opt_dt, s.gravity_z)
@@ -149,6 +147,30 @@ def test_solve_matches_oracle(ctx):
     ref_warm = ref_world.warm()
     assert {k: np.float64(v).view(np.uint64) for k, v in warm.items()} == \
         {k: np.float64(v).view(np.uint64) for k, v in ref_warm.items()}
+    return clusters, hits
+
+
+def test_solve_matches_oracle(ctx):
+    # a state with many contacts: the cube scene after 120 oracle steps
+    s = D.make_scene(1, nx=2, ny=2, nz=2)
+    w = O.World(s.copy(), s.opt_dt, s.gravity_z)
+    w.step(120)
+    solve_against_oracle(ctx, w.get_bodies().copy(), s)
+
+
+def test_solve_wide_cluster_grid_matches_oracle(ctx):
+    # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling
+    # at 0.5 m/s: one cluster of 144 moving bodies with hundreds of contacts,
+    # solved by the cooperative grid
+    s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
+    s.cur[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
+    s.cur[1:, 10] = 0.51
+    s.cur[1:, 11:14] = [0.0, 0.0, -0.5]
+    s.fut[1:] = s.cur[1:]
+    s.last[1:] = s.cur[1:]
+    clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+    assert max(len(parts) for parts, _ in clusters) > 128
+    assert max(len(h) for h in hits) >= 128
 
 
 def test_fp32_bounds_do_not_change_results(ctx):
