@@ -156,6 +156,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def tuned(ctx):
+    """Apply the launch-shape settings of the committed tuning file
+    (delta2_gb300/autotune.py, measured on GB300); results do not depend on them."""
+    from delta2_gb300 import autotune
+
+    ctx.apply_tuning(autotune.load())
+    return ctx
+
+
 def cpu_baseline(scene, pairs, mt, budget_s):
     """The oracle (single thread, the reference's serial path) on a strided
     sample of the same pair list, for about budget_s seconds."""
@@ -193,7 +202,7 @@ def run_ours(args):
     scene, pairs, mt = build_workload(args.seed)
     n_pairs = len(pairs)
 
-    ctx = D.Context(local_rank)
+    ctx = tuned(D.Context(local_rank))
     ctx.set_scene(scene.copy())
     d_pairs = torch.from_numpy(pairs).cuda()
     d_mt = torch.from_numpy(mt).cuda()
@@ -311,7 +320,8 @@ def run_ours(args):
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "bodies": int(scene.n_bodies), "pair_queries_per_step": n_pairs,
                    "dt": scene.opt_dt, "l2": "flushed before every timed step (512 MB write)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "tuning": {D.TUNE_NAMES_INV[k]: ctx.get_tuning(k) for k in D.TUNE_NAMES_INV}},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
         "kernel_time_share": kernel_share, "precision_modes": modes, "world_steps": steps_line,
         "batched_steps": batch_line,
@@ -401,7 +411,7 @@ def world_steps(local_rank, args):
     import delta2_gb300 as D
 
     s0 = D.make_scene(2, seed=args.seed)
-    ctx = D.Context(local_rank)
+    ctx = tuned(D.Context(local_rank))
     ctx.set_scene(s0.copy())
     ctx.world_configure(s0)
     ctx.world_step(max(1, args.warmup))
@@ -469,7 +479,7 @@ def batched_steps(local_rank, args):
     t0 = time.perf_counter()
     batch, scene_of, scenes = D.make_batch(args.batch_scenes, seed=args.seed)
     build_s = time.perf_counter() - t0
-    ctx = D.Context(local_rank)
+    ctx = tuned(D.Context(local_rank))
     ctx.set_scene(batch.copy())
     ctx.set_scenes(scene_of)
     ctx.world_configure(batch)
@@ -485,7 +495,7 @@ def batched_steps(local_rank, args):
     ctx.close()
     ctxs = []
     for sc in scenes:
-        x = D.Context(local_rank)
+        x = tuned(D.Context(local_rank))
         x.set_scene(sc.copy())
         x.world_configure(sc)
         x.world_step(max(1, min(args.warmup, 2)))

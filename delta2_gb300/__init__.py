@@ -305,6 +305,9 @@ def broad_phase(scene):
 
 
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
+TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS = range(2)
+TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS}
+TUNE_NAMES_INV = {v: k for k, v in TUNE_NAMES.items()}
 
 
 def pcg32_seed(initstate, initseq):
@@ -358,6 +361,20 @@ class Context:
         """FP32 candidate bounds before the FP64 primitive tests (default on;
         results are identical either way)."""
         _check(lib().d2g_ctx_set_fp32_bounds(self.h, int(bool(enable))))
+
+    def set_tuning(self, key, value):
+        """Launch-shape setting (TUNE_*); results are identical for every value."""
+        _check(lib().d2g_ctx_set_tuning(self.h, int(key), int(value)))
+
+    def get_tuning(self, key):
+        v = C.c_int32()
+        _check(lib().d2g_ctx_get_tuning(self.h, int(key), C.byref(v)))
+        return v.value
+
+    def apply_tuning(self, settings):
+        """Apply {name: value} settings, e.g. those written by delta2_gb300.autotune."""
+        for name, value in settings.items():
+            self.set_tuning(TUNE_NAMES[name], value)
 
     def set_scenes(self, scene_of_body):
         """Batch independent scenes: scene index of every body (after set_bodies)."""

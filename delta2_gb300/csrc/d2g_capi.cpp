@@ -497,6 +497,28 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* c, int32_t enable) {
     return D2G_OK;
 }
 
+int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
+    if (!c || key < 0 || key >= D2G_TUNE_KEYS) {
+        set_error("null context or unknown tuning key");
+        return D2G_ERR_INVALID;
+    }
+    if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10)) {
+        set_error("tuning value out of range");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.tune[key] = value;
+    return D2G_OK;
+}
+
+int d2g_ctx_get_tuning(d2g_ctx* c, int32_t key, int32_t* value) {
+    if (!c || !value || key < 0 || key >= D2G_TUNE_KEYS) {
+        set_error("null argument or unknown tuning key");
+        return D2G_ERR_INVALID;
+    }
+    *value = c->eng.tune[key];
+    return D2G_OK;
+}
+
 int d2g_ctx_launches(d2g_ctx* c, int64_t* launches) {
     if (!c || !launches) {
         set_error("null argument");

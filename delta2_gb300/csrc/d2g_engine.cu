@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, c
 //                iterations with about half the instructions per iteration,
 //                on few enough warps that each has an SMSP to itself.
 // Each test performs exactly the operations of edge_edge_ccd, in order.
-constexpr int kEeFirstIters = 2;
+constexpr int kEeFirstItersDefault = 2;  // the first-pass iteration cap (context setting D2G_TUNE_EE_FIRST_ITERS)
 constexpr int kEeRec = 34;  // saved test: 24 point coordinates, t, min_dist, P, Q, toc, iterations done
 struct EeArgs {
     int n_tp, n_conn;
@@ -603,6 +603,7 @@ struct EeArgs {
     int32_t* out;    // the test's result slot: soup sub-result s >= 0, or leaf-pair item -1 - s
     float* thr;      // the test's hit threshold (leaf-pair tests)
     int32_t* count;  // [0] listed tests
+    int first_iters;  // Newton iterations in the first pass
 };
 
 __device__ __forceinline__ void ee_store_at(const EeArgs& a, int o, float thr, const Ccd& r) {
@@ -683,7 +684,7 @@ __global__ void __launch_bounds__(kPrimBlock) k_ee_first(int n_total, const int3
             }
             bool done = !(min_dist > 1e-8);
             if (!done && !bisected) {
-                for (; iters < kEeFirstIters; iters++)
+                for (; iters < a.first_iters; iters++)
                     if (ee_newton_iter(aS, aE, bS, bE, t, min_dist, r)) {
                         done = true;
                         break;
@@ -1576,6 +1577,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             ea.out = E.ee_out.p;
             ea.thr = E.ee_thr.p;
             ea.count = E.ee_count.p;
+            ea.first_iters = E.tune[D2G_TUNE_EE_FIRST_ITERS];
             D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
             k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, off_ee + w_ee, E.pm.p,
                                                                           ctx->tris.p, ea);

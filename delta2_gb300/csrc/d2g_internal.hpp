@@ -183,6 +183,8 @@ struct Engine {
     DBuf<int32_t> ee_out, ee_count;
     DBuf<float> ee_thr;
     int ee_grid = 0;  // k_ee_rest4 grid (every block resident)
+    // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
+    int tune[D2G_TUNE_KEYS] = {2, 256};
   // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing

@@ -30,7 +30,8 @@ constexpr int kBlock = 128;
 constexpr int kSolveBlock = 256;
 constexpr int kGridMinContacts = 128;  // a cluster this large may take a cooperative grid
 constexpr int kGridMaxClusters = 8;    // ... when the call has at most this many clusters
-constexpr int kGridMinParts = 128;     // ... and its waves can be wider than one block takes at once
+// ... and it has more parts than the context's D2G_TUNE_GRID_MIN_PARTS (default
+// 256): its waves can be wider than one block takes at once
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -826,7 +827,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
         a.pair_warm = d_pair_warm;
         // A large cluster among few is solved by a cooperative grid over the
         // SMs; the others one block each.  A wave holds at most one contact
-        // per moving body, so a cluster of at most kGridMinParts parts never
+        // per moving body, so a cluster of at most D2G_TUNE_GRID_MIN_PARTS parts never
         // has waves much wider than the kSolveBlock / 4 contacts one block
         // takes at once, and the grid would only add its barriers.
         std::vector<int32_t> small, big;
@@ -834,7 +835,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
             const int nck = h_con_off ? h_con_off[c + 1] - h_con_off[c] : 0;
             const int npc = h_part_off ? h_part_off[c + 1] - h_part_off[c] : 0;
             if (h_con_off && h_part_off && n_clusters <= kGridMaxClusters && nck >= kGridMinContacts &&
-                npc > kGridMinParts)
+                npc > E.tune[D2G_TUNE_GRID_MIN_PARTS])
                 big.push_back(c);
             else
                 small.push_back(c);

@@ -144,6 +144,21 @@ int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
  * above FP32 and FP64 rounding) and run the FP64 test only where a hit is
  * possible; with 0 every test runs in FP64.  Results are identical. */
 int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
+/* Launch-shape settings (no reference counterpart).  They change only how
+ * the work is spread over the GPU; every setting gives identical results.
+ *   D2G_TUNE_EE_FIRST_ITERS (default 2, 0..10): Newton iterations an
+ *     edge-edge CCD test runs on one lane before the tests still running
+ *     continue on four lanes each.
+ *   D2G_TUNE_GRID_MIN_PARTS (default 256, >= 0): a cluster with at least 128
+ *     contacts, among at most 8 clusters in a solve call, is solved by a
+ *     cooperative grid over the SMs when it has more parts than this.
+ * delta2_gb300/autotune.py measures candidate values on a workload and
+ * writes them to a file that the Python layer applies. */
+#define D2G_TUNE_EE_FIRST_ITERS 0
+#define D2G_TUNE_GRID_MIN_PARTS 1
+#define D2G_TUNE_KEYS 2
+int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
+int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library launched on the context, and, with profiling on, CUDA-event times
  * of the dominant kernels: kind 0 swept-box filter, 1 point-triangle CCD

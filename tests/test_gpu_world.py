@@ -158,19 +158,45 @@ def test_solve_matches_oracle(ctx):
     solve_against_oracle(ctx, w.get_bodies().copy(), s)
 
 
-def test_solve_wide_cluster_grid_matches_oracle(ctx):
+@pytest.mark.parametrize("grid_min_parts", [128, 1000000], ids=["grid", "block"])
+def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts):
     # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling
     # at 0.5 m/s: one cluster of 144 moving bodies with hundreds of contacts,
-    # solved by the cooperative grid
+    # solved by the cooperative grid, or by one block when the part threshold
+    # is raised
+    ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, grid_min_parts)
     s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
     s.cur[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
     s.cur[1:, 10] = 0.51
     s.cur[1:, 11:14] = [0.0, 0.0, -0.5]
     s.fut[1:] = s.cur[1:]
     s.last[1:] = s.cur[1:]
-    clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+    try:
+        clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+    finally:
+        ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, 256)
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
+
+
+def test_ee_first_iters_do_not_change_results(ctx):
+    # the edge-edge split point is a launch-shape setting: every value gives
+    # the same contacts, bit for bit
+    s = D.make_scene(2, nx=4, ny=4, nz=4, speed_sigma=2.0, seed=9)
+    pairs = D.broad_phase(s)
+    mt = np.full(len(pairs), np.float64(np.float32(s.opt_dt)) * 4)
+    outs = []
+    try:
+        for v in (0, 1, 2, 3, 10):
+            ctx.set_scene(s.copy())
+            ctx.set_tuning(D.TUNE_EE_FIRST_ITERS, v)
+            outs.append(ctx.compare_trees_full_continuous(pairs, mt))
+    finally:
+        ctx.set_tuning(D.TUNE_EE_FIRST_ITERS, 2)
+    assert len(outs[0][0]) > 0
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(bits(np.asarray(a)), bits(np.asarray(b)))
 
 
 def test_fp32_bounds_do_not_change_results(ctx):

@@ -155,3 +155,27 @@ def test_broad_phase_matches_oracle():
         got = D.broad_phase(s)
         assert np.array_equal(got, ref), (cfg, len(got), len(ref))
         assert len(got) > 0
+
+
+def test_tuning_file_loader(tmp_path):
+    # the autotuner's output format: settings by name; no file means defaults
+    from delta2_gb300 import autotune
+
+    assert autotune.load(str(tmp_path / "absent.json")) == {}
+    f = tmp_path / "t.json"
+    f.write_text('{"gpu": "x", "settings": {"ee_first_iters": 3, "grid_min_parts": 256}}')
+    got = autotune.load(str(f))
+    assert got == {"ee_first_iters": 3, "grid_min_parts": 256}
+    assert set(got) <= set(D.TUNE_NAMES)
+
+
+def test_open_box_scene_and_parallel_trees():
+    # the noisy-icosphere scene: one static open box, then one mesh and tree per
+    # body built on all host cores from per-mesh streams (same trees every time)
+    a = D.make_scene(5, nx=2, ny=1, nz=1)
+    b = D.make_scene(5, nx=2, ny=1, nz=1)
+    assert a.n_bodies == 3 and a.is_static.tolist() == [1, 0, 0]
+    assert len(a.mesh_node_off) == 4  # box + one mesh per body
+    assert np.array_equal(a.tris, b.tris) and np.array_equal(a.nodes, b.nodes)
+    lo, hi = a.local_aabb[0, :3], a.local_aabb[0, 3:]
+    assert np.allclose(hi[:2] - lo[:2], 40.0) and np.isclose(hi[2] - lo[2], 20.0)
