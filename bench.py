@@ -66,6 +66,24 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(ms, world, device="cuda"):
+    """The slowest rank's time: every rank runs its own replica of the
+    workload (the path has no data exchange between GPUs), so the job's time
+    is the maximum over ranks."""
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, ms, world):
+    """Whole-job units per second: all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / (ms / 1e3)
+
+
 def build_workload(seed):
     import numpy as np
 
@@ -265,21 +283,13 @@ def run_ours(args):
              "fp64_exact": {"value": n_pairs * n_exact / (exact_ms / 1e3), "contacts": int(n_exact_contacts),
                             "steps": n_exact}}
 
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = world * n_pairs * args.steps / (max_ms / 1e3)
+    max_ms = max_over_ranks(total_ms, world)
+    value = replica_throughput(n_pairs * args.steps, max_ms, world)
 
     # ---- end to end through the host C-ABI entry points (pinned host buffers)
     e2e = e2e_host(ctx, scene, pairs, mt, args)
     steps_line, steps_scene, steps_per = world_steps(local_rank, args)
-    t = torch.tensor([steps_line["ms_per_step"]], dtype=torch.float64, device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    steps_line["value"] = world * 1e3 / float(t.item())
+    steps_line["value"] = replica_throughput(1, max_over_ranks(steps_line["ms_per_step"], world), world)
     batch_line, batch_scenes = (None, None)
     if args.batch_scenes > 0:
         batch_line, batch_scenes = batched_steps(local_rank, args)
