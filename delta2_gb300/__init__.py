@@ -371,6 +371,11 @@ class Context:
         _check(lib().d2g_ctx_get_tuning(self.h, int(key), C.byref(v)))
         return v.value
 
+    def set_level_budget(self, nbytes):
+        """Cap the bytes a traversal level may use (0: a third of the device);
+        larger calls run in chunks of body pairs, with identical results."""
+        _check(lib().d2g_ctx_set_level_budget(self.h, C.c_int64(int(nbytes))))
+
     def apply_tuning(self, settings):
         """Apply {name: value} settings, e.g. those written by delta2_gb300.autotune."""
         for name, value in settings.items():

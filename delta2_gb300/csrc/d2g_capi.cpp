@@ -510,6 +510,15 @@ int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
     return D2G_OK;
 }
 
+int d2g_ctx_set_level_budget(d2g_ctx* c, int64_t bytes) {
+    if (!c || bytes < 0) {
+        set_error("null context or negative budget");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.level_budget = bytes;
+    return D2G_OK;
+}
+
 int d2g_ctx_get_tuning(d2g_ctx* c, int32_t key, int32_t* value) {
     if (!c || !value || key < 0 || key >= D2G_TUNE_KEYS) {
         set_error("null argument or unknown tuning key");

@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, c
 //                on few enough warps that each has an SMSP to itself.
 // Each test performs exactly the operations of edge_edge_ccd, in order.
 constexpr int kEeFirstItersDefault = 2;  // the first-pass iteration cap (context setting D2G_TUNE_EE_FIRST_ITERS)
-constexpr int kEeRec = 34;  // saved test: 24 point coordinates, t, min_dist, P, Q, toc, iterations done
+constexpr int kEeRec = 10;  // saved test: t, min_dist, P, Q, toc, iterations done (the edges are recomputed)
 struct EeArgs {
     int n_tp, n_conn;
     const int32_t* items;
@@ -599,9 +599,10 @@ struct EeArgs {
     PrimResult* sub;
     PrimResult* cres;
     int32_t* chit;
+    const double* pm;
+    const double* tris;
     double* rec;     // kEeRec per listed test
-    int32_t* out;    // the test's result slot: soup sub-result s >= 0, or leaf-pair item -1 - s
-    float* thr;      // the test's hit threshold (leaf-pair tests)
+    int32_t* work;   // the listed test's work item
     int32_t* count;  // [0] listed tests
     int first_iters;  // Newton iterations in the first pass
 };
@@ -708,18 +709,10 @@ __global__ void __launch_bounds__(kPrimBlock) k_ee_first(int n_total, const int3
         if (keep) {
             const int slot = base + __popc(m & ((1u << lane) - 1u));
             double* R = a.rec + (size_t)kEeRec * slot;
-            const V3 v[8] = {aS.A, aS.B, aE.A, aE.B, bS.A, bS.B, bE.A, bE.B};
+            const double st[kEeRec] = {t, min_dist, r.P.x, r.P.y, r.P.z, r.Q.x, r.Q.y, r.Q.z, r.toc, (double)iters};
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-                R[3 * k] = v[k].x;
-                R[3 * k + 1] = v[k].y;
-                R[3 * k + 2] = v[k].z;
-            }
-            const double tail[10] = {t, min_dist, r.P.x, r.P.y, r.P.z, r.Q.x, r.Q.y, r.Q.z, r.toc, (double)iters};
-#pragma unroll
-            for (int k = 0; k < 10; k++) R[24 + k] = tail[k];
-            a.out[slot] = o;
-            a.thr[slot] = thr;
+            for (int k = 0; k < kEeRec; k++) R[k] = st[k];
+            a.work[slot] = list[kk];
         }
     }
 }
@@ -796,12 +789,28 @@ __global__ void __launch_bounds__(kBlock) k_ee_rest4(EeArgs a) {
     const int n_quads = (gridDim.x * blockDim.x) >> 2;
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < n; i += n_quads) {
         const double* R = a.rec + (size_t)kEeRec * i;
-        // aS.A, aS.B, aE.A, aE.B, bS.A, bS.B, bE.A, bE.B (this lane's component)
-        const double aSA = R[comp], aSB = R[3 + comp], aEA = R[6 + comp], aEB = R[9 + comp];
-        const double bSA = R[12 + comp], bSB = R[15 + comp], bEA = R[18 + comp], bEB = R[21 + comp];
-        double t = R[24], min_dist = R[25];
-        double rP = R[26 + comp], rQ = R[29 + comp], toc = R[32];
-        for (int iter = (int)R[33]; iter < kEeNewtonIters; iter++) {
+        const EeWork w = decode_ee(a.work[i], a.n_tp, a.items, a.soup, a.conn, a.nn_off, a.n_conn, a.ntris, a.sub,
+                                   a.cres, a.chit);
+        // this lane's component of the edges' endpoints at start and end
+        // (xform_rigid's row `comp`, the same operations in the same order)
+        const double* M = a.pm + (size_t)PM_SIZE * w.pair;
+        const double* ta = a.tris + (size_t)w.na * 72 + w.aTri * 9;
+        const double* tb = a.tris + (size_t)w.nb * 72 + w.bTri * 9;
+        const double* va0 = ta + 3 * w.aEdge;
+        const double* va1 = ta + 3 * (w.aEdge == 2 ? 0 : w.aEdge + 1);
+        const double* vb0 = tb + 3 * w.bEdge;
+        const double* vb1 = tb + 3 * (w.bEdge == 2 ? 0 : w.bEdge + 1);
+        auto row = [&](const double* T, const double* v) {
+            const double* m = T + 4 * comp;
+            return ((m[0] * v[0] + m[1] * v[1]) + m[2] * v[2]) + m[3] * 1.0;
+        };
+        const double aSA = row(M + PM_AS, va0), aSB = row(M + PM_AS, va1);
+        const double aEA = row(M + PM_AE, va0), aEB = row(M + PM_AE, va1);
+        const double bSA = row(M + PM_BS, vb0), bSB = row(M + PM_BS, vb1);
+        const double bEA = row(M + PM_BE, vb0), bEB = row(M + PM_BE, vb1);
+        double t = R[0], min_dist = R[1];
+        double rP = R[2 + comp], rQ = R[5 + comp], toc = R[8];
+        for (int iter = (int)R[9]; iter < kEeNewtonIters; iter++) {
             const double atA = q_lerp(aSA, aEA, t), atB = q_lerp(aSB, aEB, t);
             const double btA = q_lerp(bSA, bEA, t), btB = q_lerp(bSB, bEB, t);
             double P, Qv;
@@ -848,7 +857,7 @@ __global__ void __launch_bounds__(kBlock) k_ee_rest4(EeArgs a) {
             r.P = mk(Px, Py, Pz);
             r.Q = mk(Qx, Qy, Qz);
             r.toc = toc;
-            ee_store_at(a, a.out[i], a.thr[i], r);
+            ee_store_at(a, w.hit ? -1 - (int)(w.out - a.cres) : (int)(w.out - a.sub), a.search[w.pair], r);
         }
     }
 }
@@ -1464,6 +1473,16 @@ int ee_grid_size(d2g_ctx* ctx, int* grid) {
     return D2G_OK;
 }
 
+// Bytes a traversal level may use for its buffers: a third of the device
+// memory (the rest holds the scene, the records and other stages).  A test
+// may lower it (d2g_ctx_set_level_budget) to exercise the chunking.
+double level_budget(d2g_ctx* ctx) {
+    if (ctx->eng.level_budget > 0) return (double)ctx->eng.level_budget;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1e30;
+    return (double)total_b / 3.0;
+}
+
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters) {
     Engine& E = ctx->eng;
@@ -1479,13 +1498,33 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     if (n_pairs > 0)
         LAUNCH(k_ccd_prep, 4LL * n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
-    int n_soup = n_pairs, n_conn = 0;
     RC(E.pm32c.ensure((size_t)96 * n_pairs + 1));
     if (n_pairs > 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);  // FP32 poses, once per call
+    // Pair chunks: the traversal of a range of body pairs runs to the end
+    // before the next range starts.  A level whose buffers would pass the
+    // budget abandons its chunk (its records are dropped) and the chunk is
+    // halved.  A pair's records come from one chunk and are sorted by pair at
+    // the end, so the results do not depend on the chunking.
+    RC(E.roots.ensure(n_pairs + 1));
+    if (n_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(E.roots.p, E.soup.p, sizeof(Entry) * n_pairs, cudaMemcpyDeviceToDevice, s));
+    const double budget = level_budget(ctx);
+    int chunk = n_pairs;
+    for (int p0 = 0; p0 < n_pairs;) {
+    const int p1 = std::min(n_pairs, p0 + chunk);
+    const int rec_start = n_rec;
+    int64_t k_node = 0, k_tri = 0, k_leaf = 0, k_levels = 0;
+    bool abandon = false;
+    D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
+    int n_soup = p1 - p0, n_conn = 0;
     while (n_soup > 0 || n_conn > 0) {
-        c_levels++;
-        c_node += n_soup + n_conn;
-        c_leaf += n_conn;
+        if (64.0 * 8.0 * 1.5 * n_soup > budget && p1 - p0 > 1) {
+            abandon = true;
+            break;
+        }
+        k_levels++;
+        k_node += n_soup + n_conn;
+        k_leaf += n_conn;
         // (1) soup swept-box filter and leaf-pair sizes, one synchronisation
         const int n_slots = 64 * n_soup;
         RC(E.flags.ensure(n_slots + 1));
@@ -1513,7 +1552,12 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
                       " triangle pairs exceeds the 32-bit test index range");
             return D2G_ERR_INVALID;
         }
-        c_tri += (int64_t)K + 15 * (int64_t)P;
+        // bytes of the level's test buffers (x1.5 for the buffers' growth slack)
+        if (1.5 * 1900.0 * ((double)K + (double)P) > budget && p1 - p0 > 1) {
+            abandon = true;
+            break;
+        }
+        k_tri += (int64_t)K + 15 * (int64_t)P;
         // (2) all primitive tests of the level
         RC(E.items.ensure(K + 1));
         RC(E.sub.ensure(15 * (size_t)K + 1));
@@ -1541,8 +1585,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         int32_t* list_ee = E.ccd_list.p + n_pt;
         if (n_ee > 0) {
             RC(E.ee_rec.ensure((size_t)kEeRec * n_ee));
-            RC(E.ee_out.ensure(n_ee));
-            RC(E.ee_thr.ensure(n_ee));
+            RC(E.ee_work.ensure(n_ee));
             RC(E.ee_count.ensure(1));
         }
         // The point-triangle and edge-edge chains touch disjoint outputs: the
@@ -1573,9 +1616,10 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             ea.sub = E.sub.p;
             ea.cres = E.cres.p;
             ea.chit = E.chit.p;
+            ea.pm = E.pm.p;
+            ea.tris = ctx->tris.p;
             ea.rec = E.ee_rec.p;
-            ea.out = E.ee_out.p;
-            ea.thr = E.ee_thr.p;
+            ea.work = E.ee_work.p;
             ea.count = E.ee_count.p;
             ea.first_iters = E.tune[D2G_TUNE_EE_FIRST_ITERS];
             D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
@@ -1639,6 +1683,17 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         n_soup = tot2[2];
         n_conn = tot2[3];
     }
+    if (abandon) {
+        n_rec = rec_start;
+        chunk = std::max(1, (p1 - p0) / 2);
+        continue;
+    }
+    c_node += k_node;
+    c_tri += k_tri;
+    c_leaf += k_leaf;
+    c_levels += k_levels;
+    p0 = p1;
+    }
     RC(finish_records(ctx, n_pairs, n_rec));
     if (n_pairs > 0) {
         RC(E.last_pair.ensure(ctx->n_bodies + 1));
@@ -1670,11 +1725,31 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     if (n_pairs > 0)
         LAUNCH(k_np_prep, n_pairs, n_pairs, d_pairs, ctx->fut.p, ctx->mesh.p, ctx->mesh_node_off.p,
                                                      ctx->geo_eps.p, E.pm.p, E.search.p, E.soup.p, E.pm32.p);
-    int n = n_pairs, n_rec = 0;
+    int n_rec = 0;
     DBuf<double>& res_eps = E.pfut;  // reused as the per-slot eps record buffer
+    // pair chunks, as in run_ccd: a level that would pass the byte budget
+    // (~110 bytes per slot, 64 slots per node pair, x1.5 growth slack)
+    // abandons its chunk, which is halved
+    RC(E.roots.ensure(n_pairs + 1));
+    if (n_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(E.roots.p, E.soup.p, sizeof(Entry) * n_pairs, cudaMemcpyDeviceToDevice, s));
+    const double budget = level_budget(ctx);
+    int chunk = n_pairs;
+    for (int p0 = 0; p0 < n_pairs;) {
+    const int p1 = std::min(n_pairs, p0 + chunk);
+    const int rec_start = n_rec;
+    const int32_t tri_start = (int32_t)c_tri;  // the device counter's value before this chunk
+    int64_t k_node = 0, k_levels = 0;
+    bool abandon = false;
+    D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
+    int n = p1 - p0;
     while (n > 0) {
-        c_levels++;
-        c_node += n;
+        if (1.5 * 110.0 * 64.0 * n > budget && p1 - p0 > 1) {
+            abandon = true;
+            break;
+        }
+        k_levels++;
+        k_node += n;
         const int n_slots = 64 * n;
         RC(E.res.ensure(n_slots));
         RC(res_eps.ensure(4 * (size_t)n_slots));
@@ -1732,6 +1807,18 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
                                                      E.off_b.p, E.soup_next.p, E.conn_next.p);
         std::swap(E.soup, E.soup_next);
         n = tot;
+    }
+    if (abandon) {
+        n_rec = rec_start;
+        c_tri = tri_start;
+        ctx->h_pinned[0] = tri_start;  // stream-ordered before any later read into h_pinned
+        D2G_CUDA(cudaMemcpyAsync(E.np_tri.p, ctx->h_pinned, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        chunk = std::max(1, (p1 - p0) / 2);
+        continue;
+    }
+    c_node += k_node;
+    c_levels += k_levels;
+    p0 = p1;
     }
     RC(finish_records(ctx, n_pairs, n_rec));
     D2G_CUDA(cudaGetLastError());

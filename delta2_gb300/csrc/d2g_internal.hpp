@@ -180,9 +180,12 @@ struct Engine {
     DBuf<uint8_t> cub_tmp, cub_tmp2;
     // phased edge-edge CCD (d2g_engine.cu)
     DBuf<double> ee_rec;
-    DBuf<int32_t> ee_out, ee_count;
-    DBuf<float> ee_thr;
+    DBuf<int32_t> ee_work, ee_count;
     int ee_grid = 0;  // k_ee_rest4 grid (every block resident)
+    // traversal chunking: root entries of the call's pairs; a byte budget for
+    // a level's buffers (0: a third of the device memory)
+    DBuf<Entry> roots;
+    long long level_budget = 0;
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
     int tune[D2G_TUNE_KEYS] = {2, 256};
   // cub_tmp2: scans on the context's second stream

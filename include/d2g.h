@@ -159,6 +159,13 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
 #define D2G_TUNE_KEYS 2
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
+/* Memory cap (no reference counterpart): the bytes one level of a tree
+ * traversal (discrete narrow phase or CCD) may use for its buffers; 0 (the
+ * default) means a third of the device memory.  A call whose level would
+ * exceed it traverses its body pairs in chunks (halving a chunk that still
+ * exceeds it), with identical results.  The contact records themselves are
+ * output and are not capped. */
+int d2g_ctx_set_level_budget(d2g_ctx* ctx, int64_t bytes);
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library launched on the context, and, with profiling on, CUDA-event times
  * of the dominant kernels: kind 0 swept-box filter, 1 point-triangle CCD

@@ -240,3 +240,35 @@ def test_world_cube_pile_grid_solve(ctx):
     s = D.make_scene(1)
     st = run_world(ctx, s, 100)
     assert st["np_contacts"] > 0
+
+
+def test_chunked_traversals_match_unchunked(ctx):
+    # a level budget far below the calls' needs makes both traversals run in
+    # pair chunks (abandoned and halved until a level fits); the contacts are
+    # the same bits as one unchunked call
+    s = D.make_scene(2, nx=4, ny=4, nz=4, speed_sigma=2.0, seed=9)
+    pairs = D.broad_phase(s)
+    mt = np.full(len(pairs), np.float64(np.float32(s.opt_dt)) * 4)
+    out = {}
+    try:
+        for budget in (0, 200_000):
+            ctx.set_level_budget(budget)
+            ctx.set_scene(s.copy())
+            c1, o1, k1 = ctx.compare_trees_full_continuous(pairs, mt)
+            c2, o2, k2 = ctx.compare_trees_full(pairs)
+            out[budget] = (c1, o1, c2, o2)
+    finally:
+        ctx.set_level_budget(0)
+    assert len(out[0][0]) > 0 and len(out[0][2]) > 0
+    for a, b in zip(out[0], out[200_000]):
+        assert np.array_equal(bits(np.asarray(a)), bits(np.asarray(b)))
+
+
+def test_world_chunked_matches_oracle(ctx):
+    s = D.make_scene(1, nx=2, ny=2, nz=2)
+    try:
+        ctx.set_level_budget(100_000)
+        st = run_world(ctx, s, 100)
+    finally:
+        ctx.set_level_budget(0)
+    assert st["np_contacts"] > 0
