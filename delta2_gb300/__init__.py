@@ -372,7 +372,7 @@ class Context:
         return v.value
 
     def set_level_budget(self, nbytes):
-        """Cap the bytes a traversal level may use (0: a third of the device);
+        """Cap the bytes a traversal level may use (0: a sixth of the device);
         larger calls run in chunks of body pairs, with identical results."""
         _check(lib().d2g_ctx_set_level_budget(self.h, C.c_int64(int(nbytes))))
 

@@ -1207,10 +1207,11 @@ __global__ void k_iota(int n, int32_t* __restrict__ v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
 }
-__global__ void k_count_pairs(int n, int n_pairs, const int32_t* __restrict__ rec_pair, int32_t* __restrict__ cnt) {
+__global__ void k_count_pairs(int n, int p0, int n_pairs, const int32_t* __restrict__ rec_pair,
+                              int32_t* __restrict__ cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int p = rec_pair[i];
+    const int p = rec_pair[i] - p0;
     if (p >= 0 && p < n_pairs) atomicAdd(&cnt[p], 1);
 }
 __global__ void k_gather(int n, const int32_t* __restrict__ idx, const double* __restrict__ in,
@@ -1409,7 +1410,9 @@ int read_scalars(d2g_ctx* ctx, const int32_t* const* src, int k, int32_t* dst) {
     } while (0)
 
 // Sort records by pair (stable) into rec_sorted and write offsets [n_pairs+1].
-int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
+// Pairs [p0, p0 + n_pairs): the records' pair ids lie in that range and the
+// offsets are indexed from p0.
+int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec, int p0 = 0) {
     Engine& E = ctx->eng;
     RC(E.out_off.ensure(n_pairs + 1));
     RC(E.pair_cnt.ensure(n_pairs + 1));
@@ -1421,7 +1424,7 @@ int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
         RC(E.rec_pair_sorted.ensure(n_rec));
         LAUNCH(k_iota, n_rec, n_rec, E.rec_idx.p);
         int bits = 1;
-        while ((1 << bits) < n_pairs + 1 && bits < 31) bits++;
+        while ((1LL << bits) < (long long)p0 + n_pairs + 1 && bits < 31) bits++;
         size_t bytes = 0;
         D2G_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, bytes, E.rec_pair.p, E.rec_pair_sorted.p, E.rec_idx.p,
                                                  E.rec_idx_sorted.p, n_rec, 0, bits, ctx->stream));
@@ -1429,7 +1432,7 @@ int finish_records(d2g_ctx* ctx, int n_pairs, int n_rec) {
         D2G_CUDA(cub::DeviceRadixSort::SortPairs(E.cub_tmp.p, bytes, E.rec_pair.p, E.rec_pair_sorted.p, E.rec_idx.p,
                                                  E.rec_idx_sorted.p, n_rec, 0, bits, ctx->stream));
         LAUNCH(k_gather, n_rec, n_rec, E.rec_idx_sorted.p, E.rec.p, E.rec_sorted.p);
-        LAUNCH(k_count_pairs, n_rec, n_rec, n_pairs, E.rec_pair.p, E.pair_cnt.p);
+        LAUNCH(k_count_pairs, n_rec, n_rec, p0, n_pairs, E.rec_pair.p, E.pair_cnt.p);
     }
     RC(scan(ctx, E.pair_cnt.p, E.out_off.p, n_pairs));
     return D2G_OK;
@@ -1473,18 +1476,22 @@ int ee_grid_size(d2g_ctx* ctx, int* grid) {
     return D2G_OK;
 }
 
-// Bytes a traversal level may use for its buffers: a third of the device
-// memory (the rest holds the scene, the records and other stages).  A test
-// may lower it (d2g_ctx_set_level_budget) to exercise the chunking.
+// Bytes a traversal level may use for its buffers: a sixth of the device
+// memory (the rest holds the scene, the contact records with their sorted
+// copy, and other stages).  d2g_ctx_set_level_budget overrides it.
 double level_budget(d2g_ctx* ctx) {
-    if (ctx->eng.level_budget > 0) return (double)ctx->eng.level_budget;
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1e30;
-    return (double)total_b / 3.0;
+    Engine& E = ctx->eng;
+    if (E.level_budget > 0) return (double)E.level_budget;
+    if (E.device_bytes == 0) {  // queried once: the driver call is not free
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1e30;
+        E.device_bytes = total_b;
+    }
+    return (double)E.device_bytes / 6.0;
 }
 
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
-            int64_t* counters) {
+            int64_t* counters, const CcdSink* sink) {
     Engine& E = ctx->eng;
     cudaStream_t s = ctx->stream;
     int64_t c_node = 0, c_tri = 0, c_leaf = 0, c_levels = 0;
@@ -1495,6 +1502,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     int ee_grid = 0;
     RC(ee_grid_size(ctx, &ee_grid));
     int n_rec = 0;
+    long long n_streamed = 0;  // records handed to the sink
     if (n_pairs > 0)
         LAUNCH(k_ccd_prep, 4LL * n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->mesh.p,
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
@@ -1692,9 +1700,15 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     c_tri += k_tri;
     c_leaf += k_leaf;
     c_levels += k_levels;
+    if (sink) {  // the chunk's records, sorted by pair, go to the consumer and are dropped
+        RC(finish_records(ctx, p1 - p0, n_rec, p0));
+        RC(sink->consume(ctx, sink->user, p0, p1));
+        n_streamed += n_rec;
+        n_rec = 0;
+    }
     p0 = p1;
     }
-    RC(finish_records(ctx, n_pairs, n_rec));
+    if (!sink) RC(finish_records(ctx, n_pairs, n_rec));
     if (n_pairs > 0) {
         RC(E.last_pair.ensure(ctx->n_bodies + 1));
         LAUNCH(k_fill, ctx->n_bodies, ctx->n_bodies, E.last_pair.p, -1);
@@ -1702,7 +1716,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         LAUNCH(k_write_fut, n_pairs, n_pairs, d_pairs, E.last_pair.p, E.pfut.p, ctx->fut.p);
     }
     D2G_CUDA(cudaGetLastError());
-    *n_out = n_rec;
+    *n_out = sink ? (int)n_streamed : n_rec;
     if (counters) {
         counters[0] = c_node;
         counters[1] = c_tri;
@@ -2069,7 +2083,7 @@ extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const 
         D2G_CUDA(cub::DeviceRadixSort::SortPairs(tmp, avail, rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted,
                                                  n_rec, 0, bits, s));
         if (n_rec <= capacity) NA_LAUNCH(k_gather, n_rec, n_rec, rec_idx_sorted, rec, d_contacts);
-        NA_LAUNCH(k_count_pairs, n_rec, n_rec, n_pairs, rec_pair, pair_cnt);
+        NA_LAUNCH(k_count_pairs, n_rec, n_rec, 0, n_pairs, rec_pair, pair_cnt);
     }
     if (int rc = noalloc_scan(s, tmp, tmp_bytes, pair_cnt, d_offsets, n_pairs)) return rc;
     D2G_CUDA(cudaGetLastError());

@@ -28,6 +28,15 @@ void set_error(const std::string& msg);
         }                                                                                           \
     } while (0)
 
+// The failed allocation's size and the device memory then free, in the error text.
+inline void alloc_error(cudaError_t e, size_t bytes) {
+    cudaGetLastError();  // clear the (non-sticky) allocation error
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    set_error(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes (" + std::to_string(free_b) +
+              " of " + std::to_string(total_b) + " free): " + cudaGetErrorString(e));
+}
+
 // Device buffer that grows geometrically (capacity in elements); owns its
 // memory (freed on destruction, movable, not copyable).
 template <class T>
@@ -63,7 +72,8 @@ struct DBuf {
         cudaError_t e = cudaMalloc((void**)&p, c * sizeof(T));
         if (e != cudaSuccess) {
             cap = 0;
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            p = nullptr;
+            alloc_error(e, c * sizeof(T));
             return D2G_ERR_CUDA;
         }
         cap = c;
@@ -76,7 +86,7 @@ struct DBuf {
         T* q = nullptr;
         cudaError_t e = cudaMalloc((void**)&q, c * sizeof(T));
         if (e != cudaSuccess) {
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            alloc_error(e, c * sizeof(T));
             return D2G_ERR_CUDA;
         }
         if (p) {
@@ -186,6 +196,7 @@ struct Engine {
     // a level's buffers (0: a third of the device memory)
     DBuf<Entry> roots;
     long long level_budget = 0;
+    size_t device_bytes = 0;
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
     int tune[D2G_TUNE_KEYS] = {2, 256};
   // cub_tmp2: scans on the context's second stream
@@ -249,8 +260,16 @@ int prof_mark_begin(d2g_ctx* ctx, int kind, long long items);
 void prof_mark_end(d2g_ctx* ctx, int idx);
 void prof_mark_collect(d2g_ctx* ctx);
 // Engine entry points (d2g_engine.cu).
+// Consumer of a CCD call's records chunk by chunk (pairs [p0, p1)): when run_ccd
+// is given one, each chunk's records are sorted into rec_sorted with offsets
+// out_off[0 .. p1 - p0], handed over, and dropped, so the call never holds
+// every record at once.
+struct CcdSink {
+    void* user;
+    int (*consume)(d2g_ctx* ctx, void* user, int p0, int p1);
+};
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
-            int64_t* counters);
+            int64_t* counters, const CcdSink* sink = nullptr);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
 // Time-step selection (d2g_step.cu).
 // n_parts: particles of all clusters; max_cluster_parts: of the largest.

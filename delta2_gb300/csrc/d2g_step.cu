@@ -629,12 +629,29 @@ int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const in
     RC(E.st_new_dt.ensure(n_pairs + 1));
     RC(E.st_has.ensure(n_pairs + 1));
     if (n_pairs > 0) SLAUNCH(k_max_time, n_pairs, n_pairs, d_pairs, ctx->last_dt.p, E.st_mt.p);
+    // The CCD's records only feed each pair's new step: they are consumed
+    // chunk by chunk (sorted per chunk) and dropped.
+    struct Use {
+        const int32_t* pairs;
+    } use{d_pairs};
+    CcdSink sink;
+    sink.user = &use;
+    sink.consume = [](d2g_ctx* c, void* u, int p0, int p1) -> int {
+        Engine& En = c->eng;
+        const int32_t* pr = static_cast<Use*>(u)->pairs;
+        const int np = p1 - p0;
+        if (np > 0) {
+            k_pair_new_dt<<<nblocks(32LL * np), kBlock, 0, c->stream>>>(
+                np, pr + 2 * (size_t)p0, En.st_mt.p + p0, En.out_off.p, En.rec_sorted.p, En.pfut.p + 28 * (size_t)p0,
+                c->inv_inertia.p, En.st_new_dt.p + p0, En.st_has.p + p0);
+            En.launches++;
+        }
+        D2G_CUDA(cudaGetLastError());
+        return D2G_OK;
+    };
     int n_rec = 0;
-    RC(run_ccd(ctx, d_pairs, E.st_mt.p, n_pairs, &n_rec, counters));
+    RC(run_ccd(ctx, d_pairs, E.st_mt.p, n_pairs, &n_rec, counters, &sink));
     if (n_ccd_contacts) *n_ccd_contacts = n_rec;
-    if (n_pairs > 0)
-        SLAUNCH(k_pair_new_dt, 32LL * n_pairs, n_pairs, d_pairs, E.st_mt.p, E.out_off.p, E.rec_sorted.p, E.pfut.p,
-                ctx->inv_inertia.p, E.st_new_dt.p, E.st_has.p);
     if (n_clusters > 0) {
         RC(E.st_loc.ensure(ctx->n_bodies + 1));
         constexpr int kMaxSmemParts = 24 * 1024;  // 192 KB of steps

@@ -161,7 +161,7 @@ int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Memory cap (no reference counterpart): the bytes one level of a tree
  * traversal (discrete narrow phase or CCD) may use for its buffers; 0 (the
- * default) means a third of the device memory.  A call whose level would
+ * default) means a sixth of the device memory.  A call whose level would
  * exceed it traverses its body pairs in chunks (halving a chunk that still
  * exceeds it), with identical results.  The contact records themselves are
  * output and are not capped. */
