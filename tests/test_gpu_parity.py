@@ -150,6 +150,18 @@ def test_ccd_parity_hulls_benchmark_scene(ctx):
     ccd_parity(ctx, s, pairs, mt)
 
 
+def test_ccd_and_narrowphase_parity_noisy_icospheres(ctx):
+    """Non-convex bodies (1,280-triangle noisy icospheres, deep trees) in the
+    open box: a 2 x 2 x 2 block close together, moving fast."""
+    s = project_futures(D.make_scene(5, nx=2, ny=2, nz=2, spacing=1.15, speed_sigma=2.0, seed=4))
+    pairs = broad_pairs(s)
+    assert len(pairs) >= 8
+    mt = np.full(len(pairs), 0.01)
+    n, cnt = ccd_parity(ctx, s, pairs, mt)
+    assert n > 0 and cnt[2] > 0
+    assert np_parity(ctx, s, pairs) > 0
+
+
 def test_narrowphase_parity_cubes(ctx):
     s = project_futures(D.make_scene(1, spacing=1.12, speed_sigma=3.0, seed=5))
     pairs = broad_pairs(s)
