@@ -382,7 +382,7 @@ __device__ __forceinline__ PtWork decode_pt(int j, int n_tp, const int32_t* item
     return w;
 }
 
-// Edge-edge work item j (the decoding of k_prim_ee).
+// Edge-edge work item j, as the edge-edge mask and CCD kernels decode it.
 struct EeWork {
     int pair, na, nb, aTri, aEdge, bTri, bEdge;
     PrimResult* out;
