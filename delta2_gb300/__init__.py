@@ -78,7 +78,8 @@ def compare_trees_full_noalloc(device_scene, d_pairs, n_pairs, d_contacts, capac
 class SceneOpts(C.Structure):
     _fields_ = [("config", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("spacing", C.c_double), ("speed_sigma", C.c_double), ("seed", C.c_uint64), ("dt", C.c_float),
-                ("gravity_z", C.c_double), ("mu", C.c_double), ("hull_points", C.c_int32), ("count", C.c_int32)]
+                ("gravity_z", C.c_double), ("mu", C.c_double), ("hull_points", C.c_int32), ("count", C.c_int32),
+                ("tree_file", C.c_char_p)]
 
 
 def library_path():
@@ -97,6 +98,7 @@ def lib():
         L.d2g_version.restype = C.c_char_p
         L.d2g_ctx_destroy.restype = None
         L.d2g_scene_free.restype = None
+        L.d2g_tree_file_free.restype = None
         _lib = L
     return _lib
 
@@ -205,6 +207,47 @@ def split_bodies(batch, scene_of, k):
     return out
 
 
+def _trees_struct(scene):
+    t = Trees()
+    t.n_meshes = len(scene.mesh_node_off) - 1
+    scene._tree_keep = [np.ascontiguousarray(scene.mesh_node_off, dtype=np.int32),
+                        np.ascontiguousarray(scene.nodes, dtype=np.int32),
+                        np.ascontiguousarray(scene.ntris, dtype=np.int32),
+                        np.ascontiguousarray(scene.tris, dtype=np.float64),
+                        np.ascontiguousarray(scene.eps, dtype=np.float64),
+                        np.ascontiguousarray(scene.inner_eps, dtype=np.float64)]
+    k = scene._tree_keep
+    t.mesh_node_off, t.nodes, t.ntris = _p(k[0], I32P), _p(k[1], I32P), _p(k[2], I32P)
+    t.tris, t.eps, t.inner_eps = _p(k[3], F64P), _p(k[4], F64P), _p(k[5], F64P)
+    return t
+
+
+def save_trees(scene, path):
+    """Write the scene's trees to a tree file (d2g_trees_save)."""
+    _check(lib().d2g_trees_save(C.byref(_trees_struct(scene)), str(path).encode()))
+
+
+def load_trees(path):
+    """Arrays of a tree file: mesh_node_off, nodes, ntris, tris, eps, inner_eps."""
+    L = lib()
+    h = C.c_void_p()
+    _check(L.d2g_trees_load(str(path).encode(), C.byref(h)))
+    try:
+        t = Trees()
+        _check(L.d2g_tree_file_view(h, C.byref(t)))
+        M = t.n_meshes
+        off = np.ctypeslib.as_array(t.mesh_node_off, (M + 1,)).copy()
+        N = int(off[-1])
+        return {"mesh_node_off": off,
+                "nodes": np.ctypeslib.as_array(t.nodes, (N, 4)).copy() if N else np.zeros((0, 4), np.int32),
+                "ntris": np.ctypeslib.as_array(t.ntris, (N,)).copy() if N else np.zeros(0, np.int32),
+                "tris": np.ctypeslib.as_array(t.tris, (N, 8, 9)).copy() if N else np.zeros((0, 8, 9)),
+                "eps": np.ctypeslib.as_array(t.eps, (N, 8)).copy() if N else np.zeros((0, 8)),
+                "inner_eps": np.ctypeslib.as_array(t.inner_eps, (N, 8)).copy() if N else np.zeros((0, 8))}
+    finally:
+        L.d2g_tree_file_free(h)
+
+
 def make_batch(n_scenes=256, seed=0, min_bodies=8, max_bodies=512, dt=0.0):
     """The batched configuration: n_scenes independent mixed scenes (cubes,
     64-point hulls and subdivision-2 icospheres in turn), each on its own
@@ -222,10 +265,13 @@ def make_batch(n_scenes=256, seed=0, min_bodies=8, max_bodies=512, dt=0.0):
 
 
 def make_scene(config=2, nx=0, ny=0, nz=0, spacing=0.0, speed_sigma=-1.0, seed=0, dt=0.0, gravity_z=-9.8, mu=0.0,
-               hull_points=64, count=0):
-    """Synthetic scene of a benchmark configuration (host set-up, no GPU)."""
+               hull_points=64, count=0, tree_file=None):
+    """Synthetic scene of a benchmark configuration (host set-up, no GPU).
+    With tree_file, the trees are loaded from that file when it exists, else
+    built and saved there."""
     L = lib()
-    o = SceneOpts(config, nx, ny, nz, spacing, speed_sigma, seed, dt, gravity_z, mu, hull_points, count)
+    o = SceneOpts(config, nx, ny, nz, spacing, speed_sigma, seed, dt, gravity_z, mu, hull_points, count,
+                  tree_file.encode() if tree_file else None)
     h = C.c_void_p()
     _check(L.d2g_scene_make(C.byref(o), C.byref(h)))
     try:

@@ -111,6 +111,7 @@ int d2g_scene_make(const d2g_scene_opts* o, d2g_scene** out) {
     so.mu = o->mu;
     so.hull_points = o->hull_points > 3 ? o->hull_points : 64;
     so.count = o->count;
+    if (o->tree_file) so.tree_file = o->tree_file;
     d2g_scene* s = new d2g_scene();
     std::string err;
     if (!d2g::make_scene(so, s->s, &err)) {
@@ -123,6 +124,75 @@ int d2g_scene_make(const d2g_scene_opts* o, d2g_scene** out) {
 }
 
 void d2g_scene_free(d2g_scene* s) { delete s; }
+
+struct d2g_tree_file {
+    d2g::TreeSet t;
+};
+
+int d2g_trees_save(const d2g_trees* t, const char* path) {
+    if (!t || !path || t->n_meshes < 0 || !t->mesh_node_off) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    d2g::TreeSet ts;
+    const int M = t->n_meshes;
+    const int N = t->mesh_node_off[M];
+    if (N < 0 || (N > 0 && (!t->nodes || !t->ntris || !t->tris || !t->eps || !t->inner_eps))) {
+        set_error("invalid tree arrays");
+        return D2G_ERR_INVALID;
+    }
+    ts.mesh_node_off.assign(t->mesh_node_off, t->mesh_node_off + M + 1);
+    ts.nodes.assign(t->nodes, t->nodes + 4 * (size_t)N);
+    ts.ntris.assign(t->ntris, t->ntris + N);
+    ts.tris.assign(t->tris, t->tris + 72 * (size_t)N);
+    ts.eps.assign(t->eps, t->eps + 8 * (size_t)N);
+    ts.inner_eps.assign(t->inner_eps, t->inner_eps + 8 * (size_t)N);
+    for (int m = 0; m < M; m++) {  // a mesh's triangles are its leaf buckets'
+        int n = 0;
+        for (int i = ts.mesh_node_off[m]; i < ts.mesh_node_off[m + 1]; i++)
+            if (ts.nodes[4 * (size_t)i] == -1) n += ts.ntris[i];
+        ts.mesh_ntris.push_back(n);
+    }
+    std::string err;
+    if (!d2g::save_trees(ts, path, &err)) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    return D2G_OK;
+}
+
+int d2g_trees_load(const char* path, d2g_tree_file** out) {
+    if (!path || !out) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    d2g_tree_file* f = new d2g_tree_file();
+    std::string err;
+    if (!d2g::load_trees(path, f->t, &err)) {
+        delete f;
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    *out = f;
+    return D2G_OK;
+}
+
+int d2g_tree_file_view(d2g_tree_file* f, d2g_trees* t) {
+    if (!f || !t) {
+        set_error("null argument");
+        return D2G_ERR_INVALID;
+    }
+    t->n_meshes = (int32_t)f->t.mesh_ntris.size();
+    t->mesh_node_off = f->t.mesh_node_off.data();
+    t->nodes = f->t.nodes.data();
+    t->ntris = f->t.ntris.data();
+    t->tris = f->t.tris.data();
+    t->eps = f->t.eps.data();
+    t->inner_eps = f->t.inner_eps.data();
+    return D2G_OK;
+}
+
+void d2g_tree_file_free(d2g_tree_file* f) { delete f; }
 
 int d2g_scene_view(d2g_scene* sc, d2g_trees* t, d2g_bodies* b, const float** local_aabb, float* opt_dt,
                    double* gravity_z) {

@@ -6,6 +6,7 @@
 #include <array>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <deque>
 #include <limits>
 #include <map>
@@ -828,12 +829,73 @@ double normal(Pcg32& rng) {
 
 }  // namespace
 
+static bool file_exists(const std::string& path) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    std::fclose(f);
+    return true;
+}
+
+// The trees of every mesh, in creation order: loaded from o.tree_file when
+// it exists (checked against the meshes' triangle counts), else built and,
+// with a tree_file, saved there.  Meshes draw from one PCG32 stream in order,
+// except configuration 5, whose per-body meshes (all but the box) draw from
+// their own streams (42, 55 + k) and are built on all host cores.
+bool finish_trees(Scene& s, const std::vector<Mesh>& meshes, const SceneOpts& o, Pcg32& tree_rng,
+                  std::string* err) {
+    TreeSet ts;
+    const bool have_file = !o.tree_file.empty() && file_exists(o.tree_file);
+    if (have_file) {
+        if (!load_trees(o.tree_file.c_str(), ts, err)) return false;
+        if (ts.mesh_ntris.size() != meshes.size()) {
+            if (err) *err = o.tree_file + ": " + std::to_string(ts.mesh_ntris.size()) + " trees for " +
+                            std::to_string(meshes.size()) + " meshes";
+            return false;
+        }
+        for (size_t k = 0; k < meshes.size(); k++)
+            if (ts.mesh_ntris[k] != meshes[k].nf()) {
+                if (err) *err = o.tree_file + ": tree " + std::to_string(k) + " is for another mesh";
+                return false;
+            }
+        s.mesh_node_off = ts.mesh_node_off;
+        s.nodes = ts.nodes;
+        s.ntris = ts.ntris;
+        s.tris = ts.tris;
+        s.eps = ts.eps;
+        s.inner_eps = ts.inner_eps;
+        s.mesh_ntris = ts.mesh_ntris;
+        return true;
+    }
+    if (o.config == 5) {
+        if (scene_add_mesh(s, meshes[0], tree_rng, err) < 0) return false;
+        std::vector<Mesh> bodies(meshes.begin() + 1, meshes.end());
+        std::vector<Tree> trees;
+        if (!build_trees_parallel(bodies, 55u, trees, err)) return false;
+        for (size_t k = 0; k < trees.size(); k++) scene_add_tree(s, trees[k], bodies[k].nf());
+    } else {
+        for (const Mesh& m : meshes)
+            if (scene_add_mesh(s, m, tree_rng, err) < 0) return false;
+    }
+    if (!o.tree_file.empty()) {
+        ts.mesh_node_off = s.mesh_node_off;
+        ts.mesh_ntris = s.mesh_ntris;
+        ts.nodes = s.nodes;
+        ts.ntris = s.ntris;
+        ts.tris = s.tris;
+        ts.eps = s.eps;
+        ts.inner_eps = s.inner_eps;
+        if (!save_trees(ts, o.tree_file.c_str(), err)) return false;
+    }
+    return true;
+}
+
 bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
     s = Scene();
     Pcg32 rng;
     rng.seed(0x9E3779B97F4A7C15ULL ^ o.seed, 0xD2 + (uint64_t)o.config);
     Pcg32 tree_rng;
     tree_rng.seed(42u, 54u);  // common/cli_options.h:45
+    std::vector<Mesh> meshes;  // in creation order; mesh id = index, trees built at the end
     const double density = 1000.0;
     int nx, ny, nz;
     double spacing, half, geo_eps, z0, sigma, mu, ground_w;
@@ -878,13 +940,10 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
             shift_vertices(g, gmp.com);
             gmp.com[0] = gmp.com[1] = gmp.com[2] = 0.0;
         }
-        const int gm = scene_add_mesh(s, g, tree_rng, err);
-        if (gm < 0) return false;
+        const int gm = (int)meshes.size();
+        meshes.push_back(g);
         add_body(s, gm, g, gmp, true, density, geo_eps, mu, at, ident, zero3, dt);
     }
-    // noisy icospheres: every body has its own mesh; the trees are built
-    // afterwards on all host cores (mesh ids follow the box's)
-    std::vector<Mesh> pending;
 
     int shared_mesh = -1;
     Mesh shared;
@@ -894,8 +953,8 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
         shared_mp = mass_volume(shared);
         shift_vertices(shared, shared_mp.com);
         shared_mp.com[0] = shared_mp.com[1] = shared_mp.com[2] = 0.0;
-        shared_mesh = scene_add_mesh(s, shared, tree_rng, err);
-        if (shared_mesh < 0) return false;
+        shared_mesh = (int)meshes.size();
+        meshes.push_back(shared);
     }
     constexpr int kMixHulls = 4;
     int mix_mesh[2 + kMixHulls];
@@ -931,13 +990,8 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
                         mp = mass_volume(m);
                         shift_vertices(m, mp.com);
                         mp.com[0] = mp.com[1] = mp.com[2] = 0.0;
-                        if (o.config == 5) {
-                            mesh_id = 1 + (int)pending.size();
-                            pending.push_back(m);
-                        } else {
-                            mesh_id = scene_add_mesh(s, m, tree_rng, err);
-                            if (mesh_id < 0) return false;
-                        }
+                        mesh_id = (int)meshes.size();
+                        meshes.push_back(m);
                         if (o.config == 3) {
                             mix_mesh[slot] = mesh_id;
                             mix_geom[slot] = m;
@@ -962,15 +1016,7 @@ bool make_scene(const SceneOpts& o, Scene& s, std::string* err) {
                 for (int k = 0; k < 3; k++) v[k] = sigma * normal(rng);
                 add_body(s, mesh_id, m, mp, false, density, geo_eps, mu, x, q, v, dt);
             }
-    if (!pending.empty()) {
-        std::vector<Tree> trees;
-        if (!build_trees_parallel(pending, 55u, trees, err)) return false;
-        for (size_t k = 0; k < trees.size(); k++)
-            if (scene_add_tree(s, trees[k], pending[k].nf()) != (int)k + 1) {
-                if (err) *err = "mesh numbering";
-                return false;
-            }
-    }
+    return finish_trees(s, meshes, o, tree_rng, err);
     return true;
 }
 

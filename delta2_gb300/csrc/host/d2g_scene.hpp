@@ -84,8 +84,18 @@ struct SceneOpts {
     double mu = 0;
     int hull_points = 64;
     int count = 0;  // > 0: bodies only in the first `count` grid cells
+    std::string tree_file;  // non-empty: load the trees from this file, or build and save them there
 };
 bool make_scene(const SceneOpts& o, Scene& s, std::string* err);
+
+// Flattened trees of a scene's meshes and the versioned binary file they are
+// saved to (d2g_treefile.cpp).
+struct TreeSet {
+    std::vector<int32_t> mesh_node_off, mesh_ntris, nodes, ntris;
+    std::vector<double> tris, eps, inner_eps;
+};
+bool save_trees(const TreeSet& t, const char* path, std::string* err);
+bool load_trees(const char* path, TreeSet& t, std::string* err);
 
 // Adds one mesh (tree built with rng) and returns its mesh id.
 int scene_add_mesh(Scene& s, const Mesh& m, Pcg32& tree_rng, std::string* err);

@@ -93,7 +93,22 @@ typedef struct d2g_scene_opts {
     double mu;          /* 0 = default */
     int32_t hull_points;
     int32_t count;      /* > 0: only the first `count` grid cells get a body */
+    const char* tree_file; /* non-null: load the trees from this tree file when it
+                              exists (d2g_trees_load's format, checked against the
+                              meshes), else build them and save them there */
 } d2g_scene_opts;
+
+/* Tree files (no reference counterpart: the reference builds its trees when
+ * it loads a mesh).  A versioned little-endian binary file of d2g_trees'
+ * arrays plus each mesh's triangle count (the sum of its leaf buckets), with
+ * a checksum; loading checks the structure (offsets, child links inside
+ * their mesh, at most 8 triangles per bucket). */
+typedef struct d2g_tree_file d2g_tree_file;
+int d2g_trees_save(const d2g_trees* trees, const char* path);
+int d2g_trees_load(const char* path, d2g_tree_file** out);
+/* Pointers into the loaded file's storage (valid until d2g_tree_file_free). */
+int d2g_tree_file_view(d2g_tree_file* f, d2g_trees* trees);
+void d2g_tree_file_free(d2g_tree_file* f);
 
 typedef struct d2g_scene d2g_scene;
 int d2g_scene_make(const d2g_scene_opts* opts, d2g_scene** out);

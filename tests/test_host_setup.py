@@ -179,3 +179,44 @@ def test_open_box_scene_and_parallel_trees():
     assert np.array_equal(a.tris, b.tris) and np.array_equal(a.nodes, b.nodes)
     lo, hi = a.local_aabb[0, :3], a.local_aabb[0, 3:]
     assert np.allclose(hi[:2] - lo[:2], 40.0) and np.isclose(hi[2] - lo[2], 20.0)
+
+
+def test_tree_file_round_trip(tmp_path):
+    # the versioned tree file stores the flattened trees exactly
+    s = D.make_scene(3)
+    path = tmp_path / "trees.bin"
+    D.save_trees(s, path)
+    t = D.load_trees(path)
+    for f in ["mesh_node_off", "nodes", "ntris", "tris", "eps", "inner_eps"]:
+        assert np.array_equal(np.asarray(t[f]), np.asarray(getattr(s, f))), f
+
+
+def test_scene_tree_file_builds_then_loads(tmp_path):
+    # the first call builds the trees and writes the file, the second loads
+    # it; both scenes are the same, field by field
+    path = str(tmp_path / "c5.trees")
+    a = D.make_scene(5, nx=2, ny=2, nz=1, tree_file=path)
+    assert os.path.exists(path)
+    b = D.make_scene(5, nx=2, ny=2, nz=1, tree_file=path)
+    c = D.make_scene(5, nx=2, ny=2, nz=1)
+    for f in ["mesh_node_off", "nodes", "ntris", "tris", "eps", "inner_eps", "mesh", "cur", "mass"]:
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        assert np.array_equal(getattr(a, f), getattr(c, f)), f
+
+
+def test_tree_file_rejects_corruption_and_other_meshes(tmp_path):
+    path = tmp_path / "t.bin"
+    D.save_trees(D.make_scene(1, nx=2, ny=1, nz=1), path)
+    raw = bytearray(path.read_bytes())
+    raw[-3] ^= 0x40  # a payload byte
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(D.D2GError, match="checksum"):
+        D.load_trees(bad)
+    short = tmp_path / "short.bin"
+    short.write_bytes(path.read_bytes()[:100])
+    with pytest.raises(D.D2GError):
+        D.load_trees(short)
+    # trees of the 2-cube scene do not fit the mixed scene's meshes
+    with pytest.raises(D.D2GError):
+        D.make_scene(3, tree_file=str(path))
