@@ -275,6 +275,14 @@ def make_scene(config=2, nx=0, ny=0, nz=0, spacing=0.0, speed_sigma=-1.0, seed=0
     h = C.c_void_p()
     _check(L.d2g_scene_make(C.byref(o), C.byref(h)))
     try:
+        return _scene_view(L, h, config)
+    finally:
+        L.d2g_scene_free(h)
+
+
+def _scene_view(L, h, config):
+    """Scene object with copies of a d2g_scene handle's arrays."""
+    if True:
         t = Trees()
         b = Bodies()
         aabb = F32P()
@@ -308,8 +316,77 @@ def make_scene(config=2, nx=0, ny=0, nz=0, spacing=0.0, speed_sigma=-1.0, seed=0
         s.gravity_z = float(gz.value)
         s.config = config
         return s
-    finally:
-        L.d2g_scene_free(h)
+
+
+def load_obj(path):
+    """Vertices [n][3] and triangles [m][3] (0-based) of a Wavefront OBJ file
+    (v and f records; polygons are split into fans; v/vt/vn index forms and
+    negative indices are read; everything else is ignored), as the
+    reference's mesh import does (model/mesh.cpp:9-21, igl::readOBJ)."""
+    V, F = [], []
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if not parts:
+                continue
+            if parts[0] == "v" and len(parts) >= 4:
+                V.append([float(x) for x in parts[1:4]])
+            elif parts[0] == "f" and len(parts) >= 4:
+                idx = []
+                for tok in parts[1:]:
+                    k = int(tok.split("/")[0])
+                    idx.append(k - 1 if k > 0 else len(V) + k)
+                for j in range(1, len(idx) - 1):
+                    F.append([idx[0], idx[j], idx[j + 1]])
+    V = np.asarray(V, dtype=np.float64).reshape(-1, 3)
+    F = np.asarray(F, dtype=np.int32).reshape(-1, 3)
+    if len(F) and (F.min() < 0 or F.max() >= len(V)):
+        raise ValueError(f"{path}: face index out of range")
+    return V, F
+
+
+class SceneBuilder:
+    """A scene of the caller's meshes and bodies (d2g_scene_create):
+
+        b = SceneBuilder(dt=1/240)
+        box, com = b.add_mesh(*load_obj("box.obj"), surface=True)
+        b.add_body(box, position=com, static=True)
+        rock, _ = b.add_mesh(V, F)
+        b.add_body(rock, position=(0, 0, 2), velocity=(0, 0, -1))
+        scene = b.finish()
+
+    Meshes are centred at their centre of mass (add_mesh returns it)."""
+
+    def __init__(self, dt=0.01, gravity_z=-9.8):
+        self.h = C.c_void_p()
+        _check(lib().d2g_scene_create(C.c_float(dt), C.c_double(gravity_z), C.byref(self.h)))
+
+    def add_mesh(self, V, F, surface=False):
+        V = np.ascontiguousarray(V, dtype=np.float64).reshape(-1, 3)
+        F = np.ascontiguousarray(F, dtype=np.int32).reshape(-1, 3)
+        com = np.zeros(3)
+        mid = C.c_int32()
+        _check(lib().d2g_scene_add_mesh(self.h, _p(V, F64P), len(V), _p(F, I32P), len(F), int(bool(surface)),
+                                        _p(com, F64P), C.byref(mid)))
+        return mid.value, com
+
+    def add_body(self, mesh_id, position=(0, 0, 0), quaternion=(1, 0, 0, 0), velocity=(0, 0, 0), static=False,
+                 density=1000.0, geo_eps=0.01, mu=0.5):
+        x = np.ascontiguousarray(position, dtype=np.float64)
+        q = np.ascontiguousarray(quaternion, dtype=np.float64)
+        v = np.ascontiguousarray(velocity, dtype=np.float64)
+        _check(lib().d2g_scene_add_body(self.h, int(mesh_id), int(bool(static)), C.c_double(density),
+                                        C.c_double(geo_eps), C.c_double(mu), _p(x, F64P), _p(q, F64P),
+                                        _p(v, F64P)))
+
+    def finish(self):
+        L = lib()
+        _check(L.d2g_scene_finish(self.h))
+        try:
+            return _scene_view(L, self.h, 0)
+        finally:
+            L.d2g_scene_free(self.h)
+            self.h = None
 
 
 def build_tree(V, F, rng_state=None):

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -28,6 +29,7 @@ using d2g::set_error;
 
 struct d2g_scene {
     d2g::Scene s;
+    std::unique_ptr<d2g::SceneBuilder> b;  // a scene of the caller's meshes, until finished
 };
 
 namespace {
@@ -125,6 +127,66 @@ int d2g_scene_make(const d2g_scene_opts* o, d2g_scene** out) {
 
 void d2g_scene_free(d2g_scene* s) { delete s; }
 
+int d2g_scene_create(float dt, double gravity_z, d2g_scene** out) {
+    if (!out || !(dt > 0.0f)) {
+        set_error("null argument or non-positive time step");
+        return D2G_ERR_INVALID;
+    }
+    d2g_scene* sc = new d2g_scene();
+    sc->b.reset(new d2g::SceneBuilder());
+    sc->b->s.opt_dt = dt;
+    sc->b->s.gravity_z = gravity_z;
+    *out = sc;
+    return D2G_OK;
+}
+
+int d2g_scene_add_mesh(d2g_scene* sc, const double* vertices, int32_t n_vertices, const int32_t* faces,
+                       int32_t n_faces, int32_t surface, double* com, int32_t* mesh_id) {
+    if (!sc || !sc->b || !com || !mesh_id) {
+        set_error(sc && !sc->b ? "the scene is finished" : "null argument");
+        return D2G_ERR_INVALID;
+    }
+    std::string err;
+    const int id = d2g::builder_add_mesh(*sc->b, vertices, n_vertices, faces, n_faces, surface != 0, com, &err);
+    if (id < 0) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    *mesh_id = id;
+    return D2G_OK;
+}
+
+int d2g_scene_add_body(d2g_scene* sc, int32_t mesh_id, int32_t is_static, double density, double geo_eps, double mu,
+                       const double* position, const double* quaternion, const double* velocity) {
+    if (!sc || !sc->b) {
+        set_error(sc ? "the scene is finished" : "null scene");
+        return D2G_ERR_INVALID;
+    }
+    std::string err;
+    if (!d2g::builder_add_body(*sc->b, mesh_id, is_static != 0, density, geo_eps, mu, position, quaternion, velocity,
+                               &err)) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    return D2G_OK;
+}
+
+int d2g_scene_finish(d2g_scene* sc) {
+    if (!sc) {
+        set_error("null scene");
+        return D2G_ERR_INVALID;
+    }
+    if (!sc->b) return D2G_OK;
+    std::string err;
+    if (!d2g::builder_finish(*sc->b, &err)) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    sc->s = std::move(sc->b->s);
+    sc->b.reset();
+    return D2G_OK;
+}
+
 struct d2g_tree_file {
     d2g::TreeSet t;
 };
@@ -198,6 +260,10 @@ int d2g_scene_view(d2g_scene* sc, d2g_trees* t, d2g_bodies* b, const float** loc
                    double* gravity_z) {
     if (!sc) {
         set_error("null scene");
+        return D2G_ERR_INVALID;
+    }
+    if (sc->b) {
+        set_error("the scene is still being built: call d2g_scene_finish first");
         return D2G_ERR_INVALID;
     }
     d2g::Scene& s = sc->s;
@@ -586,6 +652,7 @@ int d2g_ctx_set_level_budget(d2g_ctx* c, int64_t bytes) {
         return D2G_ERR_INVALID;
     }
     c->eng.level_budget = bytes;
+    c->eng.ccd_chunk = c->eng.np_chunk = 0;  // sizes learned under the old budget
     return D2G_OK;
 }
 

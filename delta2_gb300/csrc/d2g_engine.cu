@@ -1517,12 +1517,17 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     if (n_pairs > 0)
         D2G_CUDA(cudaMemcpyAsync(E.roots.p, E.soup.p, sizeof(Entry) * n_pairs, cudaMemcpyDeviceToDevice, s));
     const double budget = level_budget(ctx);
-    int chunk = n_pairs;
+    // start from the chunk size that fitted last time (abandoning a chunk
+    // wastes its finished levels), growing it when the last call used under
+    // a third of the budget
+    int chunk = E.ccd_chunk > 0 ? std::min(n_pairs, E.ccd_chunk) : n_pairs;
+    double peak = 0.0;  // largest level need / budget among finished chunks
     for (int p0 = 0; p0 < n_pairs;) {
     const int p1 = std::min(n_pairs, p0 + chunk);
     const int rec_start = n_rec;
     int64_t k_node = 0, k_tri = 0, k_leaf = 0, k_levels = 0;
     bool abandon = false;
+    double chunk_peak = 0.0;
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n_soup = p1 - p0, n_conn = 0;
     while (n_soup > 0 || n_conn > 0) {
@@ -1530,6 +1535,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             abandon = true;
             break;
         }
+        chunk_peak = std::max(chunk_peak, 64.0 * 8.0 * 1.5 * n_soup / budget);
         k_levels++;
         k_node += n_soup + n_conn;
         k_leaf += n_conn;
@@ -1565,6 +1571,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             abandon = true;
             break;
         }
+        chunk_peak = std::max(chunk_peak, 1.5 * 1900.0 * ((double)K + (double)P) / budget);
         k_tri += (int64_t)K + 15 * (int64_t)P;
         // (2) all primitive tests of the level
         RC(E.items.ensure(K + 1));
@@ -1700,6 +1707,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     c_tri += k_tri;
     c_leaf += k_leaf;
     c_levels += k_levels;
+    peak = std::max(peak, chunk_peak);
     if (sink) {  // the chunk's records, sorted by pair, go to the consumer and are dropped
         RC(finish_records(ctx, p1 - p0, n_rec, p0));
         RC(sink->consume(ctx, sink->user, p0, p1));
@@ -1708,6 +1716,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     }
     p0 = p1;
     }
+    if (n_pairs > 0) E.ccd_chunk = chunk >= n_pairs ? 0 : (peak < 1.0 / 3.0 ? 2 * chunk : chunk);
     if (!sink) RC(finish_records(ctx, n_pairs, n_rec));
     if (n_pairs > 0) {
         RC(E.last_pair.ensure(ctx->n_bodies + 1));
@@ -1748,13 +1757,15 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     if (n_pairs > 0)
         D2G_CUDA(cudaMemcpyAsync(E.roots.p, E.soup.p, sizeof(Entry) * n_pairs, cudaMemcpyDeviceToDevice, s));
     const double budget = level_budget(ctx);
-    int chunk = n_pairs;
+    int chunk = E.np_chunk > 0 ? std::min(n_pairs, E.np_chunk) : n_pairs;  // as in run_ccd
+    double peak = 0.0;
     for (int p0 = 0; p0 < n_pairs;) {
     const int p1 = std::min(n_pairs, p0 + chunk);
     const int rec_start = n_rec;
     const int32_t tri_start = (int32_t)c_tri;  // the device counter's value before this chunk
     int64_t k_node = 0, k_levels = 0;
     bool abandon = false;
+    double chunk_peak = 0.0;
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n = p1 - p0;
     while (n > 0) {
@@ -1762,6 +1773,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
             abandon = true;
             break;
         }
+        chunk_peak = std::max(chunk_peak, 1.5 * 110.0 * 64.0 * n / budget);
         k_levels++;
         k_node += n;
         const int n_slots = 64 * n;
@@ -1832,8 +1844,10 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     }
     c_node += k_node;
     c_levels += k_levels;
+    peak = std::max(peak, chunk_peak);
     p0 = p1;
     }
+    if (n_pairs > 0) E.np_chunk = chunk >= n_pairs ? 0 : (peak < 1.0 / 3.0 ? 2 * chunk : chunk);
     RC(finish_records(ctx, n_pairs, n_rec));
     D2G_CUDA(cudaGetLastError());
     *n_out = n_rec;

@@ -197,6 +197,7 @@ struct Engine {
     DBuf<Entry> roots;
     long long level_budget = 0;
     size_t device_bytes = 0;
+    int ccd_chunk = 0, np_chunk = 0;  // pair-chunk sizes that fitted the budget last time (0: whole calls)
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
     int tune[D2G_TUNE_KEYS] = {2, 256};
   // cub_tmp2: scans on the context's second stream

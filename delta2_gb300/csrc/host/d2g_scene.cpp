@@ -836,6 +836,72 @@ static bool file_exists(const std::string& path) {
     return true;
 }
 
+// ------------------------------------------- scenes of the caller's meshes --
+// Meshes are centred at their centre of mass (model/mesh.cpp:77) with the
+// volume mass model of a closed surface or the surface model of a thin shell
+// (model/mesh.cpp:93-130, thickness 0.01); bodies as Particle's constructor
+// sets them up (model/particle.cpp:7-40); the trees are built at the end from
+// one PCG32 stream seeded (42, 54), in mesh order.
+int builder_add_mesh(SceneBuilder& b, const double* V, int nv, const int32_t* F, int nf, bool surface, double* com,
+                     std::string* err) {
+    if (b.finished || !V || !F || nv < 3 || nf < 1) {
+        if (err) *err = b.finished ? "scene already finished" : "a mesh needs 3 vertices and a face";
+        return -1;
+    }
+    Mesh m;
+    m.V.assign(V, V + 3 * (size_t)nv);
+    m.F.assign(F, F + 3 * (size_t)nf);
+    for (int32_t f : m.F)
+        if (f < 0 || f >= nv) {
+            if (err) *err = "face index out of range";
+            return -1;
+        }
+    for (double x : m.V)
+        if (!std::isfinite(x)) {
+            if (err) *err = "non-finite vertex";
+            return -1;
+        }
+    MassProps mp = surface ? mass_surface(m, 0.01) : mass_volume(m);
+    if (!(mp.volume > 0.0) || !std::isfinite(mp.volume)) {
+        if (err) *err = surface ? "the surface has no area" : "the mesh encloses no volume (open or inside out)";
+        return -1;
+    }
+    for (int k = 0; k < 3; k++) com[k] = mp.com[k];
+    shift_vertices(m, mp.com);
+    mp.com[0] = mp.com[1] = mp.com[2] = 0.0;
+    b.meshes.push_back(m);
+    b.mass.push_back(mp);
+    return (int)b.meshes.size() - 1;
+}
+
+bool builder_add_body(SceneBuilder& b, int mesh, bool is_static, double density, double geo_eps, double mu,
+                      const double* x, const double* q, const double* v, std::string* err) {
+    if (b.finished || mesh < 0 || mesh >= (int)b.meshes.size() || !x || !q || !v) {
+        if (err) *err = b.finished ? "scene already finished" : "unknown mesh or null argument";
+        return false;
+    }
+    if (!(density > 0.0) || !(geo_eps >= 0.0) || !(mu >= 0.0) || !(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] > 0.0)) {
+        if (err) *err = "density must be positive, geo_eps and mu non-negative, the quaternion non-zero";
+        return false;
+    }
+    add_body(b.s, mesh, b.meshes[mesh], b.mass[mesh], is_static, density, geo_eps, mu, x, q, v, b.s.opt_dt);
+    return true;
+}
+
+bool builder_finish(SceneBuilder& b, std::string* err) {
+    if (b.finished) return true;
+    if (b.s.n_bodies() == 0) {
+        if (err) *err = "a scene needs a body";
+        return false;
+    }
+    Pcg32 tree_rng;
+    tree_rng.seed(42u, 54u);  // common/cli_options.h:45
+    for (const Mesh& m : b.meshes)
+        if (scene_add_mesh(b.s, m, tree_rng, err) < 0) return false;
+    b.finished = true;
+    return true;
+}
+
 // The trees of every mesh, in creation order: loaded from o.tree_file when
 // it exists (checked against the meshes' triangle counts), else built and,
 // with a tree_file, saved there.  Meshes draw from one PCG32 stream in order,

@@ -88,6 +88,20 @@ struct SceneOpts {
 };
 bool make_scene(const SceneOpts& o, Scene& s, std::string* err);
 
+// A scene of the caller's meshes and bodies (d2g_scene_create and friends).
+struct SceneBuilder {
+    Scene s;
+    std::vector<Mesh> meshes;
+    std::vector<MassProps> mass;
+    bool finished = false;
+};
+// Returns the mesh id (and the centre of mass it was centred at), or -1.
+int builder_add_mesh(SceneBuilder& b, const double* V, int nv, const int32_t* F, int nf, bool surface, double* com,
+                     std::string* err);
+bool builder_add_body(SceneBuilder& b, int mesh, bool is_static, double density, double geo_eps, double mu,
+                      const double* x, const double* q, const double* v, std::string* err);
+bool builder_finish(SceneBuilder& b, std::string* err);
+
 // Flattened trees of a scene's meshes and the versioned binary file they are
 // saved to (d2g_treefile.cpp).
 struct TreeSet {

@@ -116,6 +116,21 @@ void d2g_scene_free(d2g_scene* s);
 /* Pointers into the scene's own storage (valid until d2g_scene_free). */
 int d2g_scene_view(d2g_scene* s, d2g_trees* trees, d2g_bodies* bodies, const float** local_aabb, float* opt_dt,
                    double* gravity_z);
+
+/* Scenes of the caller's meshes and bodies: the reference's mesh loading
+ * and particle set-up (model/mesh.cpp:9-130: meshes centred at their centre
+ * of mass, volume mass model of a closed surface or, with surface != 0, the
+ * thin-shell surface model used for static planes; model/particle.cpp:7-40).
+ * d2g_scene_add_mesh returns the mesh id and the centre of mass it centred
+ * the mesh at (world position = body position + rotated local vertex).
+ * d2g_scene_finish builds the trees (one PCG32 stream seeded (42, 54), in
+ * mesh order); d2g_scene_view then works as for d2g_scene_make. */
+int d2g_scene_create(float dt, double gravity_z, d2g_scene** out);
+int d2g_scene_add_mesh(d2g_scene* s, const double* vertices, int32_t n_vertices, const int32_t* faces,
+                       int32_t n_faces, int32_t surface, double* com, int32_t* mesh_id);
+int d2g_scene_add_body(d2g_scene* s, int32_t mesh_id, int32_t is_static, double density, double geo_eps, double mu,
+                       const double* position, const double* quaternion, const double* velocity);
+int d2g_scene_finish(d2g_scene* s);
 /* Build one mesh's surrogate tree from a triangle mesh, drawing from the PCG32
  * stream (state, inc) in rng[2] (updated).  Sizes first, then a second call
  * with buffers: nodes [n][4] (child_first local to this mesh), ntris, tris

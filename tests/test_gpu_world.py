@@ -272,3 +272,23 @@ def test_world_chunked_matches_oracle(ctx):
     finally:
         ctx.set_level_budget(0)
     assert st["np_contacts"] > 0
+
+
+def test_world_obj_scene_matches_oracle(ctx, tmp_path):
+    # a scene of the caller's meshes: three OBJ cubes dropped onto an OBJ plane
+    from tests.test_host_setup import CUBE_F, CUBE_V, _write_obj
+
+    _write_obj(tmp_path / "cube.obj", [[0.4 * c for c in v] for v in CUBE_V], CUBE_F)
+    _write_obj(tmp_path / "plane.obj", [[20, 20, 0], [20, -20, 0], [-20, 20, 0], [-20, -20, 0]],
+               [[0, 2, 1], [1, 2, 3]])
+    b = D.SceneBuilder(dt=1 / 120)
+    plane, _ = b.add_mesh(*D.load_obj(tmp_path / "plane.obj"), surface=True)
+    cube, _ = b.add_mesh(*D.load_obj(tmp_path / "cube.obj"))
+    b.add_body(plane, static=True, geo_eps=0.1)
+    s2 = np.sqrt(0.5)
+    for k, (x, z) in enumerate([(0.0, 0.6), (0.5, 1.6), (-0.4, 2.7)]):
+        b.add_body(cube, position=(x, 0.1 * k, z), quaternion=(s2, s2, 0, 0) if k == 1 else (1, 0, 0, 0),
+                   velocity=(0, 0, -0.5), geo_eps=0.1)
+    s = b.finish()
+    st = run_world(ctx, s, 80)
+    assert st["np_contacts"] > 0

@@ -220,3 +220,56 @@ def test_tree_file_rejects_corruption_and_other_meshes(tmp_path):
     # trees of the 2-cube scene do not fit the mixed scene's meshes
     with pytest.raises(D.D2GError):
         D.make_scene(3, tree_file=str(path))
+
+
+CUBE_V = [[1, 1, 1], [1, 1, -1], [1, -1, 1], [1, -1, -1], [-1, 1, 1], [-1, 1, -1], [-1, -1, 1], [-1, -1, -1]]
+CUBE_F = [[0, 2, 1], [1, 2, 3], [2, 6, 3], [3, 6, 7], [4, 5, 6], [5, 7, 6], [4, 0, 1], [4, 1, 5], [0, 4, 6],
+          [0, 6, 2], [3, 7, 1], [7, 5, 1]]
+
+
+def _write_obj(path, V, F, quads=()):
+    with open(path, "w") as f:
+        f.write("# test mesh\no m\n")
+        for v in V:
+            f.write("v %r %r %r\n" % tuple(v))
+        f.write("vt 0 0\nvn 0 0 1\n")
+        for t in F:
+            f.write("f %d/1/1 %d//1 %d\n" % tuple(k + 1 for k in t))
+        for q in quads:
+            f.write("f " + " ".join(str(k - len(V)) for k in q) + "\n")  # negative (relative) indices
+
+
+def test_obj_loader(tmp_path):
+    p = tmp_path / "m.obj"
+    _write_obj(p, [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], [[0, 1, 2]], quads=[[0, 1, 2, 3]])
+    V, F = D.load_obj(p)
+    assert V.shape == (4, 3) and F.tolist() == [[0, 1, 2], [0, 1, 2], [0, 2, 3]]
+
+
+def test_scene_builder_reproduces_the_cube_scene(tmp_path):
+    # the 1-cube configuration rebuilt from OBJ files: ground plane (surface
+    # mass model) and a unit cube (volume model), same bodies, same trees
+    ref = D.make_scene(1, nx=1, ny=1, nz=1)
+    _write_obj(tmp_path / "cube.obj", [[0.5 * c for c in v] for v in CUBE_V], CUBE_F)
+    _write_obj(tmp_path / "plane.obj", [[50, 50, 0], [50, -50, 0], [-50, 50, 0], [-50, -50, 0]], [[0, 2, 1], [1, 2, 3]])
+    b = D.SceneBuilder(dt=ref.opt_dt, gravity_z=ref.gravity_z)
+    plane, pcom = b.add_mesh(*D.load_obj(tmp_path / "plane.obj"), surface=True)
+    cube, ccom = b.add_mesh(*D.load_obj(tmp_path / "cube.obj"))
+    assert np.allclose(pcom, 0) and np.allclose(ccom, 0)
+    b.add_body(plane, static=True, density=1000.0, geo_eps=ref.geo_eps[0], mu=ref.mu[0])
+    b.add_body(cube, position=ref.cur[1, 8:11], quaternion=ref.cur[1, 1:5], velocity=ref.cur[1, 11:14],
+               density=1000.0, geo_eps=ref.geo_eps[1], mu=ref.mu[1])
+    got = b.finish()
+    for f in ["mesh_node_off", "nodes", "ntris", "tris", "eps", "inner_eps", "mesh", "is_static", "geo_eps", "mu",
+              "mass", "inv_inertia", "last", "cur", "fut", "last_dt", "bounding_radius", "local_aabb"]:
+        assert np.array_equal(getattr(got, f), getattr(ref, f)), f
+
+
+def test_scene_builder_rejects_invalid_meshes():
+    b = D.SceneBuilder()
+    with pytest.raises(D.D2GError, match="no volume"):
+        b.add_mesh([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]])  # open surface
+    with pytest.raises(D.D2GError, match="out of range"):
+        b.add_mesh([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 5]])
+    with pytest.raises(D.D2GError):
+        b.finish()  # no body
