@@ -1528,6 +1528,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     int64_t k_node = 0, k_tri = 0, k_leaf = 0, k_levels = 0;
     bool abandon = false;
     double chunk_peak = 0.0;
+    RC(E.soup.ensure((size_t)(p1 - p0) + 1));  // the frontiers swap every level: this one may be the smaller
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n_soup = p1 - p0, n_conn = 0;
     while (n_soup > 0 || n_conn > 0) {
@@ -1766,6 +1767,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     int64_t k_node = 0, k_levels = 0;
     bool abandon = false;
     double chunk_peak = 0.0;
+    RC(E.soup.ensure((size_t)(p1 - p0) + 1));  // the frontiers swap every level: this one may be the smaller
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n = p1 - p0;
     while (n > 0) {
