@@ -234,9 +234,9 @@ def test_world_noisy_icospheres_in_open_box(ctx):
     assert np.isfinite(got.cur).all()
 
 
-def test_world_cube_pile_grid_solve(ctx):
-    # the 64-cube configuration: one cluster whose contacts grow past the
-    # threshold where the solve runs as a cooperative grid over the SMs
+def test_world_cube_pile(ctx):
+    # the 64-cube configuration: the bodies land and pile into one cluster
+    # with hundreds of contacts (one block solves it: 65 parts)
     s = D.make_scene(1)
     st = run_world(ctx, s, 100)
     assert st["np_contacts"] > 0
