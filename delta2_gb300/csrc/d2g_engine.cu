@@ -1532,7 +1532,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n_soup = p1 - p0, n_conn = 0;
     while (n_soup > 0 || n_conn > 0) {
-        if (64.0 * 8.0 * 1.5 * n_soup > budget && p1 - p0 > 1) {
+        // past the budget, or past 32-bit slot indices (64 slots per node pair)
+        if ((64.0 * 8.0 * 1.5 * n_soup > budget || 64LL * n_soup > (long long)INT32_MAX / 2) && p1 - p0 > 1) {
             abandon = true;
             break;
         }
@@ -1563,6 +1564,10 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         RC(read_scalars(ctx, src1, 2, tot1));
         const int K = tot1[0], P = tot1[1];  // soup triangle pairs, leaf-pair triangle pairs
         if (15LL * K + 15LL * P > (long long)INT32_MAX) {  // test indices are 32-bit
+            if (p1 - p0 > 1) {
+                abandon = true;
+                break;
+            }
             set_error("CCD level with " + std::to_string(K) + " + " + std::to_string(P) +
                       " triangle pairs exceeds the 32-bit test index range");
             return D2G_ERR_INVALID;
@@ -1771,7 +1776,7 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     D2G_CUDA(cudaMemcpyAsync(E.soup.p, E.roots.p + p0, sizeof(Entry) * (p1 - p0), cudaMemcpyDeviceToDevice, s));
     int n = p1 - p0;
     while (n > 0) {
-        if (1.5 * 110.0 * 64.0 * n > budget && p1 - p0 > 1) {
+        if ((1.5 * 110.0 * 64.0 * n > budget || 64LL * n > (long long)INT32_MAX / 2) && p1 - p0 > 1) {
             abandon = true;
             break;
         }
