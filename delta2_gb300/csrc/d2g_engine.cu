@@ -863,11 +863,13 @@ __global__ void __launch_bounds__(kBlock) k_ee_rest4(EeArgs a) {
 }
 
 // triTriCCDLinear's sequential (dist, toc) selection over its 15 sub-tests
-// (continuous_comparison.h:682-778), then the soup hit test (:817).
+// (continuous_comparison.h:682-778), then the soup hit test (:817) and the
+// final-contact flag (a hit between two leaves, as k_final_flags sets it).
 __global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entry* __restrict__ soup,
                             const PrimResult* __restrict__ sub, const float* __restrict__ search,
                             PrimResult* __restrict__ res, int32_t* __restrict__ hit,
-                            int32_t* __restrict__ entry_hits) {
+                            int32_t* __restrict__ entry_hits, const int4* __restrict__ nodes,
+                            int32_t* __restrict__ flags) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     PrimResult best;
@@ -885,6 +887,7 @@ __global__ void k_soup_fold(int K, const int32_t* __restrict__ items, const Entr
     const int h = best.dist < (double)search[e.pair] ? 1 : 0;
     hit[k] = h;
     if (h) atomicAdd(&entry_hits[slot >> 6], 1);
+    flags[k] = (h && !ld_node(nodes, e.na).z && !ld_node(nodes, e.nb).z) ? 1 : 0;
 }
 
 // ----------------------------------------------------------- discrete -----
@@ -1668,8 +1671,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         }
         // (3) soup fold and finals, leaf-pair finals, expansion; one synchronisation
         if (K > 0) {
-            LAUNCH(k_soup_fold, K, K, E.items.p, E.soup.p, E.sub.p, E.search.p, E.res.p, E.hit.p, E.entry_hits.p);
-            LAUNCH(k_final_flags, K, K, E.items.p, E.soup.p, ctx->nodes.p, E.hit.p, E.flags.p);
+            LAUNCH(k_soup_fold, K, K, E.items.p, E.soup.p, E.sub.p, E.search.p, E.res.p, E.hit.p, E.entry_hits.p,
+                   ctx->nodes.p, E.flags.p);
         }
         RC(scan2(ctx, E.flags.p, E.flag_off.p, K, E.chit.p, E.cflag_off.p, 15 * P));
         RC(E.cnt_a.ensure(n_soup + 1));
