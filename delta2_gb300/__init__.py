@@ -428,8 +428,9 @@ def broad_phase(scene):
 
 
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
-TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS = range(2)
-TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS}
+TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES = range(3)
+TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS,
+              "solve_lanes": TUNE_SOLVE_LANES}
 TUNE_NAMES_INV = {v: k for k, v in TUNE_NAMES.items()}
 
 

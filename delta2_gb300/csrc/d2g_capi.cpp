@@ -638,7 +638,8 @@ int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
         set_error("null context or unknown tuning key");
         return D2G_ERR_INVALID;
     }
-    if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10)) {
+    if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10) ||
+        (key == D2G_TUNE_SOLVE_LANES && value != 0 && value != 4 && value != 16)) {
         set_error("tuning value out of range");
         return D2G_ERR_INVALID;
     }

@@ -29,33 +29,39 @@
 
 namespace d2g {
 
-D2G_HD double m_kernel_sin(double r) {
-    const double z = r * r;
-    double p = -8.22063524662433e-18;
-    p = 2.8114572543455206e-15 + z * p;
-    p = -7.647163731819816e-13 + z * p;
-    p = 1.6059043836821613e-10 + z * p;
-    p = -2.505210838544172e-08 + z * p;
-    p = 2.7557319223985893e-06 + z * p;
-    p = -0.0001984126984126984 + z * p;
-    p = 0.008333333333333333 + z * p;
-    p = -0.16666666666666666 + z * p;
-    return r + (r * z) * p;
+// Horner coefficients, highest order first, of sin(r) = r + r z S(z) and
+// cos(r) = 1 + z C(z), z = r^2.
+D2G_HD double m_sincos_coef(int i, bool cosine) {
+    switch (i) {
+        case 0: return cosine ? -1.5619206968586225e-16 : -8.22063524662433e-18;
+        case 1: return cosine ? 4.779477332387385e-14 : 2.8114572543455206e-15;
+        case 2: return cosine ? -1.1470745597729725e-11 : -7.647163731819816e-13;
+        case 3: return cosine ? 2.08767569878681e-09 : 1.6059043836821613e-10;
+        case 4: return cosine ? -2.755731922398589e-07 : -2.505210838544172e-08;
+        case 5: return cosine ? 2.48015873015873e-05 : 2.7557319223985893e-06;
+        case 6: return cosine ? -0.001388888888888889 : -0.0001984126984126984;
+        case 7: return cosine ? 0.041666666666666664 : 0.008333333333333333;
+        default: return cosine ? -0.5 : -0.16666666666666666;
+    }
 }
 
-D2G_HD double m_kernel_cos(double r) {
+// The sine (cosine = false) or cosine series on the reduced argument r.  One
+// instruction stream for both: lanes of a warp may evaluate different ones.
+D2G_HD double m_kernel_sincos(double r, bool cosine) {
     const double z = r * r;
-    double p = -1.5619206968586225e-16;
-    p = 4.779477332387385e-14 + z * p;
-    p = -1.1470745597729725e-11 + z * p;
-    p = 2.08767569878681e-09 + z * p;
-    p = -2.755731922398589e-07 + z * p;
-    p = 2.48015873015873e-05 + z * p;
-    p = -0.001388888888888889 + z * p;
-    p = 0.041666666666666664 + z * p;
-    p = -0.5 + z * p;
-    return 1.0 + z * p;
+    double p = m_sincos_coef(0, cosine);
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+    for (int i = 1; i < 9; i++) p = m_sincos_coef(i, cosine) + z * p;
+    const double a = cosine ? z : r * z;
+    const double b = cosine ? 1.0 : r;
+    return b + a * p;  // sin: r + (r z) S, cos: 1 + z C
 }
+
+D2G_HD double m_kernel_sin(double r) { return m_kernel_sincos(r, false); }
+
+D2G_HD double m_kernel_cos(double r) { return m_kernel_sincos(r, true); }
 
 // x = k*pi/2 + r, |r| <= pi/4 (for |x| <= pi/4 no reduction).
 D2G_HD void m_reduce(double x, double& r, int& q) {

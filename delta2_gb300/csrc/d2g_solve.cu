@@ -269,7 +269,167 @@ struct SolveArgs {
     int32_t* out_ab;
     const int32_t* con_pair;
     double* pair_warm;
+    int lanes;  // normal-loop lanes per contact: 0 = by wave width, 4 or 16
 };
+
+// One wave of the normal loop with sixteen lanes per contact: lane bit 0
+// picks the body side (A, B) and bit 1 the integrated state (FS, FSf) as in
+// the four-lane form, bits 2-3 a component (x, y, z of the vectors and rows
+// of the matrices; the fourth lane carries the quaternions' w).  Every value
+// is the four-lane form's, operation for operation: vector and matrix work
+// is spread over the component lanes and gathered with shuffles, the
+// d1 / v1 dot products run on the FS / FSf lanes and sin / cos of the
+// quaternion exponential on even / odd component lanes, which halves the
+// FP64 instructions of a contact's dependent chain.  Each warp takes two
+// contacts; warps are dealt to SMs first, then to the SMs' sub-partitions,
+// as in the four-lane form.
+__device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __restrict__ widx, int c0, int G,
+                                              int gb, double t, const SolveArgs& a) {
+    const int lane = threadIdx.x & 31;
+    const int side = lane & 1, variant = (lane >> 1) & 1, c = (lane >> 2) & 3;
+    const int cc = c < 3 ? c : 0;   // the w lane repeats component x in vector work
+    const int grp = lane & ~12;     // component 0 of this lane's (side, state)
+    const int s1 = grp | ((cc == 2 ? 0 : cc + 1) << 2), s2 = grp | ((cc == 0 ? 2 : cc - 1) << 2);
+    const int tasks = (n1 - n0 + 1) >> 1;
+    const int wslot = (int)(threadIdx.x >> 5) * G + gb, nwarps = (int)(blockDim.x >> 5) * G;
+    for (int task = wslot; task < tasks; task += nwarps) {
+        const int q = n0 + 2 * task + (lane >> 4);
+        const bool act = q < n1;
+        ConWork& C = a.cw[c0 + widx[act ? q : n0]];
+        const int g = side ? C.b : C.a;
+        BodyWork& W = a.bw[g];
+        const bool st = a.is_static[g];
+        // this side's contact point p1 = T_FS local and its velocity
+        // v1 = v + (ii L) x (p1 - x) (State::pointVelocity), component cc
+        const double* lp = side ? C.local_B : C.local_A;
+        const double* Tr = W.T_FS + 4 * cc;
+        const double p1 = ((Tr[0] * lp[0] + Tr[1] * lp[1]) + Tr[2] * lp[2]) + Tr[3] * 1.0;
+        const double* Ir = a.ii + 9 * (size_t)g + 3 * cc;
+        const double wv = (Ir[0] * W.FS[5] + Ir[1] * W.FS[6]) + Ir[2] * W.FS[7];
+        const double r = p1 - W.FS[8 + cc];
+        const double w1 = shfl_d(wv, s1), w2 = shfl_d(wv, s2), r1 = shfl_d(r, s1), r2 = shfl_d(r, s2);
+        const double v1s = W.FS[11 + cc] + (w1 * r2 - w2 * r1);
+        const double pA = shfl_d(p1, lane & ~1), pB = shfl_d(p1, lane | 1);
+        const double vA = shfl_d(v1s, lane & ~1), vB = shfl_d(v1s, lane | 1);
+        // d1 = n.p1B - n.p1A on the FS lanes, v1 = n.v1A - n.v1B on the FSf lanes
+        const double ncc = C.n[cc];
+        const double PX = (variant ? vA : pB) * ncc, PY = (variant ? vB : pA) * ncc;
+        const double dd = ((shfl_d(PX, grp) + shfl_d(PX, grp | 4)) + shfl_d(PX, grp | 8)) -
+                          ((shfl_d(PY, grp) + shfl_d(PY, grp | 4)) + shfl_d(PY, grp | 8));
+        const double d1 = shfl_d(dd, lane & ~2), v1 = shfl_d(dd, lane | 2);
+        const double outer = C.outer, m = C.mass_eff, damp = 0.1;
+        const double imp0 = C.impulse, off0 = C.impulse_offset;
+        const double dimp = d1 < outer ? (v1 * m) * damp : -imp0;
+        const double imp1 = dmax(imp0 + dimp, 0.0);
+        const double u = (-ncc) * (imp1 - imp0);
+        const double lower_slop = dmax(outer * 0.2, outer - C.start_dist);
+        const double slop = lerp1(lower_slop, outer * 0.2, 0.3);
+        const double pen = outer - d1;
+        const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -off0;
+        const double off1 = dmax(off0 + doff, 0.0);
+        const double uo = (-ncc) * (off1 - off0);
+        // this side's impulse sums after the contact: imp + us,
+        // rimp + (-us) x (p1 - x), ioff + uso (us, uso: u, uo or their negatives)
+        const double us = side ? -u : u;
+        const double nus = -us;
+        const double imp = W.imp[cc] + us;
+        const double rimp = W.rimp[cc] + (shfl_d(nus, s1) * r2 - shfl_d(nus, s2) * r1);
+        const double ioff = W.ioff[cc] + (side ? -uo : uo);
+        // integrate_one on these sums, component cc
+        const double* F = a.fut + 14 * (size_t)g;
+        const double ms = a.mass[g];
+        const double im = imp / ms;
+        const double vnew = F[11 + cc] + im;
+        const double xa = F[8 + cc] + (ioff / ms) * t;
+        const double xb = xa + im * t;
+        const double xnew = variant ? xb : xa;
+        const double Lnew = F[5 + cc] + rimp;
+        const double La = F[5 + cc] + t * W.roff[cc];
+        const double Lb = La + t * rimp;
+        const double Ls = variant ? Lb : La;
+        const double* Ii = W.Iinv + 3 * cc;
+        const double om = (Ii[0] * shfl_d(Ls, grp) + Ii[1] * shfl_d(Ls, grp | 4)) + Ii[2] * shfl_d(Ls, grp | 8);
+        const double d = (0.5 * om) * t;
+        // qexp(d) = (cos |d|, (d / |d|) sin |d|), the identity for |d| = 0
+        const double dq = d * d;
+        const double nrm = sqrt((shfl_d(dq, grp) + shfl_d(dq, grp | 4)) + shfl_d(dq, grp | 8));
+        const bool finite_arg = (nrm < 0.0 ? -nrm : nrm) < 1e9;
+        double rr;
+        int qd;
+        m_reduce(finite_arg ? nrm : 0.0, rr, qd);
+        const double kk = m_kernel_sincos(rr, (c & 1) != 0);
+        const double ks = shfl_d(kk, grp), kc = shfl_d(kk, grp | 4);
+        double sn = qd == 0 ? ks : (qd == 1 ? kc : (qd == 2 ? -ks : -kc));  // m_sin
+        double cs = qd == 0 ? kc : (qd == 1 ? -ks : (qd == 2 ? -kc : ks));  // m_cos
+        if (!finite_arg) sn = cs = nrm - nrm;
+        const bool ident = nrm == 0.0;
+        const double ew = ident ? 1.0 : cs;
+        const double ev = ident ? 0.0 : (d / nrm) * sn;
+        // u.q = qmul(e, f.q), component c (w on the fourth lane):
+        // w = ((ew bw - ex bx) - ey by) - ez bz, x = ((ew bx + ex bw) + ey bz) - ez by, ...
+        const double ex = shfl_d(ev, grp), ey = shfl_d(ev, grp | 4), ez = shfl_d(ev, grp | 8);
+        const double fw = F[1], fx = F[2], fy = F[3], fz = F[4];
+        const bool wl = c == 3;
+        const double b1 = wl ? fw : (c == 0 ? fx : (c == 1 ? fy : fz));
+        const double a2 = wl ? ex : (c == 0 ? ex : (c == 1 ? ey : ez));
+        const double b2 = wl ? fx : fw;
+        const double a3 = wl ? ey : (c == 0 ? ey : (c == 1 ? ez : ex));
+        const double b3 = wl ? fy : (c == 0 ? fz : (c == 1 ? fx : fy));
+        const double a4 = wl ? ez : (c == 0 ? ez : (c == 1 ? ex : ey));
+        const double b4 = wl ? fz : (c == 0 ? fy : (c == 1 ? fz : fx));
+        const double P1 = ew * b1, P2 = a2 * b2, P3 = a3 * b3, P4 = a4 * b4;
+        const double qn = ((P1 + (wl ? -P2 : P2)) + (wl ? -P3 : P3)) - P4;
+        // rigid12 of the new state: row cc of R(q) (qmat), then x
+        const double qw = shfl_d(qn, grp | 12), qx = shfl_d(qn, grp), qy = shfl_d(qn, grp | 4),
+                     qz = shfl_d(qn, grp | 8);
+        const double tc = 2.0 * qn;
+        const double tx = shfl_d(tc, grp), ty = shfl_d(tc, grp | 4), tz = shfl_d(tc, grp | 8);
+        // row 0: 1 - (tyy + tzz), txy - twz, txz + twy
+        // row 1: txy + twz, 1 - (txx + tzz), tyz - twx
+        // row 2: txz - twy, tyz + twx, 1 - (txx + tyy)
+        const double Pd = (cc == 0 ? ty : tx) * (cc == 0 ? qy : qx);
+        const double Qd = (cc == 2 ? ty : tz) * (cc == 2 ? qy : qz);
+        const double A1 = (cc == 2 ? tz : ty) * qx;
+        const double B1 = (cc == 2 ? ty : tz) * qw;
+        const double A2 = tz * (cc == 0 ? qx : qy);
+        const double B2 = (cc == 0 ? ty : tx) * qw;
+        const double diag = 1.0 - (Pd + Qd);
+        const double o1 = A1 + (cc == 1 ? B1 : -B1);
+        const double o2 = A2 + (cc == 1 ? -B2 : B2);
+        __syncwarp();
+        if (act && variant == 0 && c < 3) {
+            if (!st) {
+                W.imp[c] = imp;
+                W.rimp[c] = rimp;
+                W.ioff[c] = ioff;
+            }
+            if (side == 0) {
+                if (C.spos >= 0) a.sdelta[3 * (size_t)(c0 + C.spos) + c] = a.is_static[C.a] ? u : -u;
+                if (c == 0) {
+                    C.impulse = imp1;
+                    C.impulse_offset = off1;
+                }
+            }
+        }
+        if (act && !st) {
+            double* S = variant ? W.FSf : W.FS;
+            double* T = (variant ? W.T_FSf : W.T_FS) + 4 * cc;
+            if (wl) {
+                S[1] = qn;
+            } else {
+                if (c == 0) S[0] = F[0];
+                S[2 + c] = qn;
+                S[5 + c] = Lnew;
+                S[8 + c] = xnew;
+                S[11 + c] = vnew;
+                T[c] = diag;
+                T[c == 0 ? 1 : 0] = o1;
+                T[c == 2 ? 1 : 2] = o2;
+                T[3] = xnew;
+            }
+        }
+    }
+}
 
 #define SYNC()                           \
     do {                                 \
@@ -459,6 +619,14 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
         SYNC();
         while (!converged && it_n < 1000) {
             for (int l = 0; l < levels; l++) {
+                // Narrow waves (a warp of two contacts per SM sub-partition)
+                // take sixteen lanes per contact, wider ones four.
+                const int wl = woff[l + 1] - woff[l];
+                if (a.lanes == 16 || (a.lanes == 0 && (wl + 1) / 2 <= 4 * G)) {
+                    normal_wave16(woff[l], woff[l + 1], widx, c0, G, gb, t, a);
+                    SYNC();
+                    continue;
+                }
                 // Four lanes per contact, one warp instruction stream: lane bit 0
                 // picks the body side (A, B), bit 1 the integrated state (FS,
                 // FSf).  FP64 latency, not lane count, bounds a wave, so the
@@ -825,6 +993,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
         a.out_ab = d_out_ab;
         a.con_pair = d_con_pair;
         a.pair_warm = d_pair_warm;
+        a.lanes = E.tune[D2G_TUNE_SOLVE_LANES];
         // A large cluster among few is solved by a cooperative grid over the
         // SMs; the others one block each.  A wave holds at most one contact
         // per moving body, so a cluster of at most D2G_TUNE_GRID_MIN_PARTS parts never

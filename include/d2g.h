@@ -182,11 +182,15 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
  *   D2G_TUNE_GRID_MIN_PARTS (default 256, >= 0): a cluster with at least 128
  *     contacts, among at most 8 clusters in a solve call, is solved by a
  *     cooperative grid over the SMs when it has more parts than this.
+ *   D2G_TUNE_SOLVE_LANES (default 0; 0, 4 or 16): lanes per contact in the
+ *     solve's normal-impulse waves; 0 takes sixteen for a wave narrow enough
+ *     that its warps each have an SM sub-partition to themselves, else four.
  * delta2_gb300/autotune.py measures candidate values on a workload and
  * writes them to a file that the Python layer applies. */
 #define D2G_TUNE_EE_FIRST_ITERS 0
 #define D2G_TUNE_GRID_MIN_PARTS 1
-#define D2G_TUNE_KEYS 2
+#define D2G_TUNE_SOLVE_LANES 2
+#define D2G_TUNE_KEYS 3
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Memory cap (no reference counterpart): the bytes one level of a tree

@@ -150,21 +150,30 @@ def solve_against_oracle(ctx, base, s, min_contacts=1):
     return clusters, hits
 
 
-def test_solve_matches_oracle(ctx):
-    # a state with many contacts: the cube scene after 120 oracle steps
+@pytest.mark.parametrize("lanes", [0, 4, 16])
+def test_solve_matches_oracle(ctx, lanes):
+    # a state with many contacts: the cube scene after 120 oracle steps; the
+    # normal-impulse waves on four or sixteen lanes per contact, or chosen by
+    # wave width
     s = D.make_scene(1, nx=2, ny=2, nz=2)
     w = O.World(s.copy(), s.opt_dt, s.gravity_z)
     w.step(120)
-    solve_against_oracle(ctx, w.get_bodies().copy(), s)
+    ctx.set_tuning(D.TUNE_SOLVE_LANES, lanes)
+    try:
+        solve_against_oracle(ctx, w.get_bodies().copy(), s)
+    finally:
+        ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
 
 
+@pytest.mark.parametrize("lanes", [4, 16])
 @pytest.mark.parametrize("grid_min_parts", [128, 1000000], ids=["grid", "block"])
-def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts):
+def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
     # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling
     # at 0.5 m/s: one cluster of 144 moving bodies with hundreds of contacts,
     # solved by the cooperative grid, or by one block when the part threshold
-    # is raised
+    # is raised, with four or sixteen lanes per contact
     ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, grid_min_parts)
+    ctx.set_tuning(D.TUNE_SOLVE_LANES, lanes)
     s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
     s.cur[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
     s.cur[1:, 10] = 0.51
@@ -175,6 +184,7 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts):
         clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
     finally:
         ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, 256)
+        ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
 
