@@ -141,6 +141,7 @@ struct BodyWork {
 struct ConWork {
     double local_A[3], local_B[3], n[3];
     double start_dist, mass_eff, outer, impulse, impulse_offset;
+    double slop, damp_m;  // per-solve constants of the normal loop: its slop and damp * mass_eff
     double last_fi[3], last_rot_A[3], last_rot_B[3], upd_total[3];
     int a, b, level, pair_cnt;
     int spos;  // position among the contacts touching a static body, -1 if none
@@ -204,6 +205,33 @@ struct SolveSync {
     int32_t* flags;       // grid: [0] fail, [1] levels, [2] static contacts, [3], [4] "moved" by parity, [5] spin error
 };
 
+__device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel_u32(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned int* p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier: after __syncthreads each block's thread 0 arrives with an
+// acquire-release add (releasing its block's writes); the last to arrive
+// has acquired every block's writes, resets the count and releases the next
+// generation, which the others wait for with acquire loads.  A block reads
+// the generation before it arrives, so the value cannot move before it.
 __device__ bool solve_sync(const SolveSync& S) {
     if (!S.grid) {
         __syncthreads();
@@ -213,15 +241,13 @@ __device__ bool solve_sync(const SolveSync& S) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned int my = atomicAdd(S.gen, 0u);
-        __threadfence();
-        if (atomicAdd(S.count, 1u) == gridDim.x - 1) {
-            atomicExch(S.count, 0u);
-            __threadfence();
-            atomicAdd(S.gen, 1u);
+        const unsigned int my = ld_relaxed_u32(S.gen);
+        if (atom_add_acq_rel_u32(S.count, 1u) == gridDim.x - 1) {
+            st_relaxed_u32(S.count, 0u);
+            st_release_u32(S.gen, my + 1u);
         } else {
             unsigned long long spins = 0;
-            while (((volatile unsigned int*)S.gen)[0] == my) {
+            while (ld_acquire_u32(S.gen) == my) {
                 if (++spins > (1ull << 25)) {  // several seconds: the other blocks are gone
                     atomicExch(S.flags + 5, 1);
                     ok = 0;
@@ -230,7 +256,6 @@ __device__ bool solve_sync(const SolveSync& S) {
                 __nanosleep(32);
             }
         }
-        __threadfence();
         s_ok = ok;
     }
     __syncthreads();
@@ -322,10 +347,8 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         const double dimp = d1 < outer ? (v1 * m) * damp : -imp0;
         const double imp1 = dmax(imp0 + dimp, 0.0);
         const double u = (-ncc) * (imp1 - imp0);
-        const double lower_slop = dmax(outer * 0.2, outer - C.start_dist);
-        const double slop = lerp1(lower_slop, outer * 0.2, 0.3);
         const double pen = outer - d1;
-        const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -off0;
+        const double doff = d1 < outer ? (C.damp_m * dmax(0.0, pen - C.slop)) / t : -off0;
         const double off1 = dmax(off0 + doff, 0.0);
         const double uo = (-ncc) * (off1 - off0);
         // this side's impulse sums after the contact: imp + us,
@@ -494,6 +517,10 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
         if (!is_static[C.b]) kn += 1.0 / mass[C.b] + quad_form(rnB, ii + 9 * (size_t)C.b);
         C.mass_eff = kn < 1e-6 ? 0.0 : 1.0 / kn;
         C.outer = (h[6] + h[7]) * 0.25;
+        // the normal loop's slop and damp * m (sequential_impulses.cpp:
+        // 260-287) depend on the contact alone
+        C.slop = lerp1(dmax(C.outer * 0.2, C.outer - C.start_dist), C.outer * 0.2, 0.3);
+        C.damp_m = 0.1 * C.mass_eff;
         C.impulse = warm[order[c0 + i]] == warm[order[c0 + i]] ? warm[order[c0 + i]] * 0.75 : 0.0;
         C.impulse_offset = 0.0;
         for (int q = 0; q < 3; q++) C.last_fi[q] = C.last_rot_A[q] = C.last_rot_B[q] = 0.0;
@@ -658,10 +685,8 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                     const double dimp = d1 < outer ? (v1 * m) * damp : -imp0;
                     const double imp1 = dmax(imp0 + dimp, 0.0);
                     const V3 u = (-n) * (imp1 - imp0);
-                    const double lower_slop = dmax(outer * 0.2, outer - C.start_dist);
-                    const double slop = lerp1(lower_slop, outer * 0.2, 0.3);
                     const double pen = outer - d1;
-                    const double doff = d1 < outer ? ((damp * m) * dmax(0.0, pen - slop)) / t : -off0;
+                    const double doff = d1 < outer ? (C.damp_m * dmax(0.0, pen - C.slop)) / t : -off0;
                     const double off1 = dmax(off0 + doff, 0.0);
                     const V3 uo = (-n) * (off1 - off0);
                     __syncwarp();
