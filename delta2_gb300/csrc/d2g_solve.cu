@@ -674,7 +674,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                     const V3 v1s = ld3(W.FS + 11) + cross(m3_vec(ii + 9 * (size_t)g, ld3(W.FS + 5)), p1 - x);
                     const V3 p1A = shfl3(p1, quad), p1B = shfl3(p1, quad + 1);
                     const V3 v1A = shfl3(v1s, quad), v1B = shfl3(v1s, quad + 1);
-                    const bool sa = is_static[C.a], sb = is_static[C.b];
+                    const bool sa = is_static[C.a];
                     const V3 n = ld3(C.n);
                     const double outer = C.outer;
                     const double d1 = dot(p1B, n) - dot(p1A, n);
