@@ -31,7 +31,7 @@ constexpr int kSolveBlock = 256;
 constexpr int kGridMinContacts = 128;  // a cluster this large may take a cooperative grid
 constexpr int kGridMaxClusters = 8;    // ... when the call has at most this many clusters
 // ... and it has more parts than the context's D2G_TUNE_GRID_MIN_PARTS (default
-// 256): its waves can be wider than one block takes at once
+// 64): its waves can be wider than one block runs at full rate
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -1021,9 +1021,10 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
         a.lanes = E.tune[D2G_TUNE_SOLVE_LANES];
         // A large cluster among few is solved by a cooperative grid over the
         // SMs; the others one block each.  A wave holds at most one contact
-        // per moving body, so a cluster of at most D2G_TUNE_GRID_MIN_PARTS parts never
-        // has waves much wider than the kSolveBlock / 4 contacts one block
-        // takes at once, and the grid would only add its barriers.
+        // per moving body; one block runs a wave of up to eight contacts at
+        // full rate (sixteen lanes each, one warp per SM sub-partition), so a
+        // cluster of more than D2G_TUNE_GRID_MIN_PARTS parts has waves wide
+        // enough to repay the grid barrier's ~3 us per wave.
         std::vector<int32_t> small, big;
         for (int c = 0; c < n_clusters; c++) {
             const int nck = h_con_off ? h_con_off[c + 1] - h_con_off[c] : 0;

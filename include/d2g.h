@@ -179,7 +179,7 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
  *   D2G_TUNE_EE_FIRST_ITERS (default 2, 0..10): Newton iterations an
  *     edge-edge CCD test runs on one lane before the tests still running
  *     continue on four lanes each.
- *   D2G_TUNE_GRID_MIN_PARTS (default 256, >= 0): a cluster with at least 128
+ *   D2G_TUNE_GRID_MIN_PARTS (default 64, >= 0): a cluster with at least 128
  *     contacts, among at most 8 clusters in a solve call, is solved by a
  *     cooperative grid over the SMs when it has more parts than this.
  *   D2G_TUNE_SOLVE_LANES (default 0; 0, 4 or 16): lanes per contact in the

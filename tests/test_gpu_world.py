@@ -172,6 +172,7 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
     # at 0.5 m/s: one cluster of 144 moving bodies with hundreds of contacts,
     # solved by the cooperative grid, or by one block when the part threshold
     # is raised, with four or sixteen lanes per contact
+    default = ctx.get_tuning(D.TUNE_GRID_MIN_PARTS)
     ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, grid_min_parts)
     ctx.set_tuning(D.TUNE_SOLVE_LANES, lanes)
     s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
@@ -183,7 +184,7 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
     try:
         clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
     finally:
-        ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, 256)
+        ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, default)
         ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
@@ -246,7 +247,8 @@ def test_world_noisy_icospheres_in_open_box(ctx):
 
 def test_world_cube_pile(ctx):
     # the 64-cube configuration: the bodies land and pile into one cluster
-    # with hundreds of contacts (one block solves it: 65 parts)
+    # with hundreds of contacts (65 parts: the cooperative grid solves it,
+    # above the default part threshold of 64)
     s = D.make_scene(1)
     st = run_world(ctx, s, 100)
     assert st["np_contacts"] > 0
