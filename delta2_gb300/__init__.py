@@ -370,6 +370,15 @@ class SceneBuilder:
                                         _p(com, F64P), C.byref(mid)))
         return mid.value, com
 
+    def add_obj(self, path, surface=False):
+        """add_mesh of a Wavefront OBJ file read by the library's own reader
+        (d2g_scene_add_obj; the same rules as load_obj)."""
+        com = np.zeros(3)
+        mid = C.c_int32()
+        _check(lib().d2g_scene_add_obj(self.h, os.fsencode(str(path)), int(bool(surface)), _p(com, F64P),
+                                       C.byref(mid)))
+        return mid.value, com
+
     def add_body(self, mesh_id, position=(0, 0, 0), quaternion=(1, 0, 0, 0), velocity=(0, 0, 0), static=False,
                  density=1000.0, geo_eps=0.01, mu=0.5):
         x = np.ascontiguousarray(position, dtype=np.float64)

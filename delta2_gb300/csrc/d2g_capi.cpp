@@ -156,6 +156,26 @@ int d2g_scene_add_mesh(d2g_scene* sc, const double* vertices, int32_t n_vertices
     return D2G_OK;
 }
 
+int d2g_scene_add_obj(d2g_scene* sc, const char* path, int32_t surface, double* com, int32_t* mesh_id) {
+    if (!sc || !sc->b || !path || !com || !mesh_id) {
+        set_error(sc && !sc->b ? "the scene is finished" : "null argument");
+        return D2G_ERR_INVALID;
+    }
+    std::vector<double> V;
+    std::vector<int32_t> F;
+    std::string err;
+    if (!d2g::read_obj(path, V, F, &err)) {
+        set_error(err);
+        return D2G_ERR_INVALID;
+    }
+    if (V.size() / 3 > (size_t)INT32_MAX || F.size() / 3 > (size_t)INT32_MAX) {
+        set_error("mesh too large");
+        return D2G_ERR_INVALID;
+    }
+    return d2g_scene_add_mesh(sc, V.data(), (int32_t)(V.size() / 3), F.data(), (int32_t)(F.size() / 3), surface, com,
+                              mesh_id);
+}
+
 int d2g_scene_add_body(d2g_scene* sc, int32_t mesh_id, int32_t is_static, double density, double geo_eps, double mu,
                        const double* position, const double* quaternion, const double* velocity) {
     if (!sc || !sc->b) {

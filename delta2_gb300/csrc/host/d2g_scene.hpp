@@ -101,6 +101,8 @@ int builder_add_mesh(SceneBuilder& b, const double* V, int nv, const int32_t* F,
 bool builder_add_body(SceneBuilder& b, int mesh, bool is_static, double density, double geo_eps, double mu,
                       const double* x, const double* q, const double* v, std::string* err);
 bool builder_finish(SceneBuilder& b, std::string* err);
+// Vertices [n][3] and triangles [m][3] of a Wavefront OBJ file (d2g_obj.cpp).
+bool read_obj(const char* path, std::vector<double>& V, std::vector<int32_t>& F, std::string* err);
 
 // Flattened trees of a scene's meshes and the versioned binary file they are
 // saved to (d2g_treefile.cpp).

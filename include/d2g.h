@@ -128,6 +128,12 @@ int d2g_scene_view(d2g_scene* s, d2g_trees* trees, d2g_bodies* bodies, const flo
 int d2g_scene_create(float dt, double gravity_z, d2g_scene** out);
 int d2g_scene_add_mesh(d2g_scene* s, const double* vertices, int32_t n_vertices, const int32_t* faces,
                        int32_t n_faces, int32_t surface, double* com, int32_t* mesh_id);
+/* Reads a Wavefront OBJ file (v records; f records of three or more vertex
+ * references, the first field of each v/vt/vn form, negative references
+ * counting back from the last vertex read; polygons split into fans) and
+ * adds it as d2g_scene_add_mesh does; the reference reads its meshes with
+ * igl::readOBJ (model/mesh.cpp:9-21). */
+int d2g_scene_add_obj(d2g_scene* s, const char* path, int32_t surface, double* com, int32_t* mesh_id);
 int d2g_scene_add_body(d2g_scene* s, int32_t mesh_id, int32_t is_static, double density, double geo_eps, double mu,
                        const double* position, const double* quaternion, const double* velocity);
 int d2g_scene_finish(d2g_scene* s);

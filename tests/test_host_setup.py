@@ -265,6 +265,66 @@ def test_scene_builder_reproduces_the_cube_scene(tmp_path):
         assert np.array_equal(getattr(got, f), getattr(ref, f)), f
 
 
+def test_native_obj_reader_matches_python_reader(tmp_path):
+    # d2g_scene_add_obj (the library's C++ reader) and load_obj + add_mesh
+    # give the same scene, array for array: triangles in v/vt/vn forms,
+    # quads and pentagons with negative references (fans), comments, CRLF
+    # line ends, records that are ignored
+    pent = tmp_path / "pent.obj"
+    with open(pent, "w", newline="") as f:
+        f.write("# prism with pentagonal caps\r\nmtllib none.mtl\r\n")
+        import math
+        for z in (0.0, 0.7):
+            for k in range(5):
+                a = 2 * math.pi * k / 5
+                f.write("v %r %r %r\r\n" % (math.cos(a), math.sin(a), z))
+        f.write("vt 0 0\r\nvn 0 0 1\r\ns off\r\n")
+        f.write("f 5 4 3 2 1\r\n")              # bottom cap, outward (-z)
+        f.write("f -5 -4 -3 -2 -1\r\n")         # top cap: vertices 6..10
+        for k in range(5):
+            a, b = k + 1, (k + 1) % 5 + 1
+            f.write("f %d/1/1 %d//1 %d/1 %d\r\n" % (a, b, b + 5, a + 5))
+    _write_obj(tmp_path / "cube.obj", [[0.5 * c for c in v] for v in CUBE_V], CUBE_F)
+    scenes = []
+    for native in (False, True):
+        b = D.SceneBuilder(dt=0.005)
+        ids = []
+        for name, surface in (("cube.obj", False), ("pent.obj", False), ("cube.obj", True)):
+            if native:
+                ids.append(b.add_obj(tmp_path / name, surface=surface))
+            else:
+                ids.append(b.add_mesh(*D.load_obj(tmp_path / name), surface=surface))
+        for k, (mid, com) in enumerate(ids):
+            b.add_body(mid, position=(3.0 * k, 0.0, 1.0 + k), static=(k == 2))
+        scenes.append((b.finish(), ids))
+    (a, ia), (n, inat) = scenes
+    for (m0, c0), (m1, c1) in zip(ia, inat):
+        assert m0 == m1 and np.array_equal(c0, c1)
+    for f in ["mesh_node_off", "nodes", "ntris", "tris", "eps", "inner_eps", "mesh", "is_static", "mass",
+              "inv_inertia", "cur", "bounding_radius", "local_aabb"]:
+        assert np.array_equal(getattr(a, f), getattr(n, f)), f
+    assert len(D.load_obj(pent)[1]) == 2 * 3 + 5 * 2
+
+
+def test_native_obj_reader_rejects_bad_files(tmp_path):
+    b = D.SceneBuilder()
+    with pytest.raises(D.D2GError, match="cannot open"):
+        b.add_obj(tmp_path / "missing.obj")
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 7\n")
+    with pytest.raises(D.D2GError, match="out of range"):
+        b.add_obj(bad)
+    bad.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 -4\n")
+    with pytest.raises(D.D2GError, match="out of range"):
+        b.add_obj(bad)
+    bad.write_text("v 0 0 x\n")
+    with pytest.raises(D.D2GError, match="bad vertex"):
+        b.add_obj(bad)
+    bad.write_text("v 0 0 0\nf 1 a 1\n")
+    with pytest.raises(D.D2GError, match="bad face"):
+        b.add_obj(bad)
+
+
 def test_scene_builder_rejects_invalid_meshes():
     b = D.SceneBuilder()
     with pytest.raises(D.D2GError, match="no volume"):
