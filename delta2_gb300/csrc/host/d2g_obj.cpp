@@ -34,14 +34,16 @@ void split_fields(const std::string& line, std::vector<std::string>& out) {
     }
 }
 
+// A whole field as a double (out-of-range magnitudes become +-inf or 0, as
+// Python's float() gives for the mirror reader).
 bool parse_double(const std::string& s, double* v) {
     if (s.empty()) return false;
     char* end = nullptr;
-    errno = 0;
     *v = std::strtod(s.c_str(), &end);
     return end && *end == '\0';
 }
 
+// A whole field as an integer that fits 64 bits.
 bool parse_int(const std::string& s, long long* v) {
     if (s.empty()) return false;
     char* end = nullptr;
