@@ -297,8 +297,11 @@ struct SolveArgs {
     int lanes;  // normal-loop lanes per contact: 0 = by wave width, 4 or 16
 };
 
-// One wave of the normal loop with sixteen lanes per contact: lane bit 0
-// picks the body side (A, B) and bit 1 the integrated state (FS, FSf) as in
+// One wave of the normal loop (sequential_impulses.cpp:239-378: per contact
+// the normal and offset impulses, then updateState :46-70 and
+// updateStateImmediate :72-96 of both bodies) with sixteen lanes per
+// contact: lane bit 0 picks the body side (A, B) and bit 1 the integrated
+// state (FS, FSf) as in
 // the four-lane form, bits 2-3 a component (x, y, z of the vectors and rows
 // of the matrices; the fourth lane carries the quaternions' w).  Every value
 // is the four-lane form's, operation for operation: vector and matrix work
