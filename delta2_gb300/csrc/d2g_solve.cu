@@ -301,9 +301,9 @@ struct SolveArgs {
 // the normal and offset impulses, then updateState :46-70 and
 // updateStateImmediate :72-96 of both bodies) with sixteen lanes per
 // contact: lane bit 0 picks the body side (A, B) and bit 1 the integrated
-// state (FS, FSf) as in
-// the four-lane form, bits 2-3 a component (x, y, z of the vectors and rows
-// of the matrices; the fourth lane carries the quaternions' w).  Every value
+// state (FS, FSf) as in the four-lane form, bits 2-3 a component (x, y, z
+// of the vectors and rows of the matrices; the fourth lane carries the
+// quaternions' w).  Every value
 // is the four-lane form's, operation for operation: vector and matrix work
 // is spread over the component lanes and gathered with shuffles, the
 // d1 / v1 dot products run on the FS / FSf lanes and sin / cos of the
