@@ -39,7 +39,7 @@ def _cuda_home():
 def _all_inputs():
     files = []
     for d, _, fs in os.walk(CSRC):
-        files += [os.path.join(d, f) for f in fs if f.endswith((".cu", ".cuh", ".cpp", ".hpp", ".h"))]
+        files += [os.path.join(d, f) for f in fs if f.endswith((".cu", ".cuh", ".cpp", ".hpp", ".h", ".map"))]
     files.append(os.path.join(ROOT, "include", "d2g.h"))
     files.append(os.path.abspath(__file__))
     return sorted(files)
@@ -90,7 +90,8 @@ def build(force=False, verbose=False):
                 print(o)
     objs = [j[j.index("-o") + 1] for j in jobs]
     tmp = LIB + ".tmp"
-    _run([nvcc, "-shared", ARCH, "-o", tmp] + objs + ["-Xcompiler=-fPIC,-pthread"])
+    _run([nvcc, "-shared", ARCH, "-o", tmp] + objs +
+         ["-Xcompiler=-fPIC,-pthread", "-Xlinker=--version-script=" + os.path.join(CSRC, "d2g.map")])
     os.replace(tmp, LIB)
     with open(stamp, "w") as f:
         f.write(fp)
