@@ -58,7 +58,7 @@ class DeviceScene(C.Structure):
                 ("geo_eps", C.c_void_p)]
 
 
-NOALLOC_MAX_PAIRS = 4096
+NOALLOC_MAX_PAIRS = 2048
 NOALLOC_MAX_NODE_PAIRS = 2048
 NOALLOC_MAX_CONTACTS = 32768
 
@@ -437,9 +437,9 @@ def broad_phase(scene):
 
 
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
-TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES = range(3)
+TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES, TUNE_SPIN_LIMIT = range(4)
 TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS,
-              "solve_lanes": TUNE_SOLVE_LANES}
+              "solve_lanes": TUNE_SOLVE_LANES, "spin_limit": TUNE_SPIN_LIMIT}
 TUNE_NAMES_INV = {v: k for k, v in TUNE_NAMES.items()}
 
 
@@ -691,6 +691,24 @@ class Context:
         return self._query(lambda cap, out, off, cnt: lib().d2g_compare_trees_full(
             self.h, _p(pairs, I32P), len(pairs), _p(out, F64P), cap, _p(off, I32P), _p(cnt, I64P)), len(pairs),
             capacity)
+
+    def find_contacts_bucket_comparison(self, a, b, node_pairs, capacity=None):
+        """findContactsBucketComparison: one level of body pair (a, b)'s discrete
+        traversal over node_pairs [n, 2] (global node ids) -> (hits [m, 14],
+        pair_used [n], the cumulative hit counts)."""
+        npairs = np.ascontiguousarray(node_pairs, dtype=np.int32).reshape(-1, 2)
+        cap = capacity if capacity is not None else 64 * len(npairs)
+        while True:
+            out = np.zeros((max(cap, 1), CONTACT_LEN))
+            used = np.zeros(max(1, len(npairs)), np.int32)
+            rc = lib().d2g_find_contacts_bucket_comparison(self.h, int(a), int(b), _p(npairs, I32P), len(npairs),
+                                                           _p(out, F64P), cap, _p(used, I32P))
+            total = int(used[len(npairs) - 1]) if len(npairs) else 0
+            if rc == 2 and capacity is None:
+                cap = total
+                continue
+            _check(rc)
+            return out[:total].copy(), used[:len(npairs)].copy()
 
     def compare_trees_full_continuous(self, pairs, max_time, capacity=None):
         """compareTreesFullContinuous for each pair over max_time[i]."""

@@ -659,7 +659,8 @@ int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
         return D2G_ERR_INVALID;
     }
     if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10) ||
-        (key == D2G_TUNE_SOLVE_LANES && value != 0 && value != 4 && value != 16)) {
+        (key == D2G_TUNE_SOLVE_LANES && value != 0 && value != 4 && value != 16) ||
+        (key == D2G_TUNE_SPIN_LIMIT && value < 1)) {
         set_error("tuning value out of range");
         return D2G_ERR_INVALID;
     }
@@ -737,6 +738,43 @@ int d2g_compare_trees_full(d2g_ctx* c, const int32_t* pairs, int32_t n_pairs, do
     int n_rec = 0;
     RC(d2g::run_narrowphase(c, c->eng.d_pairs.p, n_pairs, &n_rec, counters));
     return copy_out(c, n_pairs, n_rec, contacts, capacity, offsets);
+}
+
+int d2g_find_contacts_bucket_comparison(d2g_ctx* c, int32_t body_a, int32_t body_b, const int32_t* node_pairs,
+                                        int32_t n_node_pairs, double* hits, int32_t capacity, int32_t* pair_used) {
+    RC(check_ready(c));
+    const int32_t ab[2] = {body_a, body_b};
+    RC(check_pairs(c, ab, 1));
+    if (n_node_pairs < 0 || (n_node_pairs > 0 && (!node_pairs || !pair_used)) || capacity < 0 ||
+        (capacity > 0 && !hits) || n_node_pairs > (INT32_MAX >> 6)) {
+        set_error("invalid node pair list or output buffers");
+        return D2G_ERR_INVALID;
+    }
+    for (int i = 0; i < 2 * n_node_pairs; i++)
+        if (node_pairs[i] < 0 || node_pairs[i] >= c->n_nodes) {
+            set_error("node pair " + std::to_string(i / 2) + " names node " + std::to_string(node_pairs[i]) +
+                      " outside [0, " + std::to_string(c->n_nodes) + ")");
+            return D2G_ERR_INVALID;
+        }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    RC(upload(c, E.d_pairs, ab, 2));
+    RC(upload(c, E.bucket_nodes, node_pairs, 2 * (size_t)n_node_pairs));
+    int n_hits = 0;
+    RC(d2g::run_bucket_comparison(c, E.d_pairs.p, E.bucket_nodes.p, n_node_pairs, &n_hits));
+    if (n_node_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(pair_used, E.off_a.p + 1, sizeof(int32_t) * n_node_pairs, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    const int n_copy = std::min(n_hits, capacity);
+    if (n_copy > 0)
+        D2G_CUDA(cudaMemcpyAsync(hits, E.rec.p, sizeof(double) * 14 * (size_t)n_copy, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    if (n_hits > capacity) {
+        set_error("hit capacity " + std::to_string(capacity) + " < " + std::to_string(n_hits));
+        return D2G_CAPACITY;
+    }
+    return D2G_OK;
 }
 
 int d2g_compare_trees_full_continuous(d2g_ctx* c, const int32_t* pairs, const double* max_time, int32_t n_pairs,

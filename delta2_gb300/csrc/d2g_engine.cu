@@ -1064,6 +1064,17 @@ __global__ void __launch_bounds__(kBlock) k_np(int n_slots, const Entry* __restr
     hit[k] = h;
 }
 
+// Frontier entries of one body pair (pair index 0) from a list of node pairs.
+__global__ void k_bucket_entries(int n, const int32_t* __restrict__ node_pairs, Entry* __restrict__ front) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Entry e;
+    e.pair = 0;
+    e.na = node_pairs[2 * i];
+    e.nb = node_pairs[2 * i + 1];
+    front[i] = e;
+}
+
 // --------------------------------------------------- finals / expansion ----
 // Final-contact flag of each result: a hit inside a leaf-leaf node pair.
 // `slot_entry` maps a result to its entry: item >> 6 through `items` when
@@ -1870,30 +1881,103 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
     return D2G_OK;
 }
 
+// findContactsBucketComparison (comparison_dist.h:205-240) as the reference's
+// strategy interface issues it: one body pair, the node pairs of one level of
+// compareTreesFull (full_tree_comparison.h:25).  The level runs as a level of
+// run_narrowphase does (FP32 candidate bounds, then one FP64 triangle
+// distance per surviving slot), except that every hit is emitted, in slot
+// order, and the per-node-pair hit counts are summed into the reference's
+// cumulative pair_used_out.
+int run_bucket_comparison(d2g_ctx* ctx, const int32_t* d_pair, const int32_t* d_node_pairs, int n, int* n_hits) {
+    Engine& E = ctx->eng;
+    cudaStream_t s = ctx->stream;
+    RC(E.pm.ensure(33));
+    RC(E.search.ensure(2));
+    RC(E.pm32.ensure(25));
+    RC(E.roots.ensure(2));
+    RC(E.np_tri.ensure(1));
+    D2G_CUDA(cudaMemsetAsync(E.np_tri.p, 0, sizeof(int32_t), s));
+    LAUNCH(k_np_prep, 1, 1, d_pair, ctx->fut.p, ctx->mesh.p, ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p,
+           E.search.p, E.roots.p, E.pm32.p);
+    RC(E.soup.ensure(n + 1));
+    RC(E.off_a.ensure(n + 1));
+    RC(E.entry_hits.ensure(n + 1));
+    D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * (n + 1), s));
+    *n_hits = 0;
+    if (n == 0) {
+        D2G_CUDA(cudaMemsetAsync(E.off_a.p, 0, sizeof(int32_t), s));
+        return D2G_OK;
+    }
+    LAUNCH(k_bucket_entries, n, n, d_node_pairs, E.soup.p);
+    const int n_slots = 64 * n;
+    const int n_words = n_slots / 32;
+    DBuf<double>& res_eps = E.pfut;  // as in run_narrowphase
+    RC(E.res.ensure(n_slots));
+    RC(res_eps.ensure(4 * (size_t)n_slots));
+    RC(E.hit.ensure(n_slots));
+    RC(E.np_mask.ensure(n_words + 1));
+    RC(E.np_cnt.ensure(n_words + 1));
+    RC(E.np_off.ensure(n_words + 1));
+    RC(E.items.ensure(n_slots + 1));
+    LAUNCH(k_np_mask, n_slots, n_slots, E.soup.p, E.pm32.p, ctx->ntris.p, ctx->tri_sph.p, ctx->tri32.p,
+           ctx->eps_up.p, E.search.p, E.np_mask.p, E.np_cnt.p, E.np_tri.p, E.fp32_bounds ? 1 : 0);
+    RC(scan(ctx, E.np_cnt.p, E.np_off.p, n_words));
+    LAUNCH(k_np_items, n_slots, n_slots, E.np_mask.p, E.np_off.p, E.items.p);
+    int32_t n_items = 0;
+    {
+        const int32_t* src = E.np_off.p + n_words;
+        RC(read_scalars(ctx, &src, 1, &n_items));
+    }
+    if (n_items > 0) {
+        const int pf = prof_begin(ctx, PROF_NP, n_slots);
+        LAUNCH(k_np, n_items, n_items, E.soup.p, d_pair, E.pm.p, ctx->ntris.p, ctx->tris.p, ctx->eps.p,
+               ctx->inner_eps.p, ctx->geo_eps.p, E.search.p, E.res.p, res_eps.p, E.hit.p, E.entry_hits.p, E.items.p,
+               (const int32_t*)nullptr);
+        prof_end(ctx, pf);
+    }
+    RC(E.flag_off.ensure(n_items + 1));
+    RC(scan(ctx, E.hit.p, E.flag_off.p, n_items));
+    RC(scan(ctx, E.entry_hits.p, E.off_a.p, n));
+    int32_t tot = 0;
+    {
+        const int32_t* src = E.off_a.p + n;
+        RC(read_scalars(ctx, &src, 1, &tot));
+    }
+    RC(E.rec.ensure(14 * (size_t)tot + 14));
+    RC(E.rec_pair.ensure((size_t)tot + 1));
+    if (tot > 0)
+        LAUNCH(k_emit, n_items, n_items, E.hit.p, E.flag_off.p, E.items.p, 6, E.soup.p, (const int32_t*)nullptr, 0,
+               d_pair, E.res.p, res_eps.p, ctx->geo_eps.p, E.rec.p, E.rec_pair.p, 0);
+    D2G_CUDA(cudaGetLastError());
+    *n_hits = tot;
+    return D2G_OK;
+}
+
 }  // namespace d2g
 
 // ============================================================================
 // Allocation-free discrete narrow phase.
 //
-// For callers that may not allocate device memory while they run: code inside
-// a CUDA-graph capture (cudaMalloc is not capturable), a host that hands this
-// library a fixed memory budget up front (game or robotics loops with
-// real-time limits, where an allocation can stall or fail mid-frame), or an
-// embedding runtime that owns every allocation itself.  Every intermediate
+// For callers that may not allocate device memory while they run: a host that
+// hands this library a fixed memory budget up front (game or robotics loops
+// with real-time limits, where an allocation can stall or fail mid-frame), or
+// an embedding runtime that owns every allocation itself.  Every intermediate
 // buffer of the traversal is carved out of the file-scope array below, which
 // each GPU that loads this library holds until the process exits.
 //
-// Limits (checked before any work; larger requests are rejected with
-// D2G_ERR_INVALID and a message):
-//   body pairs per call          <= D2G_NOALLOC_MAX_PAIRS      (4096)
+// Limits (larger requests are rejected with D2G_ERR_INVALID and a message,
+// before the traversal or at the level that would pass them):
+//   body pairs per call          <= D2G_NOALLOC_MAX_PAIRS      (2048; each pair
+//                                   puts its root node pair in the first level)
 //   node pairs per tree level    <= D2G_NOALLOC_MAX_NODE_PAIRS (2048)
 //   contacts found per call      <= D2G_NOALLOC_MAX_CONTACTS   (32768)
 // All calls share the array and it keeps the previous call's contents: the
 // counters that must start at zero are cleared on every call, and two calls
 // whose work overlaps on the GPU (different streams, or different threads)
-// race on it.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress) and caches it; make that first call before any stream
-// capture.
+// race on it.  The call reads each level's sizes back to the host, so it
+// synchronizes its stream once per tree level and once at the end.  The first
+// call on a device looks up the array's device address (cudaGetSymbolAddress)
+// and caches it; make that first call before any stream capture.
 // ============================================================================
 namespace d2g {
 namespace {
@@ -2008,6 +2092,8 @@ extern "C" int d2g_compare_trees_full_noalloc(const d2g_device_scene* sc, const 
     void* base = nullptr;
     if (int rc = noalloc_base(&base)) return rc;
     const int MP = D2G_NOALLOC_MAX_PAIRS, MN = D2G_NOALLOC_MAX_NODE_PAIRS, MR = D2G_NOALLOC_MAX_CONTACTS;
+    static_assert(D2G_NOALLOC_MAX_PAIRS <= D2G_NOALLOC_MAX_NODE_PAIRS,
+                  "the first tree level holds one root node pair per body pair");
     Carve cv{(unsigned char*)base, 0, kNoAllocBytes};
     double* pm = cv.take<double>(32 * (size_t)MP);
     float* search = cv.take<float>(MP);

@@ -185,7 +185,7 @@ struct Engine {
     // results (processing order) and the sorted output
     DBuf<double> rec, rec_sorted;
     DBuf<int32_t> rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted, out_off, pair_cnt;
-    DBuf<int32_t> d_pairs;
+    DBuf<int32_t> d_pairs, bucket_nodes;
     DBuf<double> d_max_time;
     DBuf<uint8_t> cub_tmp, cub_tmp2;
     // phased edge-edge CCD (d2g_engine.cu)
@@ -199,7 +199,7 @@ struct Engine {
     size_t device_bytes = 0;
     int ccd_chunk = 0, np_chunk = 0;  // pair-chunk sizes that fitted the budget last time (0: whole calls)
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
-    int tune[D2G_TUNE_KEYS] = {2, 64, 0};
+    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25};
   // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing
@@ -272,6 +272,11 @@ struct CcdSink {
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters, const CcdSink* sink = nullptr);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
+// One level of one body pair's discrete traversal over the caller's node
+// pairs (d_pair: the pair's two bodies; d_node_pairs [n][2] global node ids):
+// every hit as a contact record in E.rec, the cumulative hit count after each
+// node pair in E.off_a[1 .. n].
+int run_bucket_comparison(d2g_ctx* ctx, const int32_t* d_pair, const int32_t* d_node_pairs, int n, int* n_hits);
 // Time-step selection (d2g_step.cu).
 // n_parts: particles of all clusters; max_cluster_parts: of the largest.
 int run_select_steps(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, const int32_t* d_cl_pair_off,

@@ -203,6 +203,7 @@ struct SolveSync {
     unsigned int* count;  // grid barrier arrivals
     unsigned int* gen;    // grid barrier generation
     int32_t* flags;       // grid: [0] fail, [1] levels, [2] static contacts, [3], [4] "moved" by parity, [5] spin error
+    unsigned int spin_limit;  // polls before a barrier wait gives up
 };
 
 __device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
@@ -246,9 +247,9 @@ __device__ bool solve_sync(const SolveSync& S) {
             st_relaxed_u32(S.count, 0u);
             st_release_u32(S.gen, my + 1u);
         } else {
-            unsigned long long spins = 0;
+            unsigned int spins = 0;
             while (ld_acquire_u32(S.gen) == my) {
-                if (++spins > (1ull << 25)) {  // several seconds: the other blocks are gone
+                if (++spins > S.spin_limit) {  // several seconds at the default: the other blocks are gone
                     atomicExch(S.flags + 5, 1);
                     ok = 0;
                     break;
@@ -856,7 +857,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
 __global__ void __launch_bounds__(kSolveBlock) k_solve(int n_list, const int32_t* __restrict__ cl_list, SolveArgs a) {
     if ((int)blockIdx.x >= n_list) return;
     __shared__ int s_local[3];
-    const SolveSync S{false, nullptr, nullptr, nullptr};
+    const SolveSync S{false, nullptr, nullptr, nullptr, 0u};
     solve_body(cl_list ? cl_list[blockIdx.x] : (int)blockIdx.x, threadIdx.x, blockDim.x, 0, 1, s_local, S, a);
 }
 
@@ -1063,6 +1064,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
                 S.count = (unsigned int*)(E.sv_grid.p + 16 * b);
                 S.gen = (unsigned int*)(E.sv_grid.p + 16 * b + 1);
                 S.flags = E.sv_grid.p + 16 * b + 4;
+                S.spin_limit = (unsigned int)E.tune[D2G_TUNE_SPIN_LIMIT];
                 int k = big[b];
                 // about one warp of contacts per SM and wave: fewer blocks for
                 // smaller clusters keep the grid barriers cheap

@@ -191,12 +191,19 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
  *   D2G_TUNE_SOLVE_LANES (default 0; 0, 4 or 16): lanes per contact in the
  *     solve's normal-impulse waves; 0 takes sixteen for a wave narrow enough
  *     that its warps each have an SM sub-partition to themselves, else four.
+ *   D2G_TUNE_SPIN_LIMIT (default 33554432, >= 1): polls a block of the
+ *     cooperative-grid solve makes at a grid barrier before it gives up
+ *     (several seconds at the default); a call whose barrier gave up returns
+ *     D2G_SPIN_LIMIT and leaves that solve's future states unspecified, and
+ *     the context stays usable.  Unlike the settings above, a limit small
+ *     enough to be reached changes the outcome: it exists to bound the wait.
  * delta2_gb300/autotune.py measures candidate values on a workload and
  * writes them to a file that the Python layer applies. */
 #define D2G_TUNE_EE_FIRST_ITERS 0
 #define D2G_TUNE_GRID_MIN_PARTS 1
 #define D2G_TUNE_SOLVE_LANES 2
-#define D2G_TUNE_KEYS 3
+#define D2G_TUNE_SPIN_LIMIT 3
+#define D2G_TUNE_KEYS 4
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Memory cap (no reference counterpart): the bytes one level of a tree
@@ -226,6 +233,22 @@ int d2g_ctx_profile(d2g_ctx* ctx, int32_t kind, double* ms, int64_t* launches, i
  * Returns D2G_CAPACITY when the total exceeds capacity (offsets still valid). */
 int d2g_compare_trees_full(d2g_ctx* ctx, const int32_t* pairs, int32_t n_pairs, double* contacts,
                            int32_t capacity, int32_t* offsets, int64_t* counters);
+
+/* findContactsBucketComparison for one body pair and one level of its
+ * traversal: the reference's discrete detection strategy interface
+ * (strategies/contact_detection/contact_detection_strategy.h:11, implemented
+ * by ContactDetectionComparison, contact_detection_comparison.cpp:12-14 ->
+ * comparison_dist.h:205-240), which compareTreesFull calls once per level
+ * (full_tree_comparison.h:25).  node_pairs [n][2]: global node ids (a node of
+ * body_a's tree, a node of body_b's tree), the reference's DeferredCompare
+ * list.  Every (triangle of a's bucket, triangle of b's bucket) slot closer
+ * than float(geo_eps_a + geo_eps_b) + eps_i + eps_j at the bodies' device
+ * future states is a hit: hits [capacity][14] in the reference's order (node
+ * pair, a's triangle, b's triangle); pair_used [n] receives the reference's
+ * cumulative pair_used_out (hits of node pairs 0..i).  D2G_CAPACITY when the
+ * hits exceed capacity (pair_used still written). */
+int d2g_find_contacts_bucket_comparison(d2g_ctx* ctx, int32_t body_a, int32_t body_b, const int32_t* node_pairs,
+                                        int32_t n_node_pairs, double* hits, int32_t capacity, int32_t* pair_used);
 
 /* ------------------------------------------- continuous collision detection
  * compareTreesFullContinuous<double,8,8> for each pair over its max_time
@@ -363,24 +386,26 @@ int d2g_mlp_train(d2g_mlp* mlp, const float* features, const float* targets, int
 /* ------------------------------------ allocation-free discrete narrow phase
  * No counterpart in the reference.  The same compareTreesFull traversal and
  * contacts as d2g_compare_trees_full, for callers that may not allocate
- * device memory during the call: code that runs inside a CUDA-graph capture,
- * hosts with a fixed up-front memory budget (real-time game or robotics loops
- * where an allocation can stall or fail mid-frame), or embedding runtimes that
- * own every allocation.  It calls no cudaMalloc, cudaFree or allocating library
- * routine and needs no context: the caller passes the scene, pairs and output
- * buffers in device memory, and a stream.  Intermediate buffers live in one
- * file-scope device array of 24 MiB that every GPU loading this library holds
- * until the process exits.  Limits per call (larger requests fail with
- * D2G_ERR_INVALID before or during the traversal): */
-#define D2G_NOALLOC_MAX_PAIRS 4096       /* body pairs */
+ * device memory during the call: hosts with a fixed up-front memory budget
+ * (real-time game or robotics loops where an allocation can stall or fail
+ * mid-frame), or embedding runtimes that own every allocation.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine and needs no context:
+ * the caller passes the scene, pairs and output buffers in device memory, and
+ * a stream.  Intermediate buffers live in one file-scope device array of
+ * 24 MiB that every GPU loading this library holds until the process exits.
+ * Limits per call (larger requests fail with D2G_ERR_INVALID, before the
+ * traversal or at the tree level that would pass them): */
+#define D2G_NOALLOC_MAX_PAIRS 2048       /* body pairs (each puts one root node pair in the first level) */
 #define D2G_NOALLOC_MAX_NODE_PAIRS 2048  /* node pairs in one tree level */
 #define D2G_NOALLOC_MAX_CONTACTS 32768   /* contacts found */
 /* All calls share that array: counters are cleared on every call, and calls
- * whose GPU work overlaps (other streams or threads) race on it.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress) and
- * caches it: make that first call before any stream capture.  Returns
- * D2G_CAPACITY when the contacts exceed `capacity` (offsets and *n_contacts
- * are still written; contacts are not). */
+ * whose GPU work overlaps (other streams or threads) race on it.  The call
+ * reads each tree level's sizes back to the host, so it synchronizes the
+ * stream once per level and once at the end.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and caches it: make
+ * that first call before any stream capture.  Returns D2G_CAPACITY when the
+ * contacts exceed `capacity` (offsets and *n_contacts are still written;
+ * contacts are not). */
 typedef struct d2g_device_scene {
     int32_t n_meshes;
     int32_t n_nodes;

@@ -237,6 +237,29 @@ class Context {
             return d2g_compare_trees_full(c_, flat(pairs), (int32_t)pairs.size(), out, cap, off, nullptr);
         });
     }
+    // ContactDetectionStrategy::findContactsBucketComparison
+    // (strategies/contact_detection/contact_detection_strategy.h:11): one
+    // level of body pair (a, b)'s discrete traversal over node_pairs (global
+    // node ids), with the reference's outputs: hits in its order and the
+    // cumulative pair_used_out.
+    void findContactsBucketComparison(int32_t a, int32_t b, const std::vector<Pair>& node_pairs,
+                                      std::vector<Contact>& hits, std::vector<int>& pair_used_out) {
+        const int32_t n = (int32_t)node_pairs.size();
+        std::vector<int32_t> used((size_t)n + 1, 0);
+        int32_t cap = std::max<int32_t>(64, 64 * n);
+        std::vector<double> rec;
+        for (int attempt = 0; attempt < 2; attempt++) {
+            rec.assign((size_t)D2G_CONTACT_LEN * cap, 0.0);
+            const int rc = check(d2g_find_contacts_bucket_comparison(c_, a, b, flat(node_pairs), n, rec.data(), cap,
+                                                                     used.data()));
+            if (rc != D2G_CAPACITY) break;
+            cap = used[n - 1];
+        }
+        const int32_t total = n ? used[n - 1] : 0;
+        hits.clear();
+        for (int32_t k = 0; k < total; k++) hits.push_back(Contact::fromRecord(rec.data() + (size_t)D2G_CONTACT_LEN * k));
+        pair_used_out.assign(used.begin(), used.begin() + n);
+    }
     // compareTreesFullContinuous for each pair over max_time[i].
     PairContacts compareTreesFullContinuous(const std::vector<Pair>& pairs, const std::vector<double>& max_time) {
         if (max_time.size() != pairs.size()) throw Error(D2G_ERR_INVALID, "one max_time per pair");

@@ -448,4 +448,10 @@ int o_world_warm_get(o_world* W, int32_t* keys, double* vals, int cap) {
     return i;
 }
 
+// Replaces the warm-start store (a state taken from another run).
+void o_world_warm_set(o_world* W, const int32_t* keys, const double* vals, int n) {
+    W->w.warm.clear();
+    for (int i = 0; i < n; i++) W->w.warm[std::make_pair((int)keys[2 * i], (int)keys[2 * i + 1])] = vals[i];
+}
+
 }  // extern "C"

@@ -10,7 +10,8 @@ import numpy as np
 
 from . import build as _build
 
-_lib = None
+_libs = {}
+_kind = "checker"
 
 I32P = C.POINTER(C.c_int32)
 F64P = C.POINTER(C.c_double)
@@ -34,10 +35,20 @@ def _p(a, t):
     return a.ctypes.data_as(t)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = _build.build()
+def select_build(kind):
+    """Route every call of this module to one build of the oracle:
+    "checker" (the portable -O2 build the tests use, the default) or "fast"
+    (the host-tuned -O3 build the benchmark's CPU baselines time).  Both give
+    identical results."""
+    global _kind
+    assert kind in ("checker", "fast")
+    _kind = kind
+
+
+def lib(kind=None):
+    kind = kind or _kind
+    if kind not in _libs:
+        path = _build.build(fast=kind == "fast")
         L = C.CDLL(path)
         for name in ["o_sin", "o_cos", "o_acos", "o_log"]:
             getattr(L, name).restype = C.c_double
@@ -48,11 +59,11 @@ def lib():
         L.o_world_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_double]
         for name in ["o_world_destroy", "o_world_set_unstable_filter", "o_world_get_bodies", "o_world_set_bodies",
                      "o_world_step", "o_world_stats", "o_world_broad_phase", "o_world_select_dt", "o_world_solve",
-                     "o_world_warm_size", "o_world_warm_get"]:
+                     "o_world_warm_size", "o_world_warm_get", "o_world_warm_set"]:
             getattr(L, name).argtypes = None
         L.o_world_select_dt.restype = C.c_double
-        _lib = L
-    return _lib
+        _libs[kind] = L
+    return _libs[kind]
 
 
 def _d(a):
@@ -257,30 +268,31 @@ class World:
         self.scene = scene
         self.view = SceneView(scene)
         la = np.ascontiguousarray(scene.local_aabb, dtype=np.float32)
-        self.h = lib().o_world_create(C.byref(self.view.trees), C.byref(self.view.bodies), la.ctypes.data,
+        self.L = lib()  # the build this world lives in
+        self.h = self.L.o_world_create(C.byref(self.view.trees), C.byref(self.view.bodies), la.ctypes.data,
                                       C.c_float(opt_dt), C.c_double(gravity_z))
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().o_world_destroy(C.c_void_p(self.h))
+            self.L.o_world_destroy(C.c_void_p(self.h))
             self.h = None
 
     def step(self, n=1):
-        return lib().o_world_step(C.c_void_p(self.h), C.c_int(n))
+        return self.L.o_world_step(C.c_void_p(self.h), C.c_int(n))
 
     def get_bodies(self):
-        lib().o_world_get_bodies(C.c_void_p(self.h), C.byref(self.view.bodies))
+        self.L.o_world_get_bodies(C.c_void_p(self.h), C.byref(self.view.bodies))
         return self.scene
 
     def set_bodies(self):
-        lib().o_world_set_bodies(C.c_void_p(self.h), C.byref(self.view.bodies))
+        self.L.o_world_set_bodies(C.c_void_p(self.h), C.byref(self.view.bodies))
 
     def set_unstable_filter(self, u):
-        lib().o_world_set_unstable_filter(C.c_void_p(self.h), C.c_int(int(u)))
+        self.L.o_world_set_unstable_filter(C.c_void_p(self.h), C.c_int(int(u)))
 
     def stats(self):
         out = np.zeros(13, dtype=np.int64)
-        lib().o_world_stats(C.c_void_p(self.h), _p(out, I64P))
+        self.L.o_world_stats(C.c_void_p(self.h), _p(out, I64P))
         keys = ["ccd_pairs", "ccd_contacts", "np_pairs", "np_contacts", "solves", "failures", "normal_iters",
                 "friction_iters", "ccd_node_pairs", "ccd_tri_pairs", "ccd_leaf_pairs", "np_node_pairs",
                 "np_tri_pairs"]
@@ -288,27 +300,33 @@ class World:
 
     def broad_phase(self, cap=1 << 20):
         out = np.zeros((cap, 2), dtype=np.int32)
-        n = lib().o_world_broad_phase(C.c_void_p(self.h), _p(out, I32P), C.c_int(cap))
+        n = self.L.o_world_broad_phase(C.c_void_p(self.h), _p(out, I32P), C.c_int(cap))
         assert n >= 0
         return out[:n].copy()
 
     def select_dt(self, particles, interactions):
         p = np.ascontiguousarray(particles, dtype=np.int32)
         it = np.ascontiguousarray(interactions, dtype=np.int32).reshape(-1, 2)
-        return lib().o_world_select_dt(C.c_void_p(self.h), _p(p, I32P), C.c_int(len(p)), _p(it, I32P),
+        return self.L.o_world_select_dt(C.c_void_p(self.h), _p(p, I32P), C.c_int(len(p)), _p(it, I32P),
                                        C.c_int(len(it)))
 
     def solve(self, particles, step_size, contacts):
         p = np.ascontiguousarray(particles, dtype=np.int32)
         c = _d(contacts).reshape(-1, 14)
         iters = np.zeros(2, dtype=np.int32)
-        ok = lib().o_world_solve(C.c_void_p(self.h), _p(p, I32P), C.c_int(len(p)), C.c_double(step_size),
+        ok = self.L.o_world_solve(C.c_void_p(self.h), _p(p, I32P), C.c_int(len(p)), C.c_double(step_size),
                                  _p(c, F64P), C.c_int(len(c)), _p(iters, I32P))
         return bool(ok), iters
 
     def warm(self):
-        n = lib().o_world_warm_size(C.c_void_p(self.h))
+        n = self.L.o_world_warm_size(C.c_void_p(self.h))
         keys = np.zeros((max(n, 1), 2), dtype=np.int32)
         vals = np.zeros(max(n, 1))
-        m = lib().o_world_warm_get(C.c_void_p(self.h), _p(keys, I32P), _p(vals, F64P), C.c_int(n))
+        m = self.L.o_world_warm_get(C.c_void_p(self.h), _p(keys, I32P), _p(vals, F64P), C.c_int(n))
         return {(int(keys[i, 0]), int(keys[i, 1])): float(vals[i]) for i in range(m)}
+
+    def set_warm(self, warm):
+        """Replace the warm-start store by {(body a, body b): impulse}."""
+        keys = np.ascontiguousarray([k for k in warm], dtype=np.int32).reshape(-1, 2)
+        vals = np.ascontiguousarray([warm[k] for k in warm], dtype=np.float64)
+        self.L.o_world_warm_set(C.c_void_p(self.h), _p(keys, I32P), _p(vals, F64P), C.c_int(len(vals)))

@@ -97,6 +97,70 @@ def test_bucket_golden_on_gpu(ctx):
     assert len(f) == 1 and abs(f[0, 10] - 0.9) <= 0.9 * 1.1920929e-05
 
 
+def _next_level(nodes, level, used):
+    """compareTreesFull's expansion of one level (full_tree_comparison.h:26-64):
+    node pairs with new hits that are not leaf-leaf put the shallower inner
+    side's children (b on ties) into the next level, in order."""
+    nxt, last = [], 0
+    for (na, nb), u in zip(level, used):
+        if u > last:
+            a_in, b_in = nodes[na, 2] != 0, nodes[nb, 2] != 0
+            if a_in or b_in:
+                adv_a = a_in and (not b_in or nodes[na, 3] < nodes[nb, 3])
+                if adv_a:
+                    nxt += [(nodes[na, 0] + c, nb) for c in range(nodes[na, 1])]
+                else:
+                    nxt += [(na, nodes[nb, 0] + c) for c in range(nodes[nb, 1])]
+        last = u
+    return nxt
+
+
+def test_find_contacts_bucket_comparison_matches_oracle(ctx):
+    """The per-level strategy entry (ContactDetectionStrategy::
+    findContactsBucketComparison) against the oracle bit for bit: the
+    reference's pyramid/plane case (test_comparison.cpp:90-128: 8 hits, one
+    after filterContacts), then every level of two close hulls' traversal,
+    driven from the host the way compareTreesFull drives it."""
+    s = SmallScene()
+    m_pyr = s.add_leaf_mesh(tris_from(PYRAMID_V, PYRAMID_F))
+    V, F = plane_mesh(1.0)
+    m_pl = s.add_leaf_mesh(tris_from(V, F))
+    s.add_body(m_pyr, 0.01, cur=state(x=(0, 0, 1.0)), fut=state(x=(0, 0, 1.0)), is_static=True)
+    s.add_body(m_pl, 0.01, cur=state(x=(0, 0, 1.105)), fut=state(x=(0, 0, 1.105)))
+    sc = s.build().to_product()
+    ctx.set_scene(sc)
+    hits, used = ctx.find_contacts_bucket_comparison(0, 1, [[0, 1]])
+    ref, ref_used = O.bucket_comparison(sc, 0, 1, [[0, 1]])
+    assert used.tolist() == ref_used.tolist() == [8]
+    assert_bits_equal(hits, ref, "golden bucket hits")
+    assert len(O.filter_contacts(hits, 0.0)) == 1
+
+    hull = project_futures(D.make_scene(2, nx=2, ny=1, nz=1, spacing=1.02, speed_sigma=1.0, seed=4))
+    ctx.set_scene(hull.copy())
+    a, b = 1, 2
+    level = [(int(hull.mesh_node_off[hull.mesh[a]]), int(hull.mesh_node_off[hull.mesh[b]]))]
+    total, levels = 0, 0
+    while level:
+        hits, used = ctx.find_contacts_bucket_comparison(a, b, level)
+        ref, ref_used = O.bucket_comparison(hull, a, b, level)
+        assert used.tolist() == ref_used.tolist(), levels
+        assert_bits_equal(hits, ref, f"hull bucket hits, level {levels}")
+        total += len(hits)
+        levels += 1
+        level = _next_level(hull.nodes, level, used)
+    assert levels >= 3 and total > 0
+    # an empty level, an out-of-range node and a too-small buffer
+    hits, used = ctx.find_contacts_bucket_comparison(a, b, np.zeros((0, 2), np.int32))
+    assert len(hits) == 0 and len(used) == 0
+    with pytest.raises(D.D2GError, match="outside"):
+        ctx.find_contacts_bucket_comparison(a, b, [[0, len(hull.nodes)]])
+    first = [(int(hull.mesh_node_off[hull.mesh[a]]), int(hull.mesh_node_off[hull.mesh[b]]))]
+    n_first = len(ctx.find_contacts_bucket_comparison(a, b, first)[0])
+    if n_first > 1:
+        with pytest.raises(D.CapacityError):
+            ctx.find_contacts_bucket_comparison(a, b, first, capacity=1)
+
+
 def test_empty_and_invalid_pairs(ctx):
     s = D.make_scene(1, nx=2, ny=1, nz=1)
     ctx.set_scene(s)

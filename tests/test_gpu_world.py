@@ -175,12 +175,7 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
     default = ctx.get_tuning(D.TUNE_GRID_MIN_PARTS)
     ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, grid_min_parts)
     ctx.set_tuning(D.TUNE_SOLVE_LANES, lanes)
-    s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
-    s.cur[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
-    s.cur[1:, 10] = 0.51
-    s.cur[1:, 11:14] = [0.0, 0.0, -0.5]
-    s.fut[1:] = s.cur[1:]
-    s.last[1:] = s.cur[1:]
+    s = _wide_cluster_scene()
     try:
         clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
     finally:
@@ -188,6 +183,50 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
         ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
+
+
+def _wide_cluster_scene():
+    # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling at 0.5 m/s
+    s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
+    s.cur[1:, 1:5] = [1.0, 0.0, 0.0, 0.0]
+    s.cur[1:, 10] = 0.51
+    s.cur[1:, 11:14] = [0.0, 0.0, -0.5]
+    s.fut[1:] = s.cur[1:]
+    s.last[1:] = s.cur[1:]
+    return s
+
+
+def test_grid_barrier_wait_runs_out_then_the_context_recovers(ctx):
+    """The cooperative-grid solve's barrier waits are bounded.  With a limit
+    of one poll a block gives up at some barrier of the wide cluster's solve
+    (all blocks still arrive, so every wait ends): the call returns
+    D2G_SPIN_LIMIT.  The next solve on the same context, with the default
+    limit and the states uploaded again, matches the oracle bit for bit."""
+    s = _wide_cluster_scene()
+    pairs = D.broad_phase(s)
+    clusters = separate(pairs, s.is_static, s.n_bodies)
+    flat = np.array([p for _, inter in clusters for p in inter], dtype=np.int32).reshape(-1, 2)
+    raw, off = O.narrowphase(s, flat)[:2]
+    inputs, k = [], 0
+    for parts, inter in clusters:
+        h = np.concatenate([np.asarray(O.filter_contacts(raw[off[k + i]:off[k + i + 1]])).reshape(-1, 14)
+                            for i in range(len(inter))])
+        k += len(inter)
+        keys = [tuple(sorted((int(r[11]), int(r[12])))) for r in h]
+        inputs.append((parts, float(np.float32(s.opt_dt)), h, [keys.count(kk) for kk in keys],
+                       np.full(len(h), np.nan)))
+    assert max(len(h) for _, _, h, _, _ in inputs) >= 128
+    default = ctx.get_tuning(D.TUNE_SPIN_LIMIT)
+    assert default == 1 << 25
+    ctx.set_scene(s.copy())
+    ctx.set_tuning(D.TUNE_SPIN_LIMIT, 1)
+    try:
+        with pytest.raises(D.D2GError, match="grid barrier") as e:
+            ctx.solve_clusters(inputs, s.gravity_z)
+        assert e.value.code == 3  # D2G_SPIN_LIMIT
+    finally:
+        ctx.set_tuning(D.TUNE_SPIN_LIMIT, default)
+    solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
 
 
 def test_ee_first_iters_do_not_change_results(ctx):
