@@ -325,8 +325,8 @@ bool divide_and_fit(const std::vector<TriRec>& tris, const std::vector<int>& tri
                         }
                         if (ids_out[g].empty()) zero.push_back(g);
                     }
-                    const size_t moves = std::min(zero.size(), ids_out[largest].size() - 1);
-                    for (size_t z = 0; z < moves; z++) {
+                    // the reference's loop bound is re-evaluated as the largest group shrinks
+                    for (size_t z = 0; z < std::min(zero.size(), ids_out[largest].size() - 1); z++) {
                         const int zi = zero[z];
                         const int tri_i = ids_out[largest].back();
                         ids_out[zi].push_back(tri_i);

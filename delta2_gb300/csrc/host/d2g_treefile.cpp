@@ -7,7 +7,10 @@
 //
 // Layout, little-endian:
 //   char     magic[8]      "D2GTREES"
-//   uint32   version       1
+//   uint32   version       2 (version 1 files came from a builder whose
+//                          last-resort regrouping moved more triangles than
+//                          the reference's divideAndFit does; they are refused
+//                          so that a scene rebuilds its trees)
 //   uint32   endian        0x01020304
 //   uint32   n_meshes
 //   uint32   reserved      0
@@ -27,7 +30,7 @@ namespace d2g {
 namespace {
 
 constexpr char kMagic[8] = {'D', '2', 'G', 'T', 'R', 'E', 'E', 'S'};
-constexpr uint32_t kVersion = 1, kEndian = 0x01020304u;
+constexpr uint32_t kVersion = 2, kEndian = 0x01020304u;
 
 struct Header {
     char magic[8];

@@ -6,6 +6,7 @@
 
 #include "d2o_collide.hpp"
 #include "d2o_solve.hpp"
+#include "d2o_tree.hpp"
 
 using namespace d2o;
 
@@ -446,6 +447,44 @@ int o_world_warm_get(o_world* W, int32_t* keys, double* vals, int cap) {
         i++;
     }
     return i;
+}
+
+// SurrogateTree(V, F, opt) from the PCG32 stream (state, inc) in rng[2]
+// (updated): sizes first (buffers null), then a second call with buffers of
+// `capacity` nodes; layout as the library's d2g_tree_build.  Returns the node
+// count, or -1 when the reference would throw.
+int o_tree_build(const double* V, int nv, const int32_t* F, int nf, uint64_t* rng, int32_t* nodes, int32_t* ntris,
+                 double* tris, double* eps, double* inner_eps, int capacity) {
+    std::vector<Tri> T((size_t)nf);
+    for (int f = 0; f < nf; f++) {
+        V3 p[3];
+        for (int k = 0; k < 3; k++) {
+            const int v = F[3 * f + k];
+            if (v < 0 || v >= nv) return -1;
+            p[k] = V3{V[3 * v], V[3 * v + 1], V[3 * v + 2]};
+        }
+        T[f] = Tri{p[0], p[1], p[2]};
+    }
+    Pcg32 r;
+    r.state = rng[0];
+    r.inc = rng[1];
+    FlatTree out;
+    try {
+        out = build_surrogate_tree(T, r);
+    } catch (const std::exception&) {
+        return -1;
+    }
+    const int n = out.size();
+    if (nodes && n <= capacity) {
+        std::memcpy(nodes, out.nodes.data(), sizeof(int32_t) * 4 * (size_t)n);
+        std::memcpy(ntris, out.ntris.data(), sizeof(int32_t) * (size_t)n);
+        std::memcpy(tris, out.tris.data(), sizeof(double) * 72 * (size_t)n);
+        std::memcpy(eps, out.eps.data(), sizeof(double) * 8 * (size_t)n);
+        std::memcpy(inner_eps, out.inner_eps.data(), sizeof(double) * 8 * (size_t)n);
+        rng[0] = r.state;
+        rng[1] = r.inc;
+    }
+    return n;
 }
 
 // Replaces the warm-start store (a state taken from another run).

@@ -71,6 +71,28 @@ def _d(a):
 
 
 # ----------------------------------------------------------- primitives ---
+def build_tree(V, F, rng_state):
+    """SurrogateTree(V, F, opt) restated (oracle/d2o_tree.hpp) from the PCG32
+    stream rng_state = (state, inc) -> (nodes [n,4], ntris, tris [n,8,9], eps,
+    inner_eps, rng state after the build); layout as the library's."""
+    Vf = _d(V).reshape(-1, 3)
+    Ff = np.ascontiguousarray(F, dtype=np.int32).reshape(-1, 3)
+    rng = np.array(rng_state, dtype=np.uint64)
+    L = lib()
+    n = L.o_tree_build(_p(Vf, F64P), len(Vf), _p(Ff, I32P), len(Ff), rng.ctypes.data_as(C.POINTER(C.c_uint64)),
+                       None, None, None, None, None, 0)
+    assert n > 0, "the reference would throw"
+    nodes = np.zeros((n, 4), np.int32)
+    ntris = np.zeros(n, np.int32)
+    tris = np.zeros((n, 8, 9))
+    eps = np.zeros((n, 8))
+    ieps = np.zeros((n, 8))
+    m = L.o_tree_build(_p(Vf, F64P), len(Vf), _p(Ff, I32P), len(Ff), rng.ctypes.data_as(C.POINTER(C.c_uint64)),
+                       _p(nodes, I32P), _p(ntris, I32P), _p(tris, F64P), _p(eps, F64P), _p(ieps, F64P), n)
+    assert m == n
+    return nodes, ntris, tris, eps, ieps, (int(rng[0]), int(rng[1]))
+
+
 def sin(x):
     return lib().o_sin(float(x))
 

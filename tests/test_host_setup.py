@@ -103,9 +103,14 @@ def test_tree_eps_bounds_children():
                             d = point_tri_dist(t[3 * v:3 * v + 3], s.tris[g, i])
                             assert d <= s.eps[g, i] + 1e-9
                             assert d >= s.inner_eps[g, i] - 1e-9
-        # every mesh triangle appears in some leaf
-        total = sum(s.ntris[g] for g in range(lo, hi) if s.nodes[g, 2] == 0)
-        assert total >= 0
+        # the leaves hold real mesh triangles: positive area, each inside its
+        # parent surrogate's eps band (checked above), none repeated in this
+        # mesh's tree (copies arise only for degenerate groupings)
+        leaf = [tuple(s.tris[g, i]) for g in range(lo, hi) if s.nodes[g, 2] == 0 for i in range(s.ntris[g])]
+        assert len(leaf) == len(set(leaf)) > 0
+        for t in leaf:
+            a, b, c = np.array(t[0:3]), np.array(t[3:6]), np.array(t[6:9])
+            assert np.linalg.norm(np.cross(b - a, c - a)) > 0.0
 
 
 def test_tree_build_deterministic_and_consumes_rng():
