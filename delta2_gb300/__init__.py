@@ -437,6 +437,8 @@ def broad_phase(scene):
 
 
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
+CCD_STATS = ["ee_tests_cut", "newton_iters_saved", "pairs_predicted_clear", "pairs_certified", "pairs_missed",
+             "pairs_seen"]
 TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES, TUNE_SPIN_LIMIT = range(4)
 TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS,
               "solve_lanes": TUNE_SOLVE_LANES, "spin_limit": TUNE_SPIN_LIMIT}
@@ -494,6 +496,17 @@ class Context:
         """FP32 candidate bounds before the FP64 primitive tests (default on;
         results are identical either way)."""
         _check(lib().d2g_ctx_set_fp32_bounds(self.h, int(bool(enable))))
+
+    def set_ccd_certificates(self, enable):
+        """Conservative-advancement cut-off of edge-edge CCD tests (default on;
+        results are identical either way)."""
+        _check(lib().d2g_ctx_set_ccd_certificates(self.h, int(bool(enable))))
+
+    def ccd_stats(self, reset=False):
+        """CCD counters (d2g_ctx_ccd_stats) as a dict."""
+        out = np.zeros(6, np.int64)
+        _check(lib().d2g_ctx_ccd_stats(self.h, int(bool(reset)), _p(out, I64P), 6))
+        return dict(zip(CCD_STATS, out.tolist()))
 
     def set_tuning(self, key, value):
         """Launch-shape setting (TUNE_*); results are identical for every value."""

@@ -653,6 +653,24 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* c, int32_t enable) {
     return D2G_OK;
 }
 
+int d2g_ctx_set_ccd_certificates(d2g_ctx* c, int32_t enable) {
+    if (!c) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.certificates = enable != 0;
+    return D2G_OK;
+}
+
+int d2g_ctx_ccd_stats(d2g_ctx* c, int32_t reset, int64_t* stats, int32_t n) {
+    if (!c || !stats || n < 0) {
+        set_error("null context or output");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    return d2g::read_ccd_stats(c, stats, n, reset != 0);
+}
+
 int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
     if (!c || key < 0 || key >= D2G_TUNE_KEYS) {
         set_error("null context or unknown tuning key");

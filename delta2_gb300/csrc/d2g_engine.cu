@@ -605,7 +605,27 @@ struct EeArgs {
     int32_t* work;   // the listed test's work item
     int32_t* count;  // [0] listed tests
     int first_iters;  // Newton iterations in the first pass
+    int certificates;  // conservative-advancement cut-off of the first pass (results unchanged)
+    unsigned long long* ca_stats;  // [0] tests cut, [1] Newton iterations they did not run
 };
+
+// Conservative advancement over an edge-edge test's linear motion: every
+// endpoint moves on a straight line, so the points of the two edges at any
+// time t' are within V |t' - t| of where they were at time t, V being the
+// largest relative endpoint displacement |(aE.i - aS.i) - (bE.j - bS.j)| over
+// the four endpoint pairs (a point of an edge is a convex combination of its
+// endpoints, and so is its displacement).  Every distance edgeEdgeCCD
+// evaluates after time t is therefore at least dist(t) - V max(t, 1 - t).
+// When that and every distance evaluated so far are at least the search
+// distance (plus a margin far above FP64 rounding), the test cannot hit, and
+// a sub-test that cannot hit is never the best of a triangle pair that hits:
+// it is recorded as no contact, as the FP32 and box bounds record theirs.
+__device__ __forceinline__ double ee_motion_bound(const Edge& aS, const Edge& aE, const Edge& bS, const Edge& bE) {
+    const V3 da0 = aE.A - aS.A, da1 = aE.B - aS.B, db0 = bE.A - bS.A, db1 = bE.B - bS.B;
+    const V3 d00 = da0 - db0, d01 = da0 - db1, d10 = da1 - db0, d11 = da1 - db1;
+    const double m = fmax(fmax(dot(d00, d00), dot(d01, d01)), fmax(dot(d10, d10), dot(d11, d11)));
+    return sqrt(m);
+}
 
 __device__ __forceinline__ void ee_store_at(const EeArgs& a, int o, float thr, const Ccd& r) {
     if (o < 0) {  // leaf-pair test: P and Q swapped (continuous_comparison.h:881-896)
@@ -683,15 +703,34 @@ __global__ void __launch_bounds__(kPrimBlock) k_ee_first(int n_total, const int3
                 min_dist = ee_bisect(aS, aE, bS, bE, dot_start, r);
                 bisected = true;
             }
-            bool done = !(min_dist > 1e-8);
+            bool done = !(min_dist > 1e-8), cut = false;
             if (!done && !bisected) {
-                for (; iters < a.first_iters; iters++)
-                    if (ee_newton_iter(aS, aE, bS, bE, t, min_dist, r)) {
+                double V = 0.0, lim = 0.0;
+                if (a.certificates) {
+                    V = ee_motion_bound(aS, aE, bS, bE);
+                    const double mag = fmax(fmax(fmax(fabs(aS.A.x), fabs(aS.A.y)), fabs(aS.A.z)),
+                                            fmax(fmax(fabs(bS.A.x), fabs(bS.A.y)), fabs(bS.A.z)));
+                    lim = ((double)thr + 1e-6) + 1e-12 * (mag + V);
+                }
+                for (; iters < a.first_iters; iters++) {
+                    const double t_at = t;
+                    double d_at;
+                    if (ee_newton_iter(aS, aE, bS, bE, t, min_dist, r, &d_at)) {
                         done = true;
                         break;
                     }
+                    if (a.certificates && min_dist >= lim && d_at - V * fmax(t_at, 1.0 - t_at) >= lim) {
+                        cut = true;
+                        iters++;
+                        break;
+                    }
+                }
             }
-            if (done) {
+            if (cut) {
+                record_no_contact(w.out, w.hit);
+                atomicAdd(a.ca_stats, 1ull);
+                atomicAdd(a.ca_stats + 1, (unsigned long long)(kEeNewtonIters - iters));
+            } else if (done) {
                 r.dist = min_dist;
                 ee_store_at(a, o, thr, r);
             } else {
@@ -1504,11 +1543,33 @@ double level_budget(d2g_ctx* ctx) {
     return (double)E.device_bytes / 6.0;
 }
 
+// The CCD counters live on the device across calls (one read when asked).
+int ensure_ccd_stats(d2g_ctx* ctx) {
+    Engine& E = ctx->eng;
+    if (!E.ccd_stats.p) {
+        RC(E.ccd_stats.ensure(kCcdStats));
+        D2G_CUDA(cudaMemsetAsync(E.ccd_stats.p, 0, sizeof(unsigned long long) * kCcdStats, ctx->stream));
+    }
+    return D2G_OK;
+}
+
+int read_ccd_stats(d2g_ctx* ctx, int64_t* out, int n, bool reset) {
+    Engine& E = ctx->eng;
+    RC(ensure_ccd_stats(ctx));
+    unsigned long long h[kCcdStats];
+    D2G_CUDA(cudaMemcpyAsync(h, E.ccd_stats.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    if (reset) D2G_CUDA(cudaMemsetAsync(E.ccd_stats.p, 0, sizeof(h), ctx->stream));
+    D2G_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n && i < kCcdStats; i++) out[i] = (int64_t)h[i];
+    return D2G_OK;
+}
+
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters, const CcdSink* sink) {
     Engine& E = ctx->eng;
     cudaStream_t s = ctx->stream;
     int64_t c_node = 0, c_tri = 0, c_leaf = 0, c_levels = 0;
+    RC(ensure_ccd_stats(ctx));
     RC(E.pm.ensure((size_t)PM_SIZE * n_pairs + 1));
     RC(E.pfut.ensure(28 * (size_t)n_pairs + 1));
     RC(E.search.ensure(n_pairs + 1));
@@ -1657,6 +1718,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             ea.work = E.ee_work.p;
             ea.count = E.ee_count.p;
             ea.first_iters = E.tune[D2G_TUNE_EE_FIRST_ITERS];
+            ea.certificates = E.certificates ? 1 : 0;
+            ea.ca_stats = E.ccd_stats.p;
             D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
             k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, off_ee + w_ee, E.pm.p,
                                                                           ctx->tris.p, ea);

@@ -642,11 +642,12 @@ D2G_HD double ee_bisect(const Edge& aS, const Edge& aE, const Edge& bS, const Ed
 // recompute the same distance, which cannot lower min_dist, and stopping
 // gives the same result.
 D2G_HD bool ee_newton_iter(const Edge& aS, const Edge& aE, const Edge& bS, const Edge& bE, double& t,
-                           double& min_dist, Ccd& r) {
+                           double& min_dist, Ccd& r, double* dist_out = nullptr) {
     const V3 atA = lerp(aS.A, aE.A, t), atB = lerp(aS.B, aE.B, t);
     const V3 btA = lerp(bS.A, bE.A, t), btB = lerp(bS.B, bE.B, t);
     V3 P, Q;
     const double dist = edge_closest(atA, atB, btA, btB, P, Q);
+    if (dist_out) *dist_out = dist;
     if (dist < min_dist) {
         min_dist = dist;
         r.P = P;

@@ -206,6 +206,10 @@ struct Engine {
     long long launches = 0;
     bool profiling = false;
     bool fp32_bounds = true;  // FP32 candidate bounds before the FP64 tests (results identical either way)
+    bool certificates = true;  // conservative-advancement cut-off of edge-edge CCD tests (results identical)
+    // CCD counters since the last read-and-reset: [0] edge-edge tests cut by
+    // conservative advancement, [1] Newton iterations they did not run
+    DBuf<unsigned long long> ccd_stats;
     struct Pending {
         int kind;
         cudaEvent_t e0, e1;
@@ -272,6 +276,9 @@ struct CcdSink {
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters, const CcdSink* sink = nullptr);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
+// CCD counters (D2G_CCD_STATS entries, see d2g_ctx_ccd_stats), read on the host.
+constexpr int kCcdStats = 8;
+int read_ccd_stats(d2g_ctx* ctx, int64_t* out, int n, bool reset);
 // One level of one body pair's discrete traversal over the caller's node
 // pairs (d_pair: the pair's two bodies; d_node_pairs [n][2] global node ids):
 // every hit as a contact record in E.rec, the cumulative hit count after each

@@ -180,6 +180,23 @@ int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
  * above FP32 and FP64 rounding) and run the FP64 test only where a hit is
  * possible; with 0 every test runs in FP64.  Results are identical. */
 int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
+/* Conservative-advancement certificates (no reference counterpart): with
+ * enable != 0 (the default) an edge-edge CCD test whose distance at a Newton
+ * iterate, less the largest relative endpoint displacement times the time
+ * still ahead, stays above the search distance (and whose distances so far
+ * do too) is cut there: no later iterate can come closer, so it cannot hit and
+ * is recorded as no contact, as the reference's min over its iterates would
+ * leave it.  Results are identical; 0 runs every test to the end. */
+int d2g_ctx_set_ccd_certificates(d2g_ctx* ctx, int32_t enable);
+/* CCD counters since the context was created or last reset (reset != 0
+ * clears them after reading), n of D2G_CCD_STATS entries:
+ *   0 edge-edge tests cut by the certificates, 1 Newton iterations they did
+ *   not run (of the reference's 10 per test), 2 pair queries the learned
+ *   proposal predicted to have no contact, 3 of those the root certificate
+ *   proved contact-free (skipped), 4 of those it could not prove (misses,
+ *   traversed as usual), 5 pair queries seen by the proposal. */
+#define D2G_CCD_STATS 6
+int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
 /* Launch-shape settings (no reference counterpart).  They change only how
  * the work is spread over the GPU; every setting gives identical results.
  *   D2G_TUNE_EE_FIRST_ITERS (default 2, 0..10): Newton iterations an

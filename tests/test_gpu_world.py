@@ -249,6 +249,33 @@ def test_ee_first_iters_do_not_change_results(ctx):
             assert np.array_equal(bits(np.asarray(a)), bits(np.asarray(b)))
 
 
+def test_ccd_certificates_do_not_change_results(ctx):
+    """The conservative-advancement cut-off of edge-edge CCD tests gives the
+    same contacts, bit for bit, as running every test to its end, and as the
+    oracle; it does cut tests on a hull scene in motion."""
+    s = D.make_scene(2, nx=4, ny=4, nz=4, spacing=1.3, speed_sigma=2.0, seed=9)
+    pairs = D.broad_phase(s)
+    mt = np.full(len(pairs), np.float64(np.float32(s.opt_dt)) * 4)
+    ref = O.ccd(s.copy(), pairs, mt)
+    out = {}
+    try:
+        for mode in (True, False):
+            ctx.set_scene(s.copy())
+            ctx.set_ccd_certificates(mode)
+            ctx.ccd_stats(reset=True)
+            out[mode] = ctx.compare_trees_full_continuous(pairs, mt)
+            out[(mode, "stats")] = ctx.ccd_stats(reset=True)
+    finally:
+        ctx.set_ccd_certificates(True)
+    for mode in (True, False):
+        c, off, cnt = out[mode]
+        assert np.array_equal(off, ref[1])
+        assert np.array_equal(bits(c), bits(ref[0]))
+    assert len(ref[0]) > 0
+    assert out[(True, "stats")]["ee_tests_cut"] > 0 and out[(True, "stats")]["newton_iters_saved"] > 0
+    assert out[(False, "stats")]["ee_tests_cut"] == 0
+
+
 def test_fp32_bounds_do_not_change_results(ctx):
     # the FP64-exact mode (every primitive test in FP64) and the default FP32
     # candidate bounds give the same contacts, bit for bit
