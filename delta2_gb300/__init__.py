@@ -502,6 +502,22 @@ class Context:
         results are identical either way)."""
         _check(lib().d2g_ctx_set_ccd_certificates(self.h, int(bool(enable))))
 
+    def ccd_features(self, pairs, max_time):
+        """The proposal's features [n, 20] of CCD pair queries (d2g_ccd_features)."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        mt = np.ascontiguousarray(np.broadcast_to(np.asarray(max_time, dtype=np.float64), (len(pairs),)))
+        out = np.zeros((max(1, len(pairs)), 20), np.float32)
+        _check(lib().d2g_ccd_features(self.h, _p(pairs, I32P), _p(mt, F64P), len(pairs), _p(out, F32P)))
+        return out[:len(pairs)]
+
+    def set_ccd_proposal(self, mlp, threshold=0.5):
+        """The learned proposal in every CCD call (d2g_ctx_set_ccd_proposal):
+        queries the network predicts contact-free (hit probability below
+        threshold) are skipped when the root certificate proves it; mlp None
+        turns it off.  Results are identical."""
+        self._proposal = mlp
+        _check(lib().d2g_ctx_set_ccd_proposal(self.h, mlp.h if mlp is not None else None, C.c_float(threshold)))
+
     def ccd_stats(self, reset=False):
         """CCD counters (d2g_ctx_ccd_stats) as a dict."""
         out = np.zeros(6, np.int64)

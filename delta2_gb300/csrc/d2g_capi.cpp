@@ -662,6 +662,37 @@ int d2g_ctx_set_ccd_certificates(d2g_ctx* c, int32_t enable) {
     return D2G_OK;
 }
 
+int d2g_ccd_features(d2g_ctx* c, const int32_t* pairs, const double* max_time, int32_t n_pairs, float* features) {
+    RC(check_ready(c));
+    RC(check_pairs(c, pairs, n_pairs));
+    if (n_pairs > 0 && (!max_time || !features)) {
+        set_error("null max_time or output");
+        return D2G_ERR_INVALID;
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    RC(upload(c, c->eng.d_pairs, pairs, 2 * (size_t)n_pairs));
+    RC(upload(c, c->eng.d_max_time, max_time, (size_t)n_pairs));
+    RC(d2g::run_ccd_features(c, c->eng.d_pairs.p, c->eng.d_max_time.p, n_pairs));
+    if (n_pairs > 0)
+        D2G_CUDA(cudaMemcpyAsync(features, c->eng.pp_feat.p, sizeof(float) * 20 * (size_t)n_pairs,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    return D2G_OK;
+}
+
+int d2g_ctx_set_ccd_proposal(d2g_ctx* c, d2g_mlp* mlp, float threshold) {
+    if (!c || (mlp && d2g::mlp_context(mlp) != c) || !(threshold >= 0.0f && threshold <= 1.0f)) {
+        set_error("null context, a network of another context, or a threshold outside [0, 1]");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.proposal = mlp;
+    // predicted contact-free: sigmoid(logit) < threshold, i.e. logit < log(threshold / (1 - threshold))
+    c->eng.proposal_logit = threshold >= 1.0f ? INFINITY
+                            : threshold <= 0.0f ? -INFINITY
+                                                : (float)std::log((double)threshold / (1.0 - (double)threshold));
+    return D2G_OK;
+}
+
 int d2g_ctx_ccd_stats(d2g_ctx* c, int32_t reset, int64_t* stats, int32_t n) {
     if (!c || !stats || n < 0) {
         set_error("null context or output");

@@ -243,11 +243,16 @@ __global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const 
                               const double* __restrict__ pm, const float* __restrict__ pm32,
                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
                               const float* __restrict__ tri32, const double* __restrict__ geo_eps,
-                              int32_t* __restrict__ flags) {
+                              const uint8_t* __restrict__ skip, int32_t* __restrict__ flags) {
     const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= n_soup) return;  // uniform per warp
     const Entry e = soup[w];
+    if (skip && skip[e.pair]) {  // a pair the root certificate proved contact-free: no slot goes on
+        flags[64 * (size_t)w + lane] = 0;
+        flags[64 * (size_t)w + lane + 32] = 0;
+        return;
+    }
     const int na = ntris[e.na], nb = ntris[e.nb];
     const bool side_b = lane >= 8;
     const int t = lane & 7;
@@ -329,6 +334,162 @@ __global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const 
     flags[64 * (size_t)w + lane + 32] = res[1];
 }
 
+
+__global__ void k_add_u64(unsigned long long* __restrict__ v, unsigned long long x) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *v += x;
+}
+
+// ------------------------------------------------- learned proposal --------
+// Features of a CCD pair query for the proposal network, from the bodies'
+// current states: B's pose in A's frame (R_a^T R_b row major, R_a^T (x_b -
+// x_a)), the relative motion over the query's horizon in A's frame
+// (R_a^T (v_b - v_a) max_time, R_a^T (w_b - w_a) max_time with w = R I^-1 R^T L)
+// and the two bounding radii; FP64, stored as FP32.
+__global__ void k_ccd_features(int n, const int32_t* __restrict__ pairs, const double* __restrict__ max_time,
+                               const double* __restrict__ cur, const double* __restrict__ ii,
+                               const double* __restrict__ radius, float* __restrict__ feat) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int ia = pairs[2 * p], ib = pairs[2 * p + 1];
+    const State a = load_state(cur + 14 * (size_t)ia), b = load_state(cur + 14 * (size_t)ib);
+    double Ra[9], Rb[9], Ia[9], Ib[9];
+    qmat(a.q, Ra);
+    qmat(b.q, Rb);
+    world_inv_inertia(a.q, ii + 9 * (size_t)ia, Ia);
+    world_inv_inertia(b.q, ii + 9 * (size_t)ib, Ib);
+    const V3 wa = m3_vec(Ia, a.L), wb = m3_vec(Ib, b.L);
+    const double mt = max_time[p];
+    float* f = feat + 20 * (size_t)p;
+    auto at = [&](V3 v, int r) { return (Ra[r] * v.x + Ra[3 + r] * v.y) + Ra[6 + r] * v.z; };  // (R_a^T v)_r
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) f[3 * r + c] = (float)((Ra[r] * Rb[c] + Ra[3 + r] * Rb[3 + c]) + Ra[6 + r] * Rb[6 + c]);
+    for (int r = 0; r < 3; r++) {
+        f[9 + r] = (float)at(b.x - a.x, r);
+        f[12 + r] = (float)(at(b.v - a.v, r) * mt);
+        f[15 + r] = (float)(at(wb - wa, r) * mt);
+    }
+    f[18] = (float)radius[ia];
+    f[19] = (float)radius[ib];
+}
+
+// The root certificate of a pair query the network predicts contact-free: a
+// warp per pair proves that no slot of the root node pair can hit, so the
+// query has no contacts (compareTreesFullContinuous expands only node pairs
+// with hits).  A slot is proven clear when the reference's swept-box test
+// rejects it (continuous_comparison.h:804-812, FP64 as there), or when the
+// two triangles' vertices, each on a straight line from its start to its end
+// position, stay apart over the motion:
+//   * along an axis n fixed at the start (the centroid difference, either
+//     face normal), min_j n.b_j(t) - max_i n.a_i(t) is concave in t, so its
+//     minimum over [0, 1] is at t = 0 or 1; the gap over |n| bounds every
+//     edge-edge distance edgeEdgeCCD evaluates (points of the two edges at
+//     one time), and the point-to-triangle distances at t = 0 and 1;
+//   * pointTriCCDLinear returns 0 only when a vertex's start and end lie on
+//     opposite sides of the other triangle's plane (its start and end frames),
+//     and otherwise the vertex's distance to that plane at t = 0 or 1 when its
+//     projection falls inside (decided with float barycentrics) or nothing:
+//     so every vertex must keep its side, and the gap carries a margin for a
+//     projection the float test puts inside by mistake (6e-7 of the
+//     triangle's size times its conditioning (L0 L1 / 2 area)^2).
+// A query whose every root slot is proven clear is skipped: it would produce
+// no contact.  Any slot not proven leaves the query to the exact traversal.
+// stats: [2] predicted clear, [3] certified, [4] not certified, [5] seen.
+__device__ __forceinline__ double axis_gap(V3 n, const V3* A0, const V3* A1, const V3* B0, const V3* B1) {
+    double g = -1e300;
+    for (int sg = 0; sg < 2; sg++) {
+        const V3 m = sg ? -n : n;
+        double gmin = 1e300;
+        for (int t = 0; t < 2; t++) {
+            const V3* A = t ? A1 : A0;
+            const V3* B = t ? B1 : B0;
+            const double amax = fmax(fmax(dot(m, A[0]), dot(m, A[1])), dot(m, A[2]));
+            const double bmin = fmin(fmin(dot(m, B[0]), dot(m, B[1])), dot(m, B[2]));
+            gmin = fmin(gmin, bmin - amax);
+        }
+        g = fmax(g, gmin);
+    }
+    const double nn = norm(n);
+    return nn > 0.0 ? g / nn : -1e300;
+}
+// every vertex of P keeps a side of T's plane (start and end frames), with
+// distances far above rounding
+__device__ __forceinline__ bool keeps_side(const V3* P0, const V3* P1, const V3* T0, const V3* T1, double tol) {
+    const V3 n0 = cross(T0[1] - T0[0], T0[2] - T0[0]), n1 = cross(T1[1] - T1[0], T1[2] - T1[0]);
+    const double l0 = norm(n0), l1 = norm(n1);
+    if (!(l0 > 0.0) || !(l1 > 0.0)) return false;
+    for (int i = 0; i < 3; i++) {
+        const double h0 = dot(n0, P0[i] - T0[0]) / l0, h1 = dot(n1, P1[i] - T1[0]) / l1;
+        if (!(h0 * h1 > 0.0) || !(fabs(h0) > tol) || !(fabs(h1) > tol)) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ double tri_conditioning(const V3* T, double& lmax) {
+    const double l0 = norm(T[1] - T[0]), l1 = norm(T[2] - T[0]), l2 = norm(T[2] - T[1]);
+    lmax = fmax(fmax(l0, l1), l2);
+    const double a2 = norm(cross(T[1] - T[0], T[2] - T[0]));
+    if (!(a2 > 0.0)) return 1e300;
+    const double k = (l0 * l1) / a2;
+    return k * k;
+}
+__global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                               const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
+                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
+                               const double* __restrict__ geo_eps, const float* __restrict__ search,
+                               const float* __restrict__ pred, float logit_cut, uint8_t* __restrict__ skip,
+                               unsigned long long* __restrict__ stats) {
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= n) return;  // uniform per warp
+    const bool gated = pred[2 * (size_t)p + 1] < logit_cut;  // NaN: not gated
+    if (!gated) {
+        if (lane == 0) skip[p] = 0;
+        return;
+    }
+    const int ia = pairs[2 * p], ib = pairs[2 * p + 1];
+    const int na_node = mesh_node_off[mesh[ia]], nb_node = mesh_node_off[mesh[ib]];
+    const int na = ntris[na_node], nb = ntris[nb_node];
+    const double* M = pm + (size_t)PM_SIZE * p;
+    const double S = (double)search[p];
+    bool clear = true;
+    for (int h = 0; h < 2; h++) {
+        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+        if (ta >= na || tb >= nb) continue;
+        const Tri A = load_tri(tris + (size_t)na_node * 72 + ta * 9), B = load_tri(tris + (size_t)nb_node * 72 + tb * 9);
+        if (!box_overlap(swept_box(A, M + PM_AS, M + PM_AE, geo_eps[ia]), swept_box(B, M + PM_BS, M + PM_BE, geo_eps[ib])))
+            continue;
+        const V3 A0[3] = {xform_rigid(A.A, M + PM_AS), xform_rigid(A.B, M + PM_AS), xform_rigid(A.C, M + PM_AS)};
+        const V3 A1[3] = {xform_rigid(A.A, M + PM_AE), xform_rigid(A.B, M + PM_AE), xform_rigid(A.C, M + PM_AE)};
+        const V3 B0[3] = {xform_rigid(B.A, M + PM_BS), xform_rigid(B.B, M + PM_BS), xform_rigid(B.C, M + PM_BS)};
+        const V3 B1[3] = {xform_rigid(B.A, M + PM_BE), xform_rigid(B.B, M + PM_BE), xform_rigid(B.C, M + PM_BE)};
+        double mag = 0.0;
+        for (int i = 0; i < 3; i++)
+            mag = fmax(mag, fmax(fmax(fmax(fabs(A0[i].x), fabs(A0[i].y)), fabs(A0[i].z)),
+                                 fmax(fmax(fabs(B0[i].x), fabs(B0[i].y)), fabs(B0[i].z))));
+        double la, lb;
+        const double ka = tri_conditioning(A0, la), kb = tri_conditioning(B0, lb);
+        if (!(ka < 1e4) || !(kb < 1e4)) {
+            clear = false;
+            continue;
+        }
+        const double tol = 1e-9 + 1e-12 * mag;
+        const double margin = (1e-5 + 1e-9 * mag) + 6e-7 * fmax(ka * la, kb * lb);
+        if (!keeps_side(A0, A1, B0, B1, tol) || !keeps_side(B0, B1, A0, A1, tol)) {
+            clear = false;
+            continue;
+        }
+        const V3 ca = (A0[0] + A0[1]) + A0[2], cb = (B0[0] + B0[1]) + B0[2];
+        double g = axis_gap(cb - ca, A0, A1, B0, B1);
+        g = fmax(g, axis_gap(cross(A0[1] - A0[0], A0[2] - A0[0]), A0, A1, B0, B1));
+        g = fmax(g, axis_gap(cross(B0[1] - B0[0], B0[2] - B0[0]), A0, A1, B0, B1));
+        if (!(g >= S + margin)) clear = false;
+    }
+    const bool all = __all_sync(0xffffffffu, clear);
+    if (lane == 0) {
+        skip[p] = all ? 1 : 0;
+        atomicAdd(stats + 2, 1ull);
+        atomicAdd(stats + (all ? 3 : 4), 1ull);
+    }
+}
 
 // Point-triangle work item j (the decoding of k_prim_pt): which pair, which
 // point (body-local), which triangle (body-local) and which transforms.
@@ -1543,6 +1704,18 @@ double level_budget(d2g_ctx* ctx) {
     return (double)E.device_bytes / 6.0;
 }
 
+// The proposal's 20 features of n pair queries over the context's device
+// bodies, into E.pp_feat.
+int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n) {
+    Engine& E = ctx->eng;
+    RC(E.pp_feat.ensure(20 * (size_t)n + 1));
+    if (n > 0)
+        LAUNCH(k_ccd_features, n, n, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p, ctx->bounding_radius.p,
+               E.pp_feat.p);
+    D2G_CUDA(cudaGetLastError());
+    return D2G_OK;
+}
+
 // The CCD counters live on the device across calls (one read when asked).
 int ensure_ccd_stats(d2g_ctx* ctx) {
     Engine& E = ctx->eng;
@@ -1583,6 +1756,23 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
                ctx->mesh_node_off.p, ctx->geo_eps.p, E.pm.p, E.pfut.p, E.search.p, E.soup.p);
     RC(E.pm32c.ensure((size_t)96 * n_pairs + 1));
     if (n_pairs > 0) LAUNCH(k_ccd_pm32, 96LL * n_pairs, n_pairs, E.pm.p, E.pm32c.p);  // FP32 poses, once per call
+    // The learned proposal: the network predicts which queries have no
+    // contact; the root certificate proves it for those it can, and the
+    // proven ones are skipped (their outputs are empty either way).
+    const uint8_t* skip = nullptr;
+    if (E.proposal && n_pairs > 0) {
+        RC(E.pp_feat.ensure(20 * (size_t)n_pairs));
+        RC(E.pp_skip.ensure(n_pairs + 1));
+        LAUNCH(k_ccd_features, n_pairs, n_pairs, d_pairs, d_max_time, ctx->cur.p, ctx->inv_inertia.p,
+               ctx->bounding_radius.p, E.pp_feat.p);
+        const float* pred = nullptr;
+        RC(mlp_forward_device(E.proposal, E.pp_feat.p, n_pairs, &pred));
+        LAUNCH(k_root_certify, 32LL * n_pairs, n_pairs, d_pairs, E.pm.p, ctx->mesh.p, ctx->mesh_node_off.p,
+               ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p, pred, E.proposal_logit, E.pp_skip.p,
+               E.ccd_stats.p);
+        LAUNCH(k_add_u64, 1, E.ccd_stats.p + 5, (unsigned long long)n_pairs);
+        skip = E.pp_skip.p;
+    }
     // Pair chunks: the traversal of a range of body pairs runs to the end
     // before the next range starts.  A level whose buffers would pass the
     // budget abandons its chunk (its records are dropped) and the chunk is
@@ -1628,7 +1818,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
             const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
             LAUNCH(k_soup_filter, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, E.pm32c.p, ctx->ntris.p,
-                   ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, E.flags.p);
+                   ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, skip, E.flags.p);
             prof_end(ctx, pff);
         }
         RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));

@@ -207,6 +207,13 @@ struct Engine {
     bool profiling = false;
     bool fp32_bounds = true;  // FP32 candidate bounds before the FP64 tests (results identical either way)
     bool certificates = true;  // conservative-advancement cut-off of edge-edge CCD tests (results identical)
+    // learned proposal (d2g_ctx_set_ccd_proposal): the network consulted by
+    // CCD calls, the hit logit below which a pair is predicted contact-free,
+    // per-pair features, predictions and skip flags
+    d2g_mlp* proposal = nullptr;
+    float proposal_logit = 0.0f;
+    DBuf<float> pp_feat;
+    DBuf<uint8_t> pp_skip;
     // CCD counters since the last read-and-reset: [0] edge-edge tests cut by
     // conservative advancement, [1] Newton iterations they did not run
     DBuf<unsigned long long> ccd_stats;
@@ -276,6 +283,11 @@ struct CcdSink {
 int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n_pairs, int* n_out,
             int64_t* counters, const CcdSink* sink = nullptr);
 int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_out, int64_t* counters);
+// The learned proposal's network (d2g_mlp.cu): forward pass over device
+// feature rows, and the context the network belongs to.
+int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_out);
+d2g_ctx* mlp_context(d2g_mlp* m);
+int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n);
 // CCD counters (D2G_CCD_STATS entries, see d2g_ctx_ccd_stats), read on the host.
 constexpr int kCcdStats = 8;
 int read_ccd_stats(d2g_ctx* ctx, int64_t* out, int n, bool reset);

@@ -480,6 +480,32 @@ double unit(uint64_t& x) { return (double)(splitmix(x) >> 11) * (1.0 / 900719925
 
 using d2g::MlpState;
 
+namespace d2g {
+
+// Forward pass over n feature rows already in device memory (d_feat [n][20]
+// FP32, on the context's stream): *d_out points to n (TOI, hit logit) pairs
+// in the network's own buffer, valid until its next call.
+int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_out) {
+    MlpState& S = m->s;
+    const int n_pad = ((n + kRows - 1) / kRows) * kRows;
+    MRC(S.X.ensure((size_t)n_pad * kInPad + 1));
+    MRC(S.out.ensure(2 * (size_t)n_pad + 2));
+    if (n_pad) {
+        k_mlp_features<<<mblocks((long long)n_pad * kInPad), 256, 0, S.ctx->stream>>>(n, n_pad, d_feat, S.mean.p,
+                                                                                       S.inv_std.p, S.X.p);
+        k_mlp_forward<<<n_pad / kRows, kThreads, 0, S.ctx->stream>>>(n, S.X.p, S.W1b.p, S.W2b.p, S.W3b.p, S.P.p,
+                                                                     S.out.p, nullptr, nullptr, nullptr, nullptr);
+        S.ctx->eng.launches += 2;
+        D2G_CUDA(cudaGetLastError());
+    }
+    *d_out = S.out.p;
+    return D2G_OK;
+}
+
+d2g_ctx* mlp_context(d2g_mlp* m) { return m->s.ctx; }
+
+}  // namespace d2g
+
 extern "C" {
 
 int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out) {
@@ -539,6 +565,7 @@ void d2g_mlp_destroy(d2g_mlp* m) {
     if (!m) return;
     cudaSetDevice(m->s.ctx->device);
     cudaStreamSynchronize(m->s.ctx->stream);
+    if (m->s.ctx->eng.proposal == m) m->s.ctx->eng.proposal = nullptr;  // the CCD stops consulting it
     delete m;
 }
 

@@ -156,6 +156,7 @@ int d2g_broad_phase(const d2g_bodies* bodies, const float* local_aabb, int32_t* 
 
 /* ------------------------------------------------------------ context ---- */
 typedef struct d2g_ctx d2g_ctx;
+typedef struct d2g_mlp d2g_mlp; /* the learned proposal's network (d2g_mlp_create, below) */
 int d2g_ctx_create(int32_t device, d2g_ctx** out);
 void d2g_ctx_destroy(d2g_ctx* ctx);
 /* The context's CUDA stream (cudaStream_t) for ordering caller work. */
@@ -188,6 +189,23 @@ int d2g_ctx_set_fp32_bounds(d2g_ctx* ctx, int32_t enable);
  * is recorded as no contact, as the reference's min over its iterates would
  * leave it.  Results are identical; 0 runs every test to the end. */
 int d2g_ctx_set_ccd_certificates(d2g_ctx* ctx, int32_t enable);
+/* Learned proposal in the CCD (no reference counterpart): with a network of
+ * this context (d2g_mlp_create), every CCD call (compareTreesFullContinuous,
+ * the time-step selection, the stepper) computes each pair query's 20
+ * features, runs the network, and for the queries it predicts contact-free
+ * (hit probability below `threshold`) tries a root certificate: a proof,
+ * over the linear motion the reference's CCD assumes, that no slot of the
+ * root node pair can come within the search distance.  Proven queries are
+ * skipped (they would yield no contact); any other query runs the exact
+ * traversal, so results are unchanged.  threshold 1 sends every query to
+ * the certificate (the certificate without the network); mlp NULL turns the
+ * proposal off (the default).  The counters of d2g_ctx_ccd_stats report its
+ * effect.  Destroying the network turns the proposal off. */
+int d2g_ctx_set_ccd_proposal(d2g_ctx* ctx, d2g_mlp* mlp, float threshold);
+/* The 20 proposal features of n pair queries (pairs [n][2], max_time [n]) over
+ * the context's device bodies, as the proposal computes them (FP64, stored as
+ * FP32; layout as d2g_mlp_predict's input): features [n][20]. */
+int d2g_ccd_features(d2g_ctx* ctx, const int32_t* pairs, const double* max_time, int32_t n_pairs, float* features);
 /* CCD counters since the context was created or last reset (reset != 0
  * clears them after reading), n of D2G_CCD_STATS entries:
  *   0 edge-edge tests cut by the certificates, 1 Newton iterations they did
@@ -389,7 +407,6 @@ int d2g_world_timing(d2g_ctx* ctx, double* ms, int32_t n);
  * b2 [128], W3 [2][128], b3 [2].  Training is Adam (0.9, 0.999, 1e-8) over
  * shuffled mini-batches. */
 #define D2G_MLP_PARAMS 19458
-typedef struct d2g_mlp d2g_mlp;
 int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out);
 void d2g_mlp_destroy(d2g_mlp* mlp);
 int d2g_mlp_params(d2g_mlp* mlp, float* params, int32_t n);
