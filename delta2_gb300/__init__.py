@@ -502,6 +502,23 @@ class Context:
         results are identical either way)."""
         _check(lib().d2g_ctx_set_ccd_certificates(self.h, int(bool(enable))))
 
+    def mass_properties(self, meshes, surface=None, thickness=0.01):
+        """Mass properties of meshes [(V, F), ...] on the device
+        (d2g_mass_properties) -> [n, 22]: volume, centre of mass, unit-density
+        inertia tensor (row major), its inverse."""
+        Vs = [np.ascontiguousarray(V, dtype=np.float64).reshape(-1, 3) for V, _ in meshes]
+        Fs = [np.ascontiguousarray(F, dtype=np.int32).reshape(-1, 3) for _, F in meshes]
+        voff = np.concatenate([[0], np.cumsum([len(v) for v in Vs])]).astype(np.int32)
+        foff = np.concatenate([[0], np.cumsum([len(f) for f in Fs])]).astype(np.int32)
+        V = np.ascontiguousarray(np.concatenate(Vs) if Vs else np.zeros((0, 3)))
+        F = np.ascontiguousarray(np.concatenate(Fs) if Fs else np.zeros((0, 3), np.int32), dtype=np.int32)
+        surf = np.ascontiguousarray(surface if surface is not None else np.zeros(len(meshes)), dtype=np.uint8)
+        out = np.zeros((max(1, len(meshes)), 22))
+        _check(lib().d2g_mass_properties(self.h, _p(V, F64P), len(V), _p(F, I32P), len(F), _p(voff, I32P),
+                                         _p(foff, I32P), _p(surf, U8P), len(meshes), C.c_double(thickness),
+                                         _p(out, F64P)))
+        return out[:len(meshes)]
+
     def ccd_features(self, pairs, max_time):
         """The proposal's features [n, 20] of CCD pair queries (d2g_ccd_features)."""
         pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)

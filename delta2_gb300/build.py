@@ -21,7 +21,7 @@ OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libd2g.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["d2g_engine.cu", "d2g_step.cu", "d2g_solve.cu", "d2g_broadphase.cu", "d2g_mlp.cu"]
+CU_SOURCES = ["d2g_engine.cu", "d2g_step.cu", "d2g_solve.cu", "d2g_broadphase.cu", "d2g_mlp.cu", "d2g_mesh.cu"]
 CPP_SOURCES = ["d2g_capi.cpp", "d2g_world.cpp", "host/d2g_scene.cpp", "host/d2g_broad.cpp", "host/d2g_treefile.cpp",
                "host/d2g_obj.cpp"]
 

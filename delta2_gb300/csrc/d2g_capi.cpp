@@ -662,6 +662,50 @@ int d2g_ctx_set_ccd_certificates(d2g_ctx* c, int32_t enable) {
     return D2G_OK;
 }
 
+int d2g_mass_properties(d2g_ctx* c, const double* V, int32_t n_vertices, const int32_t* F, int32_t n_faces,
+                        const int32_t* mesh_vertex_off, const int32_t* mesh_face_off, const uint8_t* surface,
+                        int32_t n_meshes, double thickness, double* out) {
+    if (!c || n_meshes < 0 || n_vertices < 0 || n_faces < 0 || (n_meshes > 0 && (!mesh_vertex_off ||
+                                                                               !mesh_face_off || !out)) ||
+        (n_vertices > 0 && !V) || (n_faces > 0 && !F) || !(thickness > 0.0)) {
+        set_error("invalid mesh set");
+        return D2G_ERR_INVALID;
+    }
+    if (n_meshes > 0 && (mesh_vertex_off[0] != 0 || mesh_face_off[0] != 0 ||
+                         mesh_vertex_off[n_meshes] != n_vertices || mesh_face_off[n_meshes] != n_faces)) {
+        set_error("mesh offsets must start at 0 and end at the vertex and face counts");
+        return D2G_ERR_INVALID;
+    }
+    for (int m = 0; m < n_meshes; m++) {
+        const int nv = mesh_vertex_off[m + 1] - mesh_vertex_off[m], nf = mesh_face_off[m + 1] - mesh_face_off[m];
+        if (nv < 3 || nf < 1) {
+            set_error("mesh " + std::to_string(m) + " needs 3 vertices and a face");
+            return D2G_ERR_INVALID;
+        }
+        for (int i = 3 * mesh_face_off[m]; i < 3 * mesh_face_off[m + 1]; i++)
+            if (F[i] < 0 || F[i] >= nv) {
+                set_error("mesh " + std::to_string(m) + " has a face index outside its vertices");
+                return D2G_ERR_INVALID;
+            }
+    }
+    D2G_CUDA(cudaSetDevice(c->device));
+    d2g::Engine& E = c->eng;
+    std::vector<uint8_t> surf((size_t)n_meshes + 1, 0);
+    if (surface)
+        for (int m = 0; m < n_meshes; m++) surf[m] = surface[m] ? 1 : 0;
+    RC(upload(c, E.ms_V, V, 3 * (size_t)n_vertices));
+    RC(upload(c, E.ms_F, F, 3 * (size_t)n_faces));
+    RC(upload(c, E.ms_voff, mesh_vertex_off, (size_t)n_meshes + 1));
+    RC(upload(c, E.ms_foff, mesh_face_off, (size_t)n_meshes + 1));
+    RC(upload(c, E.ms_surface, surf.data(), (size_t)n_meshes));
+    RC(E.ms_out.ensure(22 * (size_t)n_meshes + 1));
+    RC(d2g::run_mass_properties(c, E.ms_V.p, E.ms_F.p, E.ms_voff.p, E.ms_foff.p, E.ms_surface.p, n_meshes,
+                                thickness, E.ms_out.p));
+    RC(download(c, out, E.ms_out, 22 * (size_t)n_meshes));
+    D2G_CUDA(cudaStreamSynchronize(c->stream));
+    return D2G_OK;
+}
+
 int d2g_ccd_features(d2g_ctx* c, const int32_t* pairs, const double* max_time, int32_t n_pairs, float* features) {
     RC(check_ready(c));
     RC(check_pairs(c, pairs, n_pairs));

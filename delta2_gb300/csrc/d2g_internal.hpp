@@ -186,6 +186,10 @@ struct Engine {
     DBuf<double> rec, rec_sorted;
     DBuf<int32_t> rec_pair, rec_pair_sorted, rec_idx, rec_idx_sorted, out_off, pair_cnt;
     DBuf<int32_t> d_pairs, bucket_nodes;
+    // mesh sets of d2g_mass_properties
+    DBuf<double> ms_V, ms_out;
+    DBuf<int32_t> ms_F, ms_voff, ms_foff;
+    DBuf<uint8_t> ms_surface;
     DBuf<double> d_max_time;
     DBuf<uint8_t> cub_tmp, cub_tmp2;
     // phased edge-edge CCD (d2g_engine.cu)
@@ -288,6 +292,10 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
 int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_out);
 d2g_ctx* mlp_context(d2g_mlp* m);
 int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n);
+// Mass properties of many meshes (d2g_mesh.cu): out [n][22].
+int run_mass_properties(d2g_ctx* ctx, const double* d_V, const int32_t* d_F, const int32_t* d_voff,
+                        const int32_t* d_foff, const uint8_t* d_surface, int n_meshes, double thickness,
+                        double* d_out);
 // CCD counters (D2G_CCD_STATS entries, see d2g_ctx_ccd_stats), read on the host.
 constexpr int kCcdStats = 8;
 int read_ccd_stats(d2g_ctx* ctx, int64_t* out, int n, bool reset);

@@ -175,6 +175,19 @@ int d2g_ctx_set_scenes(d2g_ctx* ctx, const int32_t* scene_of_body);
 /* Copy the device body states (last/cur/fut, last_dt, sleep_steps, sleeping) back. */
 int d2g_ctx_get_bodies(d2g_ctx* ctx, d2g_bodies* bodies);
 
+/* Mass properties of many meshes on the device (model/mesh.cpp:53-130,
+ * model/inertia.cpp:20-84, for large mesh sets): mesh m has vertices
+ * V[mesh_vertex_off[m] .. +1) and faces F[mesh_face_off[m] .. +1) (vertex
+ * indices local to the mesh); surface[m] != 0 takes the thin-shell model of
+ * the given thickness (as static planes use), else the closed-surface volume
+ * model (the reference's tetgen tetrahedralisation replaced by the faces'
+ * tetrahedra with the origin).  out [n_meshes][22]: volume, centre of mass
+ * (3), unit-density inertia tensor about it (9, row major), its inverse (9);
+ * the same bits as the host scene set-up gives.  surface may be NULL. */
+int d2g_mass_properties(d2g_ctx* ctx, const double* V, int32_t n_vertices, const int32_t* F, int32_t n_faces,
+                        const int32_t* mesh_vertex_off, const int32_t* mesh_face_off, const uint8_t* surface,
+                        int32_t n_meshes, double thickness, double* out);
+
 /* Mixed precision (no reference counterpart): with enable != 0 (the
  * default) the discrete narrow phase and the CCD first bound every
  * primitive test in FP32 (bounding spheres and box gaps, with a margin far

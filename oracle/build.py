@@ -24,7 +24,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libd2o.so")
 LIB_FAST = os.path.join(OUT_DIR, "libd2o_fast.so")
 SOURCES = ["d2o_capi.cpp"]
-HEADERS = ["d2o_math.hpp", "d2o_geom.hpp", "d2o_collide.hpp", "d2o_solve.hpp", "d2o_tree.hpp"]
+HEADERS = ["d2o_math.hpp", "d2o_geom.hpp", "d2o_collide.hpp", "d2o_solve.hpp", "d2o_tree.hpp", "d2o_mass.hpp"]
 
 
 def _stale(lib):

@@ -6,6 +6,7 @@
 
 #include "d2o_collide.hpp"
 #include "d2o_solve.hpp"
+#include "d2o_mass.hpp"
 #include "d2o_tree.hpp"
 
 using namespace d2o;
@@ -485,6 +486,21 @@ int o_tree_build(const double* V, int nv, const int32_t* F, int nf, uint64_t* rn
         rng[1] = r.inc;
     }
     return n;
+}
+
+// MeshData's mass properties (model/mesh.cpp:53-130): out = volume, centre of
+// mass (3), unit inertia tensor (9, row major, about the centre of mass).
+void o_mass_properties(const double* V, int nv, const int32_t* F, int nf, int surface, double thickness,
+                       double* out13) {
+    std::vector<V3> P((size_t)nv);
+    for (int i = 0; i < nv; i++) P[i] = V3{V[3 * i], V[3 * i + 1], V[3 * i + 2]};
+    std::vector<int> FF(F, F + 3 * (size_t)nf);
+    const MassOut o = surface ? mass_surface_model(P, FF, thickness) : mass_volume_model(P, FF);
+    out13[0] = o.volume;
+    out13[1] = o.com.x;
+    out13[2] = o.com.y;
+    out13[3] = o.com.z;
+    for (int k = 0; k < 9; k++) out13[4 + k] = o.unit_inertia.m[k / 3][k % 3];
 }
 
 // Replaces the warm-start store (a state taken from another run).

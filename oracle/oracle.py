@@ -71,6 +71,16 @@ def _d(a):
 
 
 # ----------------------------------------------------------- primitives ---
+def mass_properties(V, F, surface=False, thickness=0.01):
+    """MeshData's volume, centre of mass and unit inertia tensor (oracle/d2o_mass.hpp)."""
+    Vf = _d(V).reshape(-1, 3)
+    Ff = np.ascontiguousarray(F, dtype=np.int32).reshape(-1, 3)
+    out = np.zeros(13)
+    lib().o_mass_properties(_p(Vf, F64P), len(Vf), _p(Ff, I32P), len(Ff), int(bool(surface)), C.c_double(thickness),
+                            _p(out, F64P))
+    return out[0], out[1:4].copy(), out[4:13].reshape(3, 3).copy()
+
+
 def build_tree(V, F, rng_state):
     """SurrogateTree(V, F, opt) restated (oracle/d2o_tree.hpp) from the PCG32
     stream rng_state = (state, inc) -> (nodes [n,4], ntris, tris [n,8,9], eps,

@@ -133,7 +133,7 @@ def test_learned_proposal_in_the_ccd(ctx):
                 ctx.set_scene(gs)
                 ctx.set_ccd_proposal(mlp, th)
                 ctx.ccd_stats(reset=True)
-                c, off, _ = ctx.compare_trees_full_continuous(pairs, mt)
+                c, off, _ = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 20)  # one call
                 stats[(case, mode)] = ctx.ccd_stats(reset=True)
                 assert np.array_equal(off, ref_off), (case, mode)
                 assert np.array_equal(c.view(np.uint64), ref.view(np.uint64)), (case, mode)

@@ -263,7 +263,7 @@ def test_ccd_certificates_do_not_change_results(ctx):
             ctx.set_scene(s.copy())
             ctx.set_ccd_certificates(mode)
             ctx.ccd_stats(reset=True)
-            out[mode] = ctx.compare_trees_full_continuous(pairs, mt)
+            out[mode] = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 20)
             out[(mode, "stats")] = ctx.ccd_stats(reset=True)
     finally:
         ctx.set_ccd_certificates(True)

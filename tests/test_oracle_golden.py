@@ -259,3 +259,45 @@ def test_transformation_matrix():
 def test_inverse_of_rigid_transform():
     t = O.transformation_euler([0.3, -1.2, 2.0], [1.0, -2.0, 0.5])
     assert np.allclose(O.mat_inverse(t) @ t, np.eye(4), atol=1e-14)
+
+
+# ------------------------------------------------------------ model/test_mesh_data.cpp
+def _reference_sphere(r, res):
+    """common/primitive_geo.cpp:33-75 sphere(r, res, V, F) (UV sphere)."""
+    V = [[0.0, 0.0, r]]
+    for j in range(1, res - 1):
+        z = r * math.cos(math.pi * j / (res - 1))
+        for k in range(res):
+            s = r * math.sin(math.pi * j / (res - 1))
+            V.append([s * math.cos(2 * math.pi * k / res), s * math.sin(2 * math.pi * k / res), z])
+    V.append([0.0, 0.0, -r])
+    F = [[0, j + 1, (j + 1) % res + 1] for j in range(res)]
+    for j in range(1, res - 2):
+        for k in range(res):
+            v1, v2 = (j - 1) * res + k + 1, j * res + k + 1
+            v3, v4 = (j - 1) * res + 1 + (k + 1) % res, j * res + 1 + (k + 1) % res
+            F += [[v1, v4, v3], [v1, v2, v4]]
+    vo = 1 + (res - 3) * res
+    F += [[vo + res, vo + (j + 1) % res, vo + j] for j in range(res)]
+    return np.array(V), np.array(F, dtype=np.int32)
+
+
+CUBE2_V = np.array([[1, 1, 1], [1, 1, -1], [1, -1, 1], [1, -1, -1], [-1, 1, 1], [-1, 1, -1], [-1, -1, 1],
+                    [-1, -1, -1]], dtype=np.float64)
+CUBE2_F = np.array([[0, 2, 1], [1, 2, 3], [2, 6, 3], [3, 6, 7], [4, 5, 6], [5, 7, 6], [4, 0, 1], [4, 1, 5],
+                    [0, 4, 6], [0, 6, 2], [3, 7, 1], [7, 5, 1]], dtype=np.int32)
+
+
+def test_inertia_matrix():
+    """model/test_mesh_data.cpp:6-51: the side-2 cube's unit inertia is
+    V * 4/6 * I (to 1e-3), a solid sphere(1, 10) V * 2/5 * I and a hollow
+    sphere(1, 8) (surface model) V * 2/3 * I, both to 0.15."""
+    vol, com, I = O.mass_properties(CUBE2_V, CUBE2_F)
+    assert abs(vol - 8.0) < 1e-12 and np.abs(com).max() < 1e-12
+    assert np.abs(I - vol * (4.0 / 6.0) * np.eye(3)).max() <= 1e-3
+    V, F = _reference_sphere(1.0, 10)
+    vol, com, I = O.mass_properties(V, F)
+    assert np.abs(I - vol * 0.4 * np.eye(3)).max() <= 0.15
+    V, F = _reference_sphere(1.0, 8)
+    vol, com, I = O.mass_properties(V, F, surface=True, thickness=0.01)
+    assert np.abs(I - vol * (2.0 / 3.0) * np.eye(3)).max() <= 0.15
