@@ -438,7 +438,7 @@ def broad_phase(scene):
 
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
 CCD_STATS = ["ee_tests_cut", "newton_iters_saved", "pairs_predicted_clear", "pairs_certified", "pairs_missed",
-             "pairs_seen"]
+             "pairs_seen", "node_pairs_witnessed", "witnesses_written"]
 TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES, TUNE_SPIN_LIMIT = range(4)
 TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS,
               "solve_lanes": TUNE_SOLVE_LANES, "spin_limit": TUNE_SPIN_LIMIT}
@@ -527,6 +527,11 @@ class Context:
         _check(lib().d2g_ccd_features(self.h, _p(pairs, I32P), _p(mt, F64P), len(pairs), _p(out, F32P)))
         return out[:len(pairs)]
 
+    def set_ccd_witnesses(self, enable):
+        """Separation witnesses in every CCD call (d2g_ctx_set_ccd_witnesses;
+        results are identical either way)."""
+        _check(lib().d2g_ctx_set_ccd_witnesses(self.h, int(bool(enable))))
+
     def set_ccd_proposal(self, mlp, threshold=0.5):
         """The learned proposal in every CCD call (d2g_ctx_set_ccd_proposal):
         queries the network predicts contact-free (hit probability below
@@ -537,8 +542,8 @@ class Context:
 
     def ccd_stats(self, reset=False):
         """CCD counters (d2g_ctx_ccd_stats) as a dict."""
-        out = np.zeros(6, np.int64)
-        _check(lib().d2g_ctx_ccd_stats(self.h, int(bool(reset)), _p(out, I64P), 6))
+        out = np.zeros(len(CCD_STATS), np.int64)
+        _check(lib().d2g_ctx_ccd_stats(self.h, int(bool(reset)), _p(out, I64P), len(CCD_STATS)))
         return dict(zip(CCD_STATS, out.tolist()))
 
     def set_tuning(self, key, value):

@@ -737,6 +737,15 @@ int d2g_ctx_set_ccd_proposal(d2g_ctx* c, d2g_mlp* mlp, float threshold) {
     return D2G_OK;
 }
 
+int d2g_ctx_set_ccd_witnesses(d2g_ctx* c, int32_t enable) {
+    if (!c) {
+        set_error("null context");
+        return D2G_ERR_INVALID;
+    }
+    c->eng.witnesses = enable != 0;
+    return D2G_OK;
+}
+
 int d2g_ctx_ccd_stats(d2g_ctx* c, int32_t reset, int64_t* stats, int32_t n) {
     if (!c || !stats || n < 0) {
         set_error("null context or output");

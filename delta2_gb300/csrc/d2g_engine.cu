@@ -243,12 +243,15 @@ __global__ void k_soup_filter(int n_soup, const Entry* __restrict__ soup, const 
                               const double* __restrict__ pm, const float* __restrict__ pm32,
                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
                               const float* __restrict__ tri32, const double* __restrict__ geo_eps,
-                              const uint8_t* __restrict__ skip, int32_t* __restrict__ flags) {
+                              const uint8_t* __restrict__ skip, const uint8_t* __restrict__ eskip,
+                              int32_t* __restrict__ flags) {
     const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= n_soup) return;  // uniform per warp
     const Entry e = soup[w];
-    if (skip && skip[e.pair]) {  // a pair the root certificate proved contact-free: no slot goes on
+    // a pair the root certificate proved contact-free, or a node pair its
+    // separation witness proved clear: no slot goes on
+    if ((skip && skip[e.pair]) || (eskip && eskip[w])) {
         flags[64 * (size_t)w + lane] = 0;
         flags[64 * (size_t)w + lane + 32] = 0;
         return;
@@ -488,6 +491,166 @@ __global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const d
         skip[p] = all ? 1 : 0;
         atomicAdd(stats + 2, 1ull);
         atomicAdd(stats + (all ? 3 : 4), 1ull);
+    }
+}
+
+// ------------------------------------------------ separation witnesses -----
+// Temporal coherence of the CCD traversal (the separation witnesses of
+// collision_detection/contact_state.cpp:14-150 and full_tree_comparison.cpp:
+// 7-198, rebuilt so that results cannot change).  A witness is an axis, in
+// body a's frame, that separated a soup node pair at an earlier call.  At the
+// next call the node pair is skipped when that axis (through a's current
+// rotation) still proves every slot of the pair clear over the query's motion,
+// by the same proof as the root certificate (swept-box rejection, or
+// side-keeping vertices and a separating gap beyond the search distance);
+// a skipped node pair has no hit, so the reference would neither expand it
+// nor emit from it.  Node pairs without hits get a new witness (the axis
+// between their buckets' vertex centroids) when it proves them clear.  A
+// stale or foreign witness can only fail its check.  Table: open addressing,
+// 64-bit keys (bodies < 2^19, node ids local to their tree < 2^12; other
+// node pairs get no witness), at most 32 probes.
+__device__ __forceinline__ unsigned long long witness_key(int a, int b, int la, int lb) {
+    if (a < 0 || b < 0 || a >= (1 << 19) || b >= (1 << 19) || la < 0 || lb < 0 || la >= 4096 || lb >= 4096)
+        return 0ull;
+    return (1ull << 63) | ((unsigned long long)a << 43) | ((unsigned long long)b << 24) |
+           ((unsigned long long)la << 12) | (unsigned long long)lb;
+}
+__device__ __forceinline__ unsigned int witness_hash(unsigned long long k, int log2cap) {
+    return (unsigned int)((k * 0x9E3779B97F4A7C15ull) >> (64 - log2cap));
+}
+
+// Every AABB-passing slot of node pair e proven clear along the world axis n
+// (warp-collective; lanes 0-31 take two slots each).
+__device__ bool node_pair_clear(const Entry& e, V3 n, const double* M, const int32_t* ntris, const double* tris,
+                                double eps_a, double eps_b, double S) {
+    const int lane = threadIdx.x & 31;
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    bool clear = norm(n) > 0.0;
+    for (int h = 0; h < 2 && clear; h++) {
+        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+        if (ta >= na || tb >= nb) continue;
+        const Tri A = load_tri(tris + (size_t)e.na * 72 + ta * 9), B = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
+        if (!box_overlap(swept_box(A, M + PM_AS, M + PM_AE, eps_a), swept_box(B, M + PM_BS, M + PM_BE, eps_b)))
+            continue;
+        const V3 A0[3] = {xform_rigid(A.A, M + PM_AS), xform_rigid(A.B, M + PM_AS), xform_rigid(A.C, M + PM_AS)};
+        const V3 A1[3] = {xform_rigid(A.A, M + PM_AE), xform_rigid(A.B, M + PM_AE), xform_rigid(A.C, M + PM_AE)};
+        const V3 B0[3] = {xform_rigid(B.A, M + PM_BS), xform_rigid(B.B, M + PM_BS), xform_rigid(B.C, M + PM_BS)};
+        const V3 B1[3] = {xform_rigid(B.A, M + PM_BE), xform_rigid(B.B, M + PM_BE), xform_rigid(B.C, M + PM_BE)};
+        double mag = 0.0;
+        for (int i = 0; i < 3; i++)
+            mag = fmax(mag, fmax(fmax(fmax(fabs(A0[i].x), fabs(A0[i].y)), fabs(A0[i].z)),
+                                 fmax(fmax(fabs(B0[i].x), fabs(B0[i].y)), fabs(B0[i].z))));
+        double la, lb;
+        const double ka = tri_conditioning(A0, la), kb = tri_conditioning(B0, lb);
+        if (!(ka < 1e4) || !(kb < 1e4)) {
+            clear = false;
+            continue;
+        }
+        const double tol = 1e-9 + 1e-12 * mag;
+        const double margin = (1e-5 + 1e-9 * mag) + 6e-7 * fmax(ka * la, kb * lb);
+        if (!keeps_side(A0, A1, B0, B1, tol) || !keeps_side(B0, B1, A0, A1, tol) ||
+            !(axis_gap(n, A0, A1, B0, B1) >= S + margin))
+            clear = false;
+    }
+    return __all_sync(0xffffffffu, clear);
+}
+
+__global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
+                                const double* __restrict__ pm, const int32_t* __restrict__ mesh,
+                                const int32_t* __restrict__ mesh_node_off, const int32_t* __restrict__ ntris,
+                                const double* __restrict__ tris, const double* __restrict__ geo_eps,
+                                const float* __restrict__ search, const WitnessSlot* __restrict__ table,
+                                int log2cap, uint8_t* __restrict__ wflag, unsigned long long* __restrict__ stats) {
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;  // uniform per warp
+    const Entry e = soup[w];
+    const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
+    const unsigned long long key =
+        witness_key(a, b, e.na - mesh_node_off[mesh[a]], e.nb - mesh_node_off[mesh[b]]);
+    int found = -1;
+    if (key) {
+        const unsigned int mask = (1u << log2cap) - 1u;
+        unsigned int h = witness_hash(key, log2cap);
+        for (int probe = 0; probe < 32; probe++, h = (h + 1) & mask) {
+            const unsigned long long k = table[h].key;
+            if (k == key) {
+                found = (int)h;
+                break;
+            }
+            if (k == 0ull) break;
+        }
+    }
+    bool clear = false;
+    if (found >= 0) {
+        const double* M = pm + (size_t)PM_SIZE * e.pair;
+        const WitnessSlot& W = table[found];
+        // the axis through a's rotation at the start (rows 0-2 of its start transform)
+        const V3 loc = mk((double)W.ax, (double)W.ay, (double)W.az);
+        const V3 n_world = mk((M[PM_AS + 0] * loc.x + M[PM_AS + 1] * loc.y) + M[PM_AS + 2] * loc.z,
+                              (M[PM_AS + 4] * loc.x + M[PM_AS + 5] * loc.y) + M[PM_AS + 6] * loc.z,
+                              (M[PM_AS + 8] * loc.x + M[PM_AS + 9] * loc.y) + M[PM_AS + 10] * loc.z);
+        clear = node_pair_clear(e, n_world, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair]);
+    }
+    if (lane == 0) {
+        wflag[w] = clear ? 1 : 0;
+        if (clear) atomicAdd(stats + 6, 1ull);
+    }
+}
+
+__global__ void k_witness_make(int n, const Entry* __restrict__ soup, const int32_t* __restrict__ entry_hits,
+                               const uint8_t* __restrict__ wflag, const uint8_t* __restrict__ skip,
+                               const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                               const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
+                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
+                               const double* __restrict__ geo_eps, const float* __restrict__ search,
+                               WitnessSlot* __restrict__ table, int log2cap, unsigned long long* __restrict__ stats) {
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;  // uniform per warp
+    const Entry e = soup[w];
+    if (entry_hits[w] > 0 || wflag[w] || (skip && skip[e.pair])) return;
+    const int a = pairs[2 * e.pair], b = pairs[2 * e.pair + 1];
+    const unsigned long long key =
+        witness_key(a, b, e.na - mesh_node_off[mesh[a]], e.nb - mesh_node_off[mesh[b]]);
+    if (!key) return;
+    const double* M = pm + (size_t)PM_SIZE * e.pair;
+    // the axis between the two buckets' vertex centroids at the start
+    const int na = ntris[e.na], nb = ntris[e.nb];
+    V3 c = mk(0, 0, 0);
+    if (lane < 16) {
+        const int t = lane & 7;
+        const bool side_b = lane >= 8;
+        if (t < (side_b ? nb : na)) {
+            const Tri T = load_tri(tris + (size_t)(side_b ? e.nb : e.na) * 72 + t * 9);
+            const double* Ms = M + (side_b ? PM_BS : PM_AS);
+            const V3 s = (xform_rigid(T.A, Ms) + xform_rigid(T.B, Ms)) + xform_rigid(T.C, Ms);
+            c = s * (side_b ? 1.0 / nb : -1.0 / na);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c.x += __shfl_xor_sync(0xffffffffu, c.x, o);
+        c.y += __shfl_xor_sync(0xffffffffu, c.y, o);
+        c.z += __shfl_xor_sync(0xffffffffu, c.z, o);
+    }
+    if (!node_pair_clear(e, c, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair])) return;
+    if (lane == 0) {
+        // store the axis in a's frame: R_a^T n
+        const V3 loc = mk((M[PM_AS + 0] * c.x + M[PM_AS + 4] * c.y) + M[PM_AS + 8] * c.z,
+                          (M[PM_AS + 1] * c.x + M[PM_AS + 5] * c.y) + M[PM_AS + 9] * c.z,
+                          (M[PM_AS + 2] * c.x + M[PM_AS + 6] * c.y) + M[PM_AS + 10] * c.z);
+        const unsigned int mask = (1u << log2cap) - 1u;
+        unsigned int h = witness_hash(key, log2cap);
+        for (int probe = 0; probe < 32; probe++, h = (h + 1) & mask) {
+            const unsigned long long old = atomicCAS(&table[h].key, 0ull, key);
+            if (old == 0ull || old == key) {
+                table[h].ax = (float)loc.x;
+                table[h].ay = (float)loc.y;
+                table[h].az = (float)loc.z;
+                atomicAdd(stats + 7, 1ull);
+                break;
+            }
+        }
     }
 }
 
@@ -1716,6 +1879,20 @@ int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_t
     return D2G_OK;
 }
 
+// The separation-witness table: allocated on first use and cleared when the
+// witnesses written since the last clearing could fill half of it (stale
+// entries only cost a failed check; clearing keeps the probes short).
+int ensure_witness_table(d2g_ctx* ctx) {
+    Engine& E = ctx->eng;
+    const size_t cap = (size_t)1 << E.wt_log2cap;
+    if (!E.wt_table.p || E.wt_inserts > (long long)(cap / 2)) {
+        RC(E.wt_table.ensure(cap));
+        D2G_CUDA(cudaMemsetAsync(E.wt_table.p, 0, sizeof(WitnessSlot) * cap, ctx->stream));
+        E.wt_inserts = 0;
+    }
+    return D2G_OK;
+}
+
 // The CCD counters live on the device across calls (one read when asked).
 int ensure_ccd_stats(d2g_ctx* ctx) {
     Engine& E = ctx->eng;
@@ -1743,6 +1920,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
     cudaStream_t s = ctx->stream;
     int64_t c_node = 0, c_tri = 0, c_leaf = 0, c_levels = 0;
     RC(ensure_ccd_stats(ctx));
+    if (E.witnesses) RC(ensure_witness_table(ctx));
     RC(E.pm.ensure((size_t)PM_SIZE * n_pairs + 1));
     RC(E.pfut.ensure(28 * (size_t)n_pairs + 1));
     RC(E.search.ensure(n_pairs + 1));
@@ -1817,8 +1995,16 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         if (n_soup > 0) {
             D2G_CUDA(cudaMemsetAsync(E.entry_hits.p, 0, sizeof(int32_t) * n_soup, s));
             const int pff = prof_begin(ctx, PROF_SOUP_FILTER, n_slots);
+            const uint8_t* eskip = nullptr;
+            if (E.witnesses) {
+                RC(E.wt_flag.ensure(n_soup + 1));
+                LAUNCH(k_witness_check, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, ctx->mesh.p,
+                       ctx->mesh_node_off.p, ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p, E.wt_table.p,
+                       E.wt_log2cap, E.wt_flag.p, E.ccd_stats.p);
+                eskip = E.wt_flag.p;
+            }
             LAUNCH(k_soup_filter, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, E.pm32c.p, ctx->ntris.p,
-                   ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, skip, E.flags.p);
+                   ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, skip, eskip, E.flags.p);
             prof_end(ctx, pff);
         }
         RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
@@ -1943,6 +2129,12 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         RC(E.cnt_b.ensure(n_soup + 1));
         RC(E.off_a.ensure(n_soup + 1));
         RC(E.off_b.ensure(n_soup + 1));
+        if (n_soup > 0 && E.witnesses) {
+            LAUNCH(k_witness_make, 32LL * n_soup, n_soup, E.soup.p, E.entry_hits.p, E.wt_flag.p, skip, d_pairs,
+                   E.pm.p, ctx->mesh.p, ctx->mesh_node_off.p, ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p,
+                   E.wt_table.p, E.wt_log2cap, E.ccd_stats.p);
+            E.wt_inserts += n_soup;
+        }
         if (n_soup > 0)
             LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1, E.cnt_a.p, E.cnt_b.p);
         RC(scan2(ctx, E.cnt_a.p, E.off_a.p, n_soup, E.cnt_b.p, E.off_b.p, n_soup));

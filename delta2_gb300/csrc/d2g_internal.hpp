@@ -113,6 +113,14 @@ struct DBuf {
     }
 };
 
+// One separation witness (d2g_engine.cu): the key of (body a, body b, node
+// of a, node of b) and a separating axis in a's frame.
+struct WitnessSlot {
+    unsigned long long key;  // 0: empty
+    float ax, ay, az;
+    int32_t unused;
+};
+
 // One frontier entry: body pair index and the two node ids.
 struct Entry {
     int32_t pair, na, nb;
@@ -214,6 +222,14 @@ struct Engine {
     // learned proposal (d2g_ctx_set_ccd_proposal): the network consulted by
     // CCD calls, the hit logit below which a pair is predicted contact-free,
     // per-pair features, predictions and skip flags
+    // separation witnesses (d2g_ctx_set_ccd_witnesses): the table of
+    // separating axes, its size, the witnesses written since it was cleared,
+    // per-entry skip flags of the current level
+    bool witnesses = false;
+    DBuf<WitnessSlot> wt_table;
+    int wt_log2cap = 20;
+    long long wt_inserts = 0;
+    DBuf<uint8_t> wt_flag;
     d2g_mlp* proposal = nullptr;
     float proposal_logit = 0.0f;
     DBuf<float> pp_feat;

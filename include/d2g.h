@@ -219,14 +219,25 @@ int d2g_ctx_set_ccd_proposal(d2g_ctx* ctx, d2g_mlp* mlp, float threshold);
  * the context's device bodies, as the proposal computes them (FP64, stored as
  * FP32; layout as d2g_mlp_predict's input): features [n][20]. */
 int d2g_ccd_features(d2g_ctx* ctx, const int32_t* pairs, const double* max_time, int32_t n_pairs, float* features);
+/* Separation witnesses (the temporal coherence of the reference's
+ * collision_detection/contact_state.cpp:14-150 and full_tree_comparison.cpp:
+ * 7-198, which are off its live path): with enable != 0 every CCD call keeps,
+ * per (body pair, node pair) of the traversal's soup stage that had no hit,
+ * an axis in the first body's frame that proved the pair separated, and at
+ * later calls skips a node pair whose axis still proves every slot clear
+ * over the query's motion (the same proof as the learned proposal's root
+ * certificate).  A skipped node pair has no hit, so results are unchanged.
+ * Off by default; the table takes 32 MiB of device memory once enabled. */
+int d2g_ctx_set_ccd_witnesses(d2g_ctx* ctx, int32_t enable);
 /* CCD counters since the context was created or last reset (reset != 0
  * clears them after reading), n of D2G_CCD_STATS entries:
  *   0 edge-edge tests cut by the certificates, 1 Newton iterations they did
  *   not run (of the reference's 10 per test), 2 pair queries the learned
  *   proposal predicted to have no contact, 3 of those the root certificate
  *   proved contact-free (skipped), 4 of those it could not prove (misses,
- *   traversed as usual), 5 pair queries seen by the proposal. */
-#define D2G_CCD_STATS 6
+ *   traversed as usual), 5 pair queries seen by the proposal, 6 node pairs
+ *   skipped by their separation witness, 7 witnesses written. */
+#define D2G_CCD_STATS 8
 int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
 /* Launch-shape settings (no reference counterpart).  They change only how
  * the work is spread over the GPU; every setting gives identical results.

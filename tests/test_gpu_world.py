@@ -276,6 +276,36 @@ def test_ccd_certificates_do_not_change_results(ctx):
     assert out[(False, "stats")]["ee_tests_cut"] == 0
 
 
+def test_separation_witnesses_keep_the_stepper_exact(ctx):
+    """Separation witnesses on: the stepper over 100 outer steps of a hull
+    scene equals the oracle in every body state after every step, and in its
+    statistics and warm-start store; the witnesses do skip node pairs (their
+    counters), and a repeated CCD call skips node pairs the first one
+    witnessed while giving the same contacts."""
+    s = D.make_scene(2, nx=3, ny=2, nz=2, spacing=1.3, speed_sigma=1.0, seed=21)
+    ctx.set_ccd_witnesses(True)
+    try:
+        ctx.ccd_stats(reset=True)
+        run_world(ctx, s, 100)
+        st = ctx.ccd_stats(reset=True)
+        assert st["witnesses_written"] > 0 and st["node_pairs_witnessed"] > 0
+        pairs = D.broad_phase(s)
+        mt = np.full(len(pairs), np.float64(np.float32(s.opt_dt)) * 2)
+        ref = O.ccd(s.copy(), pairs, mt)
+        first, second = [], []
+        for out in (first, second):
+            ctx.set_scene(s.copy())
+            ctx.ccd_stats(reset=True)
+            out.append(ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 20))
+            out.append(ctx.ccd_stats(reset=True))
+        for c, off, _ in (first[0], second[0]):
+            assert np.array_equal(off, ref[1])
+            assert np.array_equal(bits(c), bits(ref[0]))
+        assert second[1]["node_pairs_witnessed"] > 0
+    finally:
+        ctx.set_ccd_witnesses(False)
+
+
 def test_fp32_bounds_do_not_change_results(ctx):
     # the FP64-exact mode (every primitive test in FP64) and the default FP32
     # candidate bounds give the same contacts, bit for bit
