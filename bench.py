@@ -194,6 +194,45 @@ def tuned(ctx):
     return ctx
 
 
+def train_proposal(ctx, seed=0):
+    """The learned proposal's network, trained by the library's kernels on CCD
+    queries of cube scenes (delta2_gb300.learned); returns (net, seconds)."""
+    import delta2_gb300 as D
+    from delta2_gb300 import learned as L
+
+    t0 = time.perf_counter()
+    f, y = L.dataset(ctx, 60000, seed=2 * seed + 1, nx=6, ny=6, nz=6)
+    net = D.Mlp(ctx, seed=7)
+    net.set_normalization(f.mean(0), f.std(0))
+    net.train(f, y, epochs=6, batch=2048, lr=2e-3, seed=5)
+    return net, time.perf_counter() - t0
+
+
+def clone_net(net, ctx):
+    """The same network in another context (a proposal belongs to one)."""
+    import delta2_gb300 as D
+
+    other = D.Mlp(ctx, seed=0)
+    other.set_params(net.params())
+    other.set_normalization(*net._norm)
+    return other
+
+
+PLAIN = {"fp32_bounds": False, "certificates": False, "proposal": False}
+LEARNED = {"fp32_bounds": True, "certificates": True, "proposal": True}
+
+
+def configure(ctx, mode, net=None):
+    """Apply a path mode: the plain GPU path runs the reference's algorithm
+    with every primitive test in FP64 to its end; the learned path adds the
+    FP32 bounds, the conservative-advancement cut-off and the learned
+    proposal.  Results are identical in every mode."""
+    ctx.set_fp32_bounds(mode["fp32_bounds"])
+    ctx.set_ccd_certificates(mode["certificates"])
+    ctx.set_ccd_proposal(net if mode["proposal"] else None, 0.5)
+    return ctx
+
+
 def cpu_baseline(scene, pairs, mt, budget_s):
     """The oracle (single thread, the reference's serial path; host-tuned
     -O3 build) on a strided sample of the same pair list, for about budget_s
@@ -286,26 +325,43 @@ def run_ours(args):
     launches = ctx.launches() - launches0
     prof = {k: ctx.profile(k) for k in (D.PROF_SOUP_FILTER, D.PROF_SOUP_CCD, D.PROF_CONN)}
     ctx.set_profiling(False)
-    # the FP64-exact mode: every primitive test in FP64 (identical contacts)
-    ctx.set_fp32_bounds(False)
-    step()
-    exact_ms = 0.0
-    n_exact = max(2, args.steps // 4)
-    for _ in range(n_exact):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        n_exact_contacts = step()[0]
-        e1.record(stream)
-        e1.synchronize()
-        exact_ms += e0.elapsed_time(e1)
-    ctx.set_fp32_bounds(True)
-    modes = {"fp32_bounds": {"value": n_pairs * args.steps / (total_ms / 1e3), "contacts": int(n_contacts)},
-             "fp64_exact": {"value": n_pairs * n_exact / (exact_ms / 1e3), "contacts": int(n_exact_contacts),
-                            "steps": n_exact}}
+    # the same step in every path mode, contacts checked bit for bit: the
+    # plain GPU path, FP32 bounds only, + the conservative-advancement
+    # cut-off (the default, timed above), + the learned proposal
+    import hashlib
 
+    def contacts_digest():
+        c, off, _ = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 22)
+        return hashlib.sha1(np.ascontiguousarray(c).tobytes() + np.ascontiguousarray(off).tobytes()).hexdigest()
+
+    net, train_s = train_proposal(ctx, args.seed)
+    modes = {}
+    for name, mode in (("plain_gpu", PLAIN), ("fp32_bounds", {**PLAIN, "fp32_bounds": True}),
+                       ("fp32_bounds_certificates", {**LEARNED, "proposal": False}), ("learned", LEARNED)):
+        configure(ctx, mode, net)
+        step()
+        digest = contacts_digest()
+        ctx.ccd_stats(reset=True)
+        ms = 0.0
+        n_mode = max(3, args.steps // 2)
+        for _ in range(n_mode):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            n_m = step()[0]
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+        st = ctx.ccd_stats(reset=True)
+        modes[name] = {"value": n_pairs * n_mode / (ms / 1e3), "ms_per_step": ms / n_mode, "contacts": int(n_m),
+                       "contacts_sha1": digest, "steps": n_mode,
+                       "per_step": {k: v / n_mode for k, v in st.items() if v}}
+    configure(ctx, {**LEARNED, "proposal": False})
+    assert len({m["contacts_sha1"] for m in modes.values()}) == 1, "path modes gave different contacts"
+    modes["learned_vs_plain_gpu"] = modes["learned"]["value"] / modes["plain_gpu"]["value"]
+    modes["proposal_training_s"] = train_s
     max_ms = max_over_ranks(total_ms, world)
     value = replica_throughput(n_pairs * args.steps, max_ms, world)
 
@@ -315,7 +371,7 @@ def run_ours(args):
     steps_line["value"] = replica_throughput(1, max_over_ranks(steps_line["ms_per_step"], world), world)
     batch_line, batch_scenes = (None, None)
     if args.batch_scenes > 0:
-        batch_line, batch_scenes = batched_steps(local_rank, args)
+        batch_line, batch_scenes = batched_steps(local_rank, args, net)
 
     if rank != 0:
         ctx.close()
@@ -354,7 +410,13 @@ def run_ours(args):
         "config": workload_config(scene, n_pairs), "parallelism": f"replicas x{world}",
         "tuning": {D.TUNE_NAMES_INV[k]: ctx.get_tuning(k) for k in D.TUNE_NAMES_INV},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
-        "kernel_time_share": kernel_share, "precision_modes": modes, "world_steps": steps_line,
+        "kernel_time_share": kernel_share, "path_modes": modes, "world_steps": steps_line,
+        "learned_batched_vs_plain_gpu": None if batch_line is None else {
+            "ccd_pair_queries_per_s": batch_line["ccd"]["learned_batched_vs_plain_gpu"],
+            "steps_per_s": batch_line["learned_batched_vs_plain_gpu_steps"],
+            "identical_contacts": batch_line["ccd"]["identical_contacts"],
+            "workload": f"batched configuration, {batch_line['scenes']} scenes, {batch_line['bodies']} bodies",
+            "single_scene_ccd_learned_vs_plain_gpu": modes["learned_vs_plain_gpu"]},
         "batched_steps": batch_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
@@ -515,49 +577,131 @@ def world_steps(local_rank, args):
     return out, late, step_t
 
 
-def batched_steps(local_rank, args):
-    """The batched configuration (independent mixed scenes of 8-512 bodies,
-    one context): outer steps/s of every scene at once, and the same scenes
-    stepped one at a time on the GPU (one context each) for comparison."""
+def first_step_queries(sc):
+    """The time-step-selection CCD queries of a scene's first outer step:
+    last_dt doubled up to dt, futures projected linearly for the broad phase
+    (broad_phase_embree_cluster.cpp:126-132), max_time = min(last_dt)."""
+    import numpy as np
+
+    import delta2_gb300 as D
+
+    sc = sc.copy()
+    sc.last_dt = np.minimum(2.0 * sc.last_dt, np.float64(np.float32(sc.opt_dt)))
+    sc.fut[:, 8:11] = sc.cur[:, 8:11] + sc.last_dt[:, None] * sc.cur[:, 11:14]
+    pairs = D.broad_phase(sc)
+    return pairs, np.minimum(sc.last_dt[pairs[:, 0]], sc.last_dt[pairs[:, 1]])
+
+
+def batched_steps(local_rank, args, net):
+    """The batched configuration (independent mixed scenes of 8-512 bodies):
+    the benchmark spec's comparison of the learned+batched path (every scene in
+    one context, FP32 bounds, conservative-advancement cut-off, learned
+    proposal) with the plain GPU path (one context per scene, every primitive
+    test in FP64 to its end, no proposal), in outer steps/s of every scene
+    and in CCD pair-queries/s of the scenes' first time-step selection; the
+    two paths' contacts are compared bit for bit."""
+    import numpy as np
+    import torch
+
     import delta2_gb300 as D
 
     t0 = time.perf_counter()
     batch, scene_of, scenes = D.make_batch(args.batch_scenes, seed=args.seed)
     build_s = time.perf_counter() - t0
+    body_off = np.concatenate([[0], np.cumsum([sc.n_bodies for sc in scenes])])
+    k = args.batch_steps
+    # ---- learned + batched
     ctx = tuned(D.Context(local_rank))
+    net_b = clone_net(net, ctx)
+    configure(ctx, LEARNED, net_b)
     ctx.set_scene(batch.copy())
     ctx.set_scenes(scene_of)
     ctx.world_configure(batch)
     ctx.world_step(max(1, min(args.warmup, 2)))
+    ctx.set_bodies(batch.copy())
+    ctx.set_scenes(scene_of)
     ctx.world_configure(batch)
+    ctx.ccd_stats(reset=True)
     l0 = ctx.launches()
     t0 = time.perf_counter()
-    ctx.world_step(args.batch_steps)
+    ctx.world_step(k)
     wall = time.perf_counter() - t0
     launches = ctx.launches() - l0
     stats = ctx.world_stats()
     phases = ctx.world_timing()
+    prop_stats = ctx.ccd_stats(reset=True)
+    # CCD of the first outer step, every scene's queries in one call
+    qs = [first_step_queries(sc) for sc in scenes]
+    g_pairs = np.concatenate([q[0] + body_off[i] for i, q in enumerate(qs)]).astype(np.int32)
+    g_mt = np.concatenate([q[1] for q in qs])
+    ctx.set_bodies(batch.copy())
+    ctx.set_scenes(scene_of)
+    d_pairs = torch.from_numpy(g_pairs).cuda()
+    d_mt = torch.from_numpy(g_mt).cuda()
+    for _ in range(2):
+        ctx.compare_trees_full_continuous_device(d_pairs.data_ptr(), d_mt.data_ptr(), len(g_pairs))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        ctx.compare_trees_full_continuous_device(d_pairs.data_ptr(), d_mt.data_ptr(), len(g_pairs))
+    torch.cuda.synchronize()
+    ccd_b = time.perf_counter() - t0
+    ref_c, ref_off, _ = ctx.compare_trees_full_continuous(g_pairs, g_mt, capacity=1 << 23)
     ctx.close()
+    # ---- plain GPU path, one scene at a time
     ctxs = []
     for sc in scenes:
-        x = tuned(D.Context(local_rank))
+        x = configure(tuned(D.Context(local_rank)), PLAIN)
         x.set_scene(sc.copy())
         x.world_configure(sc)
         x.world_step(max(1, min(args.warmup, 2)))
+        x.set_bodies(sc.copy())
+        x.world_configure(sc)
         ctxs.append(x)
     t0 = time.perf_counter()
-    for _ in range(args.batch_steps):
+    for _ in range(k):
         for x in ctxs:
             x.world_step(1)
     wall_plain = time.perf_counter() - t0
+    d_q = []
+    for x, sc, (pr, mt) in zip(ctxs, scenes, qs):
+        x.set_bodies(sc.copy())
+        d_q.append((torch.from_numpy(np.ascontiguousarray(pr, dtype=np.int32)).cuda(), torch.from_numpy(mt).cuda()))
+    for x, (dp, dm) in zip(ctxs, d_q):
+        if len(dp):
+            x.compare_trees_full_continuous_device(dp.data_ptr(), dm.data_ptr(), len(dp))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        for x, (dp, dm) in zip(ctxs, d_q):
+            if len(dp):
+                x.compare_trees_full_continuous_device(dp.data_ptr(), dm.data_ptr(), len(dp))
+    torch.cuda.synchronize()
+    ccd_p = time.perf_counter() - t0
+    same = True
+    for i, (x, (pr, mt)) in enumerate(zip(ctxs, qs)):
+        if not len(pr):
+            continue
+        c, off, _ = x.compare_trees_full_continuous(pr, mt, capacity=1 << 22)
+        p0 = len(np.concatenate([q[0] for q in qs[:i]])) if i else 0
+        rc = ref_c[ref_off[p0]:ref_off[p0 + len(pr)]].copy()
+        rc[:, 11:13] -= body_off[i]
+        same = same and np.array_equal(off, ref_off[p0:p0 + len(pr) + 1] - ref_off[p0]) and \
+            np.array_equal(c.view(np.uint64), rc.view(np.uint64))
     for x in ctxs:
         x.close()
-    k = args.batch_steps
+    n_q = len(g_pairs)
     return {"metric": "steps/s", "value": k / wall, "unit": "steps/s (every scene one outer step)",
             "scenes": len(scenes), "bodies": int(batch.n_bodies), "ms_per_step": 1e3 * wall / k,
-            "gpu_launches": launches, "build_s": build_s,
-            "one_scene_at_a_time": {"value": k / wall_plain, "unit": "steps/s", "ms_per_step": 1e3 * wall_plain / k,
-                                    "path": "one context per scene, d2g_world_step per scene in turn"},
+            "gpu_launches": launches, "build_s": build_s, "path": "learned+batched (one context, all features)",
+            "plain_gpu_one_scene_at_a_time": {"value": k / wall_plain, "unit": "steps/s",
+                                              "ms_per_step": 1e3 * wall_plain / k,
+                                              "path": "one context per scene, FP64 tests to their end, no proposal"},
+            "learned_batched_vs_plain_gpu_steps": (k / wall) / (k / wall_plain),
+            "ccd": {"pair_queries": n_q, "learned_batched": n_q * k / ccd_b, "plain_gpu": n_q * k / ccd_p,
+                    "unit": "pair-queries/s", "learned_batched_vs_plain_gpu": ccd_p / ccd_b,
+                    "contacts": int(len(ref_c)), "identical_contacts": bool(same)},
+            "proposal_per_step": {kk: v / k for kk, v in prop_stats.items() if v},
             "phase_ms_per_step": {kk: v / k for kk, v in phases.items() if kk != "reserved"},
             "stats_per_step": {kk: v / k for kk, v in stats.items()}}, scenes
 
