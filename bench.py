@@ -194,13 +194,15 @@ def tuned(ctx):
     return ctx
 
 
-def train_proposal(ctx, seed=0):
+def train_proposal(local_rank, seed=0):
     """The learned proposal's network, trained by the library's kernels on CCD
-    queries of cube scenes (delta2_gb300.learned); returns (net, seconds)."""
+    queries of cube scenes (delta2_gb300.learned) in a context of its own;
+    returns (net, seconds)."""
     import delta2_gb300 as D
     from delta2_gb300 import learned as L
 
     t0 = time.perf_counter()
+    ctx = D.Context(local_rank)
     f, y = L.dataset(ctx, 60000, seed=2 * seed + 1, nx=6, ny=6, nz=6)
     net = D.Mlp(ctx, seed=7)
     net.set_normalization(f.mean(0), f.std(0))
@@ -334,7 +336,8 @@ def run_ours(args):
         c, off, _ = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 22)
         return hashlib.sha1(np.ascontiguousarray(c).tobytes() + np.ascontiguousarray(off).tobytes()).hexdigest()
 
-    net, train_s = train_proposal(ctx, args.seed)
+    net_own, train_s = train_proposal(local_rank, args.seed)
+    net = clone_net(net_own, ctx)
     modes = {}
     for name, mode in (("plain_gpu", PLAIN), ("fp32_bounds", {**PLAIN, "fp32_bounds": True}),
                        ("fp32_bounds_certificates", {**LEARNED, "proposal": False}), ("learned", LEARNED)):
@@ -371,7 +374,7 @@ def run_ours(args):
     steps_line["value"] = replica_throughput(1, max_over_ranks(steps_line["ms_per_step"], world), world)
     batch_line, batch_scenes = (None, None)
     if args.batch_scenes > 0:
-        batch_line, batch_scenes = batched_steps(local_rank, args, net)
+        batch_line, batch_scenes = batched_steps(local_rank, args, net_own)
 
     if rank != 0:
         ctx.close()

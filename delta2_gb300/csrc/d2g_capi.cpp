@@ -762,7 +762,7 @@ int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
     }
     if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10) ||
         (key == D2G_TUNE_SOLVE_LANES && value != 0 && value != 4 && value != 16) ||
-        (key == D2G_TUNE_SPIN_LIMIT && value < 1)) {
+        ((key == D2G_TUNE_SPIN_LIMIT || key == D2G_TUNE_GRID_CONTACTS) && value < 1)) {
         set_error("tuning value out of range");
         return D2G_ERR_INVALID;
     }
@@ -904,13 +904,10 @@ int d2g_compare_trees_full_continuous_device(d2g_ctx* c, const int32_t* d_pairs,
         return D2G_ERR_INVALID;
     }
     D2G_CUDA(cudaSetDevice(c->device));
-    if (c->validated_pairs != d_pairs || c->validated_n != n_pairs) {  // index check once per pair buffer
-        std::vector<int32_t> h(2 * (size_t)n_pairs);
-        if (n_pairs) D2G_CUDA(cudaMemcpy(h.data(), d_pairs, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
-        RC(check_pairs(c, h.data(), n_pairs));
-        c->validated_pairs = d_pairs;
-        c->validated_n = n_pairs;
-    }
+    // every call checks the caller's device pairs against the current bodies
+    // (the buffer's contents, and the bodies, may have changed since the last
+    // call) before any kernel indexes by them
+    RC(d2g::check_device_pairs(c, d_pairs, n_pairs));
     int n_rec = 0;
     RC(d2g::run_ccd(c, d_pairs, d_max_time, n_pairs, &n_rec, counters));
     D2G_CUDA(cudaStreamSynchronize(c->stream));

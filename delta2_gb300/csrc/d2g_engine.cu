@@ -1893,6 +1893,32 @@ int ensure_witness_table(d2g_ctx* ctx) {
     return D2G_OK;
 }
 
+// Body indices of a device pair list inside [0, n_bodies): one flag, one read.
+__global__ void k_check_pairs(int n, const int32_t* __restrict__ pairs, int n_bodies, int32_t* __restrict__ bad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * n) return;
+    const int v = pairs[i];
+    if (v < 0 || v >= n_bodies) atomicMin(bad, i >> 1);
+}
+
+int check_device_pairs(d2g_ctx* ctx, const int32_t* d_pairs, int n) {
+    Engine& E = ctx->eng;
+    if (n <= 0) return D2G_OK;
+    RC(E.scratch_i32.ensure(1));
+    ctx->h_pinned[0] = INT32_MAX;
+    D2G_CUDA(cudaMemcpyAsync(E.scratch_i32.p, ctx->h_pinned, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    LAUNCH(k_check_pairs, 2LL * n, n, d_pairs, ctx->n_bodies, E.scratch_i32.p);
+    int32_t bad = 0;
+    const int32_t* src = E.scratch_i32.p;
+    RC(read_scalars(ctx, &src, 1, &bad));
+    if (bad != INT32_MAX) {
+        set_error("device pair " + std::to_string(bad) + " names a body outside [0, " +
+                  std::to_string(ctx->n_bodies) + ")");
+        return D2G_ERR_INVALID;
+    }
+    return D2G_OK;
+}
+
 // The CCD counters live on the device across calls (one read when asked).
 int ensure_ccd_stats(d2g_ctx* ctx) {
     Engine& E = ctx->eng;

@@ -211,7 +211,7 @@ struct Engine {
     size_t device_bytes = 0;
     int ccd_chunk = 0, np_chunk = 0;  // pair-chunk sizes that fitted the budget last time (0: whole calls)
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
-    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25};
+    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25, 16};
   // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing
@@ -281,8 +281,6 @@ struct d2g_ctx {
     d2g::Engine eng;
     d2g::WorldState* world = nullptr;  // adaptive cluster stepper (d2g_world.cpp)
     int32_t* h_pinned = nullptr;  // small pinned scratch for counts
-    const int32_t* validated_pairs = nullptr;  // device pair buffer last checked in range
-    int validated_n = -1;
 };
 
 namespace d2g {
@@ -308,6 +306,9 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
 int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_out);
 d2g_ctx* mlp_context(d2g_mlp* m);
 int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n);
+// D2G_ERR_INVALID (with a message) unless every body index of the device pair
+// list lies inside the context's bodies; one stream synchronisation.
+int check_device_pairs(d2g_ctx* ctx, const int32_t* d_pairs, int n);
 // Mass properties of many meshes (d2g_mesh.cu): out [n][22].
 int run_mass_properties(d2g_ctx* ctx, const double* d_V, const int32_t* d_F, const int32_t* d_voff,
                         const int32_t* d_foff, const uint8_t* d_surface, int n_meshes, double thickness,

@@ -1069,7 +1069,7 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
                 // about one warp of contacts per SM and wave: fewer blocks for
                 // smaller clusters keep the grid barriers cheap
                 const int nck = h_con_off[k + 1] - h_con_off[k];
-                const int G = std::max(1, std::min(G_max, std::max(8, nck / 16)));
+                const int G = std::max(1, std::min(G_max, std::max(8, nck / E.tune[D2G_TUNE_GRID_CONTACTS])));
                 void* args[] = {&k, &S, &a};
                 D2G_CUDA(cudaLaunchCooperativeKernel((const void*)k_solve_grid, dim3(G), dim3(kSolveBlock), args, 0,
                                                      s));

@@ -256,13 +256,18 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
  *     D2G_SPIN_LIMIT and leaves that solve's future states unspecified, and
  *     the context stays usable.  Unlike the settings above, a limit small
  *     enough to be reached changes the outcome: it exists to bound the wait.
+ *   D2G_TUNE_GRID_CONTACTS (default 16, >= 1): a cooperative-grid solve
+ *     takes one block per this many contacts of its cluster (at least 8
+ *     blocks, at most one per SM): fewer blocks make each grid barrier
+ *     cheaper, more spread a wide wave over more SMs.
  * delta2_gb300/autotune.py measures candidate values on a workload and
  * writes them to a file that the Python layer applies. */
 #define D2G_TUNE_EE_FIRST_ITERS 0
 #define D2G_TUNE_GRID_MIN_PARTS 1
 #define D2G_TUNE_SOLVE_LANES 2
 #define D2G_TUNE_SPIN_LIMIT 3
-#define D2G_TUNE_KEYS 4
+#define D2G_TUNE_GRID_CONTACTS 4
+#define D2G_TUNE_KEYS 5
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Memory cap (no reference counterpart): the bytes one level of a tree

@@ -36,7 +36,7 @@ def assert_bodies_equal(got, ref, where):
                                  f"gpu {getattr(got, f)[bad[0]]} oracle {getattr(ref, f)[bad[0]]}")
 
 
-def run_world(ctx, scene, steps):
+def run_world(ctx, scene, steps, skip_stats=()):
     ref = O.World(scene.copy(), scene.opt_dt, scene.gravity_z)
     gs = scene.copy()
     ctx.set_scene(gs)
@@ -45,8 +45,8 @@ def run_world(ctx, scene, steps):
         assert ref.step(1) == 0
         ctx.world_step(1)
         assert_bodies_equal(ctx.get_bodies(gs), ref.get_bodies(), f"after step {i + 1}")
-    ref_stats = ref.stats()
-    got_stats = ctx.world_stats()
+    ref_stats = {k: v for k, v in ref.stats().items() if k not in skip_stats}
+    got_stats = {k: v for k, v in ctx.world_stats().items() if k not in skip_stats}
     assert got_stats == ref_stats
     assert {k: np.float64(v).view(np.uint64) for k, v in ctx.world_warm().items()} == \
         {k: np.float64(v).view(np.uint64) for k, v in ref.warm().items()}
@@ -286,7 +286,8 @@ def test_separation_witnesses_keep_the_stepper_exact(ctx):
     ctx.set_ccd_witnesses(True)
     try:
         ctx.ccd_stats(reset=True)
-        run_world(ctx, s, 100)
+        # (skipped node pairs test no primitive pairs: only that counter may differ)
+        run_world(ctx, s, 100, skip_stats=("ccd_tri_pairs",))
         st = ctx.ccd_stats(reset=True)
         assert st["witnesses_written"] > 0 and st["node_pairs_witnessed"] > 0
         pairs = D.broad_phase(s)
