@@ -394,6 +394,7 @@ void d2g_ctx_destroy(d2g_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    d2g::mlp_orphan_all(c);  // its networks keep their memory until d2g_mlp_destroy
     d2g::world_free(c->world);
     c->world = nullptr;
     c->mesh_node_off.release();

@@ -281,6 +281,7 @@ struct d2g_ctx {
     d2g::Engine eng;
     d2g::WorldState* world = nullptr;  // adaptive cluster stepper (d2g_world.cpp)
     int32_t* h_pinned = nullptr;  // small pinned scratch for counts
+    std::vector<d2g_mlp*> nets;   // networks created on this context (orphaned when it is destroyed)
 };
 
 namespace d2g {
@@ -305,6 +306,10 @@ int run_narrowphase(d2g_ctx* ctx, const int32_t* d_pairs, int n_pairs, int* n_ou
 // feature rows, and the context the network belongs to.
 int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_out);
 d2g_ctx* mlp_context(d2g_mlp* m);
+// Detach every network of a context that is being destroyed: each keeps its
+// device memory until d2g_mlp_destroy, and its other calls report the lost
+// context.
+void mlp_orphan_all(d2g_ctx* ctx);
 int run_ccd_features(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int n);
 // D2G_ERR_INVALID (with a message) unless every body index of the device pair
 // list lies inside the context's bodies; one stream synchronisation.

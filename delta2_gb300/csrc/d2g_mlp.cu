@@ -395,7 +395,8 @@ __global__ void k_mlp_gather(int n, int n_pad, const int32_t* __restrict__ idx, 
 }  // namespace
 
 struct MlpState {
-    d2g_ctx* ctx = nullptr;
+    d2g_ctx* ctx = nullptr;  // null once the context was destroyed
+    int device = 0;
     DBuf<float> P, G, M, V, mean, inv_std, loss, F, Y, out, Z1, Z2, Fb, Yb;
     DBuf<__nv_bfloat16> W1b, W2b, W2T, W3b, X, H1, H2;
     DBuf<int32_t> perm;
@@ -504,6 +505,28 @@ int mlp_forward_device(d2g_mlp* m, const float* d_feat, int n, const float** d_o
 
 d2g_ctx* mlp_context(d2g_mlp* m) { return m->s.ctx; }
 
+void mlp_orphan_all(d2g_ctx* ctx) {
+    for (d2g_mlp* m : ctx->nets) m->s.ctx = nullptr;
+    ctx->nets.clear();
+}
+
+}  // namespace d2g
+
+namespace d2g {
+namespace {
+// A network whose context was destroyed keeps only its memory.
+int mlp_live(d2g_mlp* m) {
+    if (!m) {
+        set_error("null network");
+        return D2G_ERR_INVALID;
+    }
+    if (!m->s.ctx) {
+        set_error("the network's context was destroyed");
+        return D2G_ERR_STATE;
+    }
+    return D2G_OK;
+}
+}  // namespace
 }  // namespace d2g
 
 extern "C" {
@@ -518,6 +541,7 @@ int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out) {
     d2g_mlp* m = new d2g_mlp();
     MlpState& S = m->s;
     S.ctx = ctx;
+    S.device = ctx->device;
     int rc = D2G_OK;
     for (DBuf<float>* b : {&S.P, &S.G, &S.M, &S.V})
         if (!rc) rc = b->ensure(kParams);
@@ -557,20 +581,29 @@ int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out) {
         return rc;
     }
     D2G_CUDA(cudaStreamSynchronize(s));
+    ctx->nets.push_back(m);
     *out = m;
     return D2G_OK;
 }
 
 void d2g_mlp_destroy(d2g_mlp* m) {
     if (!m) return;
-    cudaSetDevice(m->s.ctx->device);
-    cudaStreamSynchronize(m->s.ctx->stream);
-    if (m->s.ctx->eng.proposal == m) m->s.ctx->eng.proposal = nullptr;  // the CCD stops consulting it
-    delete m;
+    cudaSetDevice(m->s.device);
+    if (d2g_ctx* c = m->s.ctx) {
+        cudaStreamSynchronize(c->stream);
+        if (c->eng.proposal == m) c->eng.proposal = nullptr;  // the CCD stops consulting it
+        for (size_t i = 0; i < c->nets.size(); i++)
+            if (c->nets[i] == m) {
+                c->nets.erase(c->nets.begin() + (long)i);
+                break;
+            }
+    }
+    delete m;  // frees the device buffers (the device is current)
 }
 
 int d2g_mlp_params(d2g_mlp* m, float* params, int32_t n) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || !params || n != kParams) {
         set_error("parameter buffer must hold D2G_MLP_PARAMS floats");
         return D2G_ERR_INVALID;
@@ -582,6 +615,7 @@ int d2g_mlp_params(d2g_mlp* m, float* params, int32_t n) {
 
 int d2g_mlp_set_params(d2g_mlp* m, const float* params, int32_t n) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || !params || n != kParams) {
         set_error("parameter buffer must hold D2G_MLP_PARAMS floats");
         return D2G_ERR_INVALID;
@@ -594,6 +628,7 @@ int d2g_mlp_set_params(d2g_mlp* m, const float* params, int32_t n) {
 
 int d2g_mlp_set_normalization(d2g_mlp* m, const float* mean, const float* std_dev) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || !mean || !std_dev) {
         set_error("null argument");
         return D2G_ERR_INVALID;
@@ -608,6 +643,7 @@ int d2g_mlp_set_normalization(d2g_mlp* m, const float* mean, const float* std_de
 
 int d2g_mlp_predict(d2g_mlp* m, const float* features, int32_t n, float* out) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || n < 0 || (n > 0 && (!features || !out))) {
         set_error("invalid arguments");
         return D2G_ERR_INVALID;
@@ -629,6 +665,7 @@ int d2g_mlp_predict(d2g_mlp* m, const float* features, int32_t n, float* out) {
 
 int d2g_mlp_gradient(d2g_mlp* m, const float* features, const float* targets, int32_t n, float* grad, float* loss) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || n <= 0 || !features || !targets || !grad || !loss) {
         set_error("invalid arguments");
         return D2G_ERR_INVALID;
@@ -651,6 +688,7 @@ int d2g_mlp_gradient(d2g_mlp* m, const float* features, const float* targets, in
 extern "C" int d2g_mlp_train(d2g_mlp* m, const float* features, const float* targets, int32_t n, int32_t epochs,
                              int32_t batch, float lr, uint64_t seed, float* epoch_loss) {
     using namespace d2g;
+    MRC(mlp_live(m));
     if (!m || n <= 0 || !features || !targets || epochs < 0 || batch <= 0) {
         set_error("invalid arguments");
         return D2G_ERR_INVALID;

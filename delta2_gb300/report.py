@@ -2,6 +2,7 @@
 per outer step, optionally compared step by step with the oracle stepper.
 
   python -m delta2_gb300.report --config 1 --steps 240 --oracle
+  python -m delta2_gb300.report --batch 256 --steps 300   # the batched configuration
 
 Energy of the moving bodies: translational 1/2 m |v|^2, rotational
 1/2 L . w with w = R I^-1 R^T L, and potential m |g| z.  Penetration: the
@@ -31,10 +32,20 @@ def energy(scene, gravity):
     return float(kin), float(pot)
 
 
-def run(config, steps, seed=0, oracle=False, every=1):
-    s = D.make_scene(config, seed=seed)
+def run(config, steps, seed=0, oracle=False, every=1, batch=0):
+    """batch > 0: the batched configuration of that many scenes (config 3's
+    mixed shapes) in one context; the broad phase of the penetration check
+    then pairs bodies of the same scene only."""
+    scene_of = None
+    if batch > 0:
+        s, scene_of, _ = D.make_batch(batch, seed=seed)
+        config = 3
+    else:
+        s = D.make_scene(config, seed=seed)
     ctx = D.Context(0)
     ctx.set_scene(s.copy())
+    if scene_of is not None:
+        ctx.set_scenes(scene_of)
     ctx.world_configure(s)
     ref = None
     if oracle:
@@ -58,7 +69,7 @@ def run(config, steps, seed=0, oracle=False, every=1):
         if i % every and i != steps - 1:
             continue
         kin, pot = energy(cur, s.gravity_z)
-        pairs = D.broad_phase(cur)
+        pairs = ctx.broad_phase_device(cur) if scene_of is not None else D.broad_phase(cur)
         con, off, _ = ctx.compare_trees_full(pairs)
         d = np.linalg.norm(con[:, 0:3] - con[:, 3:6], axis=1) if len(con) else np.zeros(0)
         moving = cur.is_static == 0
@@ -67,7 +78,7 @@ def run(config, steps, seed=0, oracle=False, every=1):
                      "penetrating": int(np.sum(d < 1e-6)), "finite": bool(np.isfinite(cur.cur).all())})
     ctx.close()
     e = np.array([r["kinetic"] + r["potential"] for r in rows])
-    out = {"config": config, "steps": steps, "bodies": int(s.n_bodies), "gpu_stepper_s": t_gpu,
+    out = {"config": config, "batch_scenes": batch, "steps": steps, "bodies": int(s.n_bodies), "gpu_stepper_s": t_gpu,
            "sim_seconds": rows[-1]["time"], "energy_start": float(e[0]), "energy_end": float(e[-1]),
            "energy_max_rise": float(np.max(e - e[0])), "max_penetrating": max(r["penetrating"] for r in rows),
            "min_contact_distance": min((r["min_contact_distance"] for r in rows
@@ -86,8 +97,9 @@ def main():
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--oracle", action="store_true")
     p.add_argument("--every", type=int, default=10)
+    p.add_argument("--batch", type=int, default=0, help="scenes of the batched configuration (0: one scene)")
     a = p.parse_args()
-    out, rows = run(a.config, a.steps, a.seed, a.oracle, a.every)
+    out, rows = run(a.config, a.steps, a.seed, a.oracle, a.every, a.batch)
     out["samples"] = rows
     print(json.dumps(out))
 

@@ -436,6 +436,9 @@ int d2g_world_timing(d2g_ctx* ctx, double* ms, int32_t n);
  * b2 [128], W3 [2][128], b3 [2].  Training is Adam (0.9, 0.999, 1e-8) over
  * shuffled mini-batches. */
 #define D2G_MLP_PARAMS 19458
+/* A network belongs to the context it was created on.  Destroying the context
+ * first is allowed: the network then keeps only its device memory (freed by
+ * d2g_mlp_destroy) and its other calls return D2G_ERR_STATE. */
 int d2g_mlp_create(d2g_ctx* ctx, uint64_t seed, d2g_mlp** out);
 void d2g_mlp_destroy(d2g_mlp* mlp);
 int d2g_mlp_params(d2g_mlp* mlp, float* params, int32_t n);

@@ -150,3 +150,17 @@ def test_learned_proposal_in_the_ccd(ctx):
     assert cn["pairs_predicted_clear"] < ca["pairs_predicted_clear"]
     assert cn["pairs_certified"] >= 0.5 * ca["pairs_certified"]
     print({f"{k[0]}/{k[1]}": v for k, v in stats.items()})
+
+
+def test_network_outlives_its_context(gpu_required):
+    """Destroying a context before its network: the network's calls report
+    the lost context (D2G_ERR_STATE) and destroying it afterwards is safe."""
+    c = D.Context(0)
+    net = D.Mlp(c, seed=1)
+    feats = np.zeros((8, 20), np.float32)
+    assert net.predict(feats).shape == (8, 2)
+    c.close()
+    with pytest.raises(D.D2GError) as e:
+        net.predict(feats)
+    assert e.value.code == -4
+    net.close()
