@@ -434,66 +434,6 @@ __device__ __forceinline__ double tri_conditioning(const V3* T, double& lmax) {
     const double k = (l0 * l1) / a2;
     return k * k;
 }
-__global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const double* __restrict__ pm,
-                               const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
-                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
-                               const double* __restrict__ geo_eps, const float* __restrict__ search,
-                               const float* __restrict__ pred, float logit_cut, uint8_t* __restrict__ skip,
-                               unsigned long long* __restrict__ stats) {
-    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (p >= n) return;  // uniform per warp
-    const bool gated = pred[2 * (size_t)p + 1] < logit_cut;  // NaN: not gated
-    if (!gated) {
-        if (lane == 0) skip[p] = 0;
-        return;
-    }
-    const int ia = pairs[2 * p], ib = pairs[2 * p + 1];
-    const int na_node = mesh_node_off[mesh[ia]], nb_node = mesh_node_off[mesh[ib]];
-    const int na = ntris[na_node], nb = ntris[nb_node];
-    const double* M = pm + (size_t)PM_SIZE * p;
-    const double S = (double)search[p];
-    bool clear = true;
-    for (int h = 0; h < 2; h++) {
-        const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
-        if (ta >= na || tb >= nb) continue;
-        const Tri A = load_tri(tris + (size_t)na_node * 72 + ta * 9), B = load_tri(tris + (size_t)nb_node * 72 + tb * 9);
-        if (!box_overlap(swept_box(A, M + PM_AS, M + PM_AE, geo_eps[ia]), swept_box(B, M + PM_BS, M + PM_BE, geo_eps[ib])))
-            continue;
-        const V3 A0[3] = {xform_rigid(A.A, M + PM_AS), xform_rigid(A.B, M + PM_AS), xform_rigid(A.C, M + PM_AS)};
-        const V3 A1[3] = {xform_rigid(A.A, M + PM_AE), xform_rigid(A.B, M + PM_AE), xform_rigid(A.C, M + PM_AE)};
-        const V3 B0[3] = {xform_rigid(B.A, M + PM_BS), xform_rigid(B.B, M + PM_BS), xform_rigid(B.C, M + PM_BS)};
-        const V3 B1[3] = {xform_rigid(B.A, M + PM_BE), xform_rigid(B.B, M + PM_BE), xform_rigid(B.C, M + PM_BE)};
-        double mag = 0.0;
-        for (int i = 0; i < 3; i++)
-            mag = fmax(mag, fmax(fmax(fmax(fabs(A0[i].x), fabs(A0[i].y)), fabs(A0[i].z)),
-                                 fmax(fmax(fabs(B0[i].x), fabs(B0[i].y)), fabs(B0[i].z))));
-        double la, lb;
-        const double ka = tri_conditioning(A0, la), kb = tri_conditioning(B0, lb);
-        if (!(ka < 1e4) || !(kb < 1e4)) {
-            clear = false;
-            continue;
-        }
-        const double tol = 1e-9 + 1e-12 * mag;
-        const double margin = (1e-5 + 1e-9 * mag) + 6e-7 * fmax(ka * la, kb * lb);
-        if (!keeps_side(A0, A1, B0, B1, tol) || !keeps_side(B0, B1, A0, A1, tol)) {
-            clear = false;
-            continue;
-        }
-        const V3 ca = (A0[0] + A0[1]) + A0[2], cb = (B0[0] + B0[1]) + B0[2];
-        double g = axis_gap(cb - ca, A0, A1, B0, B1);
-        g = fmax(g, axis_gap(cross(A0[1] - A0[0], A0[2] - A0[0]), A0, A1, B0, B1));
-        g = fmax(g, axis_gap(cross(B0[1] - B0[0], B0[2] - B0[0]), A0, A1, B0, B1));
-        if (!(g >= S + margin)) clear = false;
-    }
-    const bool all = __all_sync(0xffffffffu, clear);
-    if (lane == 0) {
-        skip[p] = all ? 1 : 0;
-        atomicAdd(stats + 2, 1ull);
-        atomicAdd(stats + (all ? 3 : 4), 1ull);
-    }
-}
-
 // ------------------------------------------------ separation witnesses -----
 // Temporal coherence of the CCD traversal (the separation witnesses of
 // collision_detection/contact_state.cpp:14-150 and full_tree_comparison.cpp:
@@ -519,23 +459,59 @@ __device__ __forceinline__ unsigned int witness_hash(unsigned long long k, int l
     return (unsigned int)((k * 0x9E3779B97F4A7C15ull) >> (64 - log2cap));
 }
 
-// Every AABB-passing slot of node pair e proven clear along the world axis n
-// (warp-collective; lanes 0-31 take two slots each).
-__device__ bool node_pair_clear(const Entry& e, V3 n, const double* M, const int32_t* ntris, const double* tris,
-                                double eps_a, double eps_b, double S) {
+// Every slot of node pair (na, nb) proven clear (warp-collective).  Lanes
+// 0-7 hold a's triangles and lanes 8-15 b's: each forms its triangle's world
+// vertices at the start and end and the reference's swept box once; every
+// lane then takes two slots, rejected by the boxes or proven by the
+// certificate from shuffled vertices.  With `axis` non-null only that world
+// axis is tried (a witness); otherwise the slot's centroid difference and
+// both face normals.
+__device__ bool slots_clear(int na_node, int nb_node, const double* M, const int32_t* ntris, const double* tris,
+                            double eps_a, double eps_b, double S, const V3* axis) {
     const int lane = threadIdx.x & 31;
-    const int na = ntris[e.na], nb = ntris[e.nb];
-    bool clear = norm(n) > 0.0;
-    for (int h = 0; h < 2 && clear; h++) {
+    const int na = ntris[na_node], nb = ntris[nb_node];
+    const bool side_b = lane >= 8;
+    const int t = lane & 7;
+    const bool own = lane < 16 && t < (side_b ? nb : na);
+    V3 v0[3], v1[3];
+    Box bx;
+    for (int k = 0; k < 3; k++) bx.lo[k] = bx.hi[k] = 0.0;
+    for (int i = 0; i < 3; i++) v0[i] = v1[i] = mk(0, 0, 0);
+    if (own) {
+        const Tri T = load_tri(tris + (size_t)(side_b ? nb_node : na_node) * 72 + t * 9);
+        const double* MS = M + (side_b ? PM_BS : PM_AS);
+        const double* ME = M + (side_b ? PM_BE : PM_AE);
+        bx = swept_box(T, MS, ME, side_b ? eps_b : eps_a);
+        v0[0] = xform_rigid(T.A, MS);
+        v0[1] = xform_rigid(T.B, MS);
+        v0[2] = xform_rigid(T.C, MS);
+        v1[0] = xform_rigid(T.A, ME);
+        v1[1] = xform_rigid(T.B, ME);
+        v1[2] = xform_rigid(T.C, ME);
+    }
+    auto sh3 = [&](V3 v, int src) {
+        return mk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                  __shfl_sync(0xffffffffu, v.z, src));
+    };
+    bool clear = true;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
         const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
-        if (ta >= na || tb >= nb) continue;
-        const Tri A = load_tri(tris + (size_t)e.na * 72 + ta * 9), B = load_tri(tris + (size_t)e.nb * 72 + tb * 9);
-        if (!box_overlap(swept_box(A, M + PM_AS, M + PM_AE, eps_a), swept_box(B, M + PM_BS, M + PM_BE, eps_b)))
-            continue;
-        const V3 A0[3] = {xform_rigid(A.A, M + PM_AS), xform_rigid(A.B, M + PM_AS), xform_rigid(A.C, M + PM_AS)};
-        const V3 A1[3] = {xform_rigid(A.A, M + PM_AE), xform_rigid(A.B, M + PM_AE), xform_rigid(A.C, M + PM_AE)};
-        const V3 B0[3] = {xform_rigid(B.A, M + PM_BS), xform_rigid(B.B, M + PM_BS), xform_rigid(B.C, M + PM_BS)};
-        const V3 B1[3] = {xform_rigid(B.A, M + PM_BE), xform_rigid(B.B, M + PM_BE), xform_rigid(B.C, M + PM_BE)};
+        Box A, B;
+        for (int k = 0; k < 3; k++) {
+            A.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], ta);
+            A.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], ta);
+            B.lo[k] = __shfl_sync(0xffffffffu, bx.lo[k], 8 + tb);
+            B.hi[k] = __shfl_sync(0xffffffffu, bx.hi[k], 8 + tb);
+        }
+        V3 A0[3], A1[3], B0[3], B1[3];
+        for (int i = 0; i < 3; i++) {
+            A0[i] = sh3(v0[i], ta);
+            A1[i] = sh3(v1[i], ta);
+            B0[i] = sh3(v0[i], 8 + tb);
+            B1[i] = sh3(v1[i], 8 + tb);
+        }
+        if (ta >= na || tb >= nb || !clear || !box_overlap(A, B)) continue;
         double mag = 0.0;
         for (int i = 0; i < 3; i++)
             mag = fmax(mag, fmax(fmax(fmax(fabs(A0[i].x), fabs(A0[i].y)), fabs(A0[i].z)),
@@ -548,11 +524,46 @@ __device__ bool node_pair_clear(const Entry& e, V3 n, const double* M, const int
         }
         const double tol = 1e-9 + 1e-12 * mag;
         const double margin = (1e-5 + 1e-9 * mag) + 6e-7 * fmax(ka * la, kb * lb);
-        if (!keeps_side(A0, A1, B0, B1, tol) || !keeps_side(B0, B1, A0, A1, tol) ||
-            !(axis_gap(n, A0, A1, B0, B1) >= S + margin))
+        if (!keeps_side(A0, A1, B0, B1, tol) || !keeps_side(B0, B1, A0, A1, tol)) {
             clear = false;
+            continue;
+        }
+        double g;
+        if (axis) {
+            g = axis_gap(*axis, A0, A1, B0, B1);
+        } else {
+            const V3 ca = (A0[0] + A0[1]) + A0[2], cb = (B0[0] + B0[1]) + B0[2];
+            g = axis_gap(cb - ca, A0, A1, B0, B1);
+            g = fmax(g, axis_gap(cross(A0[1] - A0[0], A0[2] - A0[0]), A0, A1, B0, B1));
+            g = fmax(g, axis_gap(cross(B0[1] - B0[0], B0[2] - B0[0]), A0, A1, B0, B1));
+        }
+        if (!(g >= S + margin)) clear = false;
     }
     return __all_sync(0xffffffffu, clear);
+}
+
+__global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                               const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
+                               const int32_t* __restrict__ ntris, const double* __restrict__ tris,
+                               const double* __restrict__ geo_eps, const float* __restrict__ search,
+                               const float* __restrict__ pred, float logit_cut, uint8_t* __restrict__ skip,
+                               unsigned long long* __restrict__ stats) {
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= n) return;  // uniform per warp
+    const bool gated = pred[2 * (size_t)p + 1] < logit_cut;  // NaN: not gated
+    if (!gated) {
+        if (lane == 0) skip[p] = 0;
+        return;
+    }
+    const int ia = pairs[2 * p], ib = pairs[2 * p + 1];
+    const bool all = slots_clear(mesh_node_off[mesh[ia]], mesh_node_off[mesh[ib]], pm + (size_t)PM_SIZE * p, ntris,
+                                 tris, geo_eps[ia], geo_eps[ib], (double)search[p], nullptr);
+    if (lane == 0) {
+        skip[p] = all ? 1 : 0;
+        atomicAdd(stats + 2, 1ull);
+        atomicAdd(stats + (all ? 3 : 4), 1ull);
+    }
 }
 
 __global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
@@ -590,7 +601,8 @@ __global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int
         const V3 n_world = mk((M[PM_AS + 0] * loc.x + M[PM_AS + 1] * loc.y) + M[PM_AS + 2] * loc.z,
                               (M[PM_AS + 4] * loc.x + M[PM_AS + 5] * loc.y) + M[PM_AS + 6] * loc.z,
                               (M[PM_AS + 8] * loc.x + M[PM_AS + 9] * loc.y) + M[PM_AS + 10] * loc.z);
-        clear = node_pair_clear(e, n_world, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair]);
+        clear = norm(n_world) > 0.0 &&
+                slots_clear(e.na, e.nb, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair], &n_world);
     }
     if (lane == 0) {
         wflag[w] = clear ? 1 : 0;
@@ -633,7 +645,8 @@ __global__ void k_witness_make(int n, const Entry* __restrict__ soup, const int3
         c.y += __shfl_xor_sync(0xffffffffu, c.y, o);
         c.z += __shfl_xor_sync(0xffffffffu, c.z, o);
     }
-    if (!node_pair_clear(e, c, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair])) return;
+    if (!(norm(c) > 0.0) || !slots_clear(e.na, e.nb, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair], &c))
+        return;
     if (lane == 0) {
         // store the axis in a's frame: R_a^T n
         const V3 loc = mk((M[PM_AS + 0] * c.x + M[PM_AS + 4] * c.y) + M[PM_AS + 8] * c.z,
