@@ -56,6 +56,8 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget (single thread)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-path-modes", action="store_true",
+                   help="skip the proposal's training and the per-mode timings (for short profiling runs)")
     p.add_argument("--world-steps", type=int, default=500, help="outer steps timed for steps/s (the whole run)")
     p.add_argument("--early-steps", type=int, default=24, help="the early window reported beside the whole run")
     p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched configuration (0: skip)")
@@ -336,11 +338,14 @@ def run_ours(args):
         c, off, _ = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 22)
         return hashlib.sha1(np.ascontiguousarray(c).tobytes() + np.ascontiguousarray(off).tobytes()).hexdigest()
 
-    net_own, train_s = train_proposal(local_rank, args.seed)
-    net = clone_net(net_own, ctx)
+    net_own, train_s, net = (None, 0.0, None)
+    if not args.no_path_modes:
+        net_own, train_s = train_proposal(local_rank, args.seed)
+        net = clone_net(net_own, ctx)
     modes = {}
-    for name, mode in (("plain_gpu", PLAIN), ("fp32_bounds", {**PLAIN, "fp32_bounds": True}),
-                       ("fp32_bounds_certificates", {**LEARNED, "proposal": False}), ("learned", LEARNED)):
+    for name, mode in () if args.no_path_modes else (
+            ("plain_gpu", PLAIN), ("fp32_bounds", {**PLAIN, "fp32_bounds": True}),
+            ("fp32_bounds_certificates", {**LEARNED, "proposal": False}), ("learned", LEARNED)):
         configure(ctx, mode, net)
         step()
         digest = contacts_digest()
@@ -363,8 +368,9 @@ def run_ours(args):
                        "per_step": {k: v / n_mode for k, v in st.items() if v}}
     configure(ctx, {**LEARNED, "proposal": False})
     assert len({m["contacts_sha1"] for m in modes.values()}) == 1, "path modes gave different contacts"
-    modes["learned_vs_plain_gpu"] = modes["learned"]["value"] / modes["plain_gpu"]["value"]
-    modes["proposal_training_s"] = train_s
+    if modes:
+        modes["learned_vs_plain_gpu"] = modes["learned"]["value"] / modes["plain_gpu"]["value"]
+        modes["proposal_training_s"] = train_s
     max_ms = max_over_ranks(total_ms, world)
     value = replica_throughput(n_pairs * args.steps, max_ms, world)
 
@@ -373,7 +379,7 @@ def run_ours(args):
     steps_line, steps_late, steps_per = world_steps(local_rank, args)
     steps_line["value"] = replica_throughput(1, max_over_ranks(steps_line["ms_per_step"], world), world)
     batch_line, batch_scenes = (None, None)
-    if args.batch_scenes > 0:
+    if args.batch_scenes > 0 and net_own is not None:
         batch_line, batch_scenes = batched_steps(local_rank, args, net_own)
 
     if rank != 0:
@@ -419,7 +425,7 @@ def run_ours(args):
             "steps_per_s": batch_line["learned_batched_vs_plain_gpu_steps"],
             "identical_contacts": batch_line["ccd"]["identical_contacts"],
             "workload": f"batched configuration, {batch_line['scenes']} scenes, {batch_line['bodies']} bodies",
-            "single_scene_ccd_learned_vs_plain_gpu": modes["learned_vs_plain_gpu"]},
+            "single_scene_ccd_learned_vs_plain_gpu": modes.get("learned_vs_plain_gpu")},
         "batched_steps": batch_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
