@@ -379,7 +379,8 @@ __global__ void k_ccd_features(int n, const int32_t* __restrict__ pairs, const d
 // warp per pair proves that no slot of the root node pair can hit, so the
 // query has no contacts (compareTreesFullContinuous expands only node pairs
 // with hits).  A slot is proven clear when the reference's swept-box test
-// rejects it (continuous_comparison.h:804-812, FP64 as there), or when the
+// rejects it (continuous_comparison.h:804-812; decided in FP32 beyond a
+// margin, as the swept-box filter decides it, else in FP64), or when the
 // two triangles' vertices, each on a straight line from its start to its end
 // position, stay apart over the motion:
 //   * along an axis n fixed at the start (the centroid difference, either
@@ -466,13 +467,55 @@ __device__ __forceinline__ unsigned int witness_hash(unsigned long long k, int l
 // certificate from shuffled vertices.  With `axis` non-null only that world
 // axis is tried (a witness); otherwise the slot's centroid difference and
 // both face normals.
-__device__ bool slots_clear(int na_node, int nb_node, const double* M, const int32_t* ntris, const double* tris,
-                            double eps_a, double eps_b, double S, const V3* axis) {
+__device__ bool slots_clear(int na_node, int nb_node, const double* M, const float* pm32, int pair,
+                            const int32_t* ntris, const double* tris, const float* tri32, double eps_a, double eps_b,
+                            double S, const V3* axis) {
     const int lane = threadIdx.x & 31;
     const int na = ntris[na_node], nb = ntris[nb_node];
     const bool side_b = lane >= 8;
     const int t = lane & 7;
     const bool own = lane < 16 && t < (side_b ? nb : na);
+    // The swept boxes first in FP32, as the swept-box filter forms them: a slot
+    // whose boxes are apart by more than the margin is rejected as the FP64
+    // boxes would reject it; only when some slot is not the warp goes on in FP64.
+    bool apart32[2];
+    {
+        Box32 b32;
+        box_init(b32);
+        float mag = 0.f;
+        if (own) {
+            const float* tv = tri32 + ((size_t)(side_b ? nb_node : na_node) * 8 + t) * 9;
+            const float* MS = pm32_of(pm32, pair, side_b ? P32_BS : P32_AS);
+            const float* ME = pm32_of(pm32, pair, side_b ? P32_BE : P32_AE);
+            float o[3];
+            for (int v = 0; v < 3; v++) {
+                box_add(b32, MS, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+                box_add(b32, ME, tv[3 * v], tv[3 * v + 1], tv[3 * v + 2], o, mag);
+            }
+            const float e32 = (float)(side_b ? eps_b : eps_a);
+            for (int k = 0; k < 3; k++) {
+                b32.lo[k] -= e32;
+                b32.hi[k] += e32;
+            }
+            mag += e32;
+        }
+        bool any_near = false;
+        for (int h = 0; h < 2; h++) {
+            const int sl = lane + 32 * h, ta = sl >> 3, tb = sl & 7;
+            bool apart = false;
+            const float m = 1e-4f + 4e-6f * fmaxf(__shfl_sync(0xffffffffu, mag, ta),
+                                                  __shfl_sync(0xffffffffu, mag, 8 + tb));
+            for (int k = 0; k < 3; k++) {
+                const float alo = __shfl_sync(0xffffffffu, b32.lo[k], ta), ahi = __shfl_sync(0xffffffffu, b32.hi[k], ta);
+                const float blo = __shfl_sync(0xffffffffu, b32.lo[k], 8 + tb),
+                            bhi = __shfl_sync(0xffffffffu, b32.hi[k], 8 + tb);
+                apart = apart || blo > ahi + m || alo > bhi + m;
+            }
+            apart32[h] = apart;
+            any_near = any_near || (ta < na && tb < nb && !apart);
+        }
+        if (!__any_sync(0xffffffffu, any_near)) return true;  // every slot rejected by the swept boxes
+    }
     V3 v0[3], v1[3];
     Box bx;
     for (int k = 0; k < 3; k++) bx.lo[k] = bx.hi[k] = 0.0;
@@ -511,7 +554,7 @@ __device__ bool slots_clear(int na_node, int nb_node, const double* M, const int
             B0[i] = sh3(v0[i], 8 + tb);
             B1[i] = sh3(v1[i], 8 + tb);
         }
-        if (ta >= na || tb >= nb || !clear || !box_overlap(A, B)) continue;
+        if (ta >= na || tb >= nb || !clear || apart32[h] || !box_overlap(A, B)) continue;
         double mag = 0.0;
         for (int i = 0; i < 3; i++)
             mag = fmax(mag, fmax(fmax(fmax(fabs(A0[i].x), fabs(A0[i].y)), fabs(A0[i].z)),
@@ -543,6 +586,7 @@ __device__ bool slots_clear(int na_node, int nb_node, const double* M, const int
 }
 
 __global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                               const float* __restrict__ pm32, const float* __restrict__ tri32,
                                const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
                                const int32_t* __restrict__ ntris, const double* __restrict__ tris,
                                const double* __restrict__ geo_eps, const float* __restrict__ search,
@@ -557,8 +601,8 @@ __global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const d
         return;
     }
     const int ia = pairs[2 * p], ib = pairs[2 * p + 1];
-    const bool all = slots_clear(mesh_node_off[mesh[ia]], mesh_node_off[mesh[ib]], pm + (size_t)PM_SIZE * p, ntris,
-                                 tris, geo_eps[ia], geo_eps[ib], (double)search[p], nullptr);
+    const bool all = slots_clear(mesh_node_off[mesh[ia]], mesh_node_off[mesh[ib]], pm + (size_t)PM_SIZE * p, pm32, p,
+                                 ntris, tris, tri32, geo_eps[ia], geo_eps[ib], (double)search[p], nullptr);
     if (lane == 0) {
         skip[p] = all ? 1 : 0;
         atomicAdd(stats + 2, 1ull);
@@ -567,7 +611,8 @@ __global__ void k_root_certify(int n, const int32_t* __restrict__ pairs, const d
 }
 
 __global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int32_t* __restrict__ pairs,
-                                const double* __restrict__ pm, const int32_t* __restrict__ mesh,
+                                const double* __restrict__ pm, const float* __restrict__ pm32,
+                                const float* __restrict__ tri32, const int32_t* __restrict__ mesh,
                                 const int32_t* __restrict__ mesh_node_off, const int32_t* __restrict__ ntris,
                                 const double* __restrict__ tris, const double* __restrict__ geo_eps,
                                 const float* __restrict__ search, const WitnessSlot* __restrict__ table,
@@ -601,8 +646,8 @@ __global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int
         const V3 n_world = mk((M[PM_AS + 0] * loc.x + M[PM_AS + 1] * loc.y) + M[PM_AS + 2] * loc.z,
                               (M[PM_AS + 4] * loc.x + M[PM_AS + 5] * loc.y) + M[PM_AS + 6] * loc.z,
                               (M[PM_AS + 8] * loc.x + M[PM_AS + 9] * loc.y) + M[PM_AS + 10] * loc.z);
-        clear = norm(n_world) > 0.0 &&
-                slots_clear(e.na, e.nb, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair], &n_world);
+        clear = norm(n_world) > 0.0 && slots_clear(e.na, e.nb, M, pm32, e.pair, ntris, tris, tri32, geo_eps[a],
+                                                   geo_eps[b], (double)search[e.pair], &n_world);
     }
     if (lane == 0) {
         wflag[w] = clear ? 1 : 0;
@@ -613,6 +658,7 @@ __global__ void k_witness_check(int n, const Entry* __restrict__ soup, const int
 __global__ void k_witness_make(int n, const Entry* __restrict__ soup, const int32_t* __restrict__ entry_hits,
                                const uint8_t* __restrict__ wflag, const uint8_t* __restrict__ skip,
                                const int32_t* __restrict__ pairs, const double* __restrict__ pm,
+                               const float* __restrict__ pm32, const float* __restrict__ tri32,
                                const int32_t* __restrict__ mesh, const int32_t* __restrict__ mesh_node_off,
                                const int32_t* __restrict__ ntris, const double* __restrict__ tris,
                                const double* __restrict__ geo_eps, const float* __restrict__ search,
@@ -645,7 +691,9 @@ __global__ void k_witness_make(int n, const Entry* __restrict__ soup, const int3
         c.y += __shfl_xor_sync(0xffffffffu, c.y, o);
         c.z += __shfl_xor_sync(0xffffffffu, c.z, o);
     }
-    if (!(norm(c) > 0.0) || !slots_clear(e.na, e.nb, M, ntris, tris, geo_eps[a], geo_eps[b], (double)search[e.pair], &c))
+    if (!(norm(c) > 0.0) ||
+        !slots_clear(e.na, e.nb, M, pm32, e.pair, ntris, tris, tri32, geo_eps[a], geo_eps[b], (double)search[e.pair],
+                     &c))
         return;
     if (lane == 0) {
         // store the axis in a's frame: R_a^T n
@@ -1984,7 +2032,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
                ctx->bounding_radius.p, E.pp_feat.p);
         const float* pred = nullptr;
         RC(mlp_forward_device(E.proposal, E.pp_feat.p, n_pairs, &pred));
-        LAUNCH(k_root_certify, 32LL * n_pairs, n_pairs, d_pairs, E.pm.p, ctx->mesh.p, ctx->mesh_node_off.p,
+        LAUNCH(k_root_certify, 32LL * n_pairs, n_pairs, d_pairs, E.pm.p, E.pm32c.p, ctx->tri32.p, ctx->mesh.p,
+               ctx->mesh_node_off.p,
                ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p, pred, E.proposal_logit, E.pp_skip.p,
                E.ccd_stats.p);
         LAUNCH(k_add_u64, 1, E.ccd_stats.p + 5, (unsigned long long)n_pairs);
@@ -2037,7 +2086,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             const uint8_t* eskip = nullptr;
             if (E.witnesses) {
                 RC(E.wt_flag.ensure(n_soup + 1));
-                LAUNCH(k_witness_check, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, ctx->mesh.p,
+                LAUNCH(k_witness_check, 32LL * n_soup, n_soup, E.soup.p, d_pairs, E.pm.p, E.pm32c.p, ctx->tri32.p,
+                       ctx->mesh.p,
                        ctx->mesh_node_off.p, ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p, E.wt_table.p,
                        E.wt_log2cap, E.wt_flag.p, E.ccd_stats.p);
                 eskip = E.wt_flag.p;
@@ -2170,7 +2220,7 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         RC(E.off_b.ensure(n_soup + 1));
         if (n_soup > 0 && E.witnesses) {
             LAUNCH(k_witness_make, 32LL * n_soup, n_soup, E.soup.p, E.entry_hits.p, E.wt_flag.p, skip, d_pairs,
-                   E.pm.p, ctx->mesh.p, ctx->mesh_node_off.p, ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p,
+                   E.pm.p, E.pm32c.p, ctx->tri32.p, ctx->mesh.p, ctx->mesh_node_off.p, ctx->ntris.p, ctx->tris.p, ctx->geo_eps.p, E.search.p,
                    E.wt_table.p, E.wt_log2cap, E.ccd_stats.p);
             E.wt_inserts += n_soup;
         }
