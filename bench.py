@@ -367,7 +367,7 @@ def run_ours(args):
                        "contacts_sha1": digest, "steps": n_mode,
                        "per_step": {k: v / n_mode for k, v in st.items() if v}}
     configure(ctx, {**LEARNED, "proposal": False})
-    assert len({m["contacts_sha1"] for m in modes.values()}) == 1, "path modes gave different contacts"
+    assert len({m["contacts_sha1"] for m in modes.values()}) <= 1, "path modes gave different contacts"
     if modes:
         modes["learned_vs_plain_gpu"] = modes["learned"]["value"] / modes["plain_gpu"]["value"]
         modes["proposal_training_s"] = train_s
