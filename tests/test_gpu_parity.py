@@ -246,3 +246,52 @@ def test_repeated_calls_are_identical(ctx):
     ctx.set_scene(s.copy())
     b = ctx.compare_trees_full_continuous(pairs, 0.05)[0]
     assert_bits_equal(a, b, "repeat")
+
+
+WORK_SAVING_CASES = {
+    # the benchmark workload: every broad-phase pair of the 1,024-hull scene
+    "benchmark_hulls": lambda: (lambda s: (s, broad_pairs(s), None))(D.make_scene(2)),
+    # non-convex noisy icospheres in the open box, close together and fast
+    "noisy_icospheres": lambda: (lambda s: (s, broad_pairs(s), 0.01))(
+        project_futures(D.make_scene(5, nx=2, ny=2, nz=2, spacing=1.15, speed_sigma=2.0, seed=4))),
+    # the cube configuration, close and fast
+    "cubes": lambda: (lambda s: (s, broad_pairs(s), 0.05))(D.make_scene(1, spacing=1.12, speed_sigma=3.0, seed=5)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(WORK_SAVING_CASES))
+def test_work_saving_modes_keep_the_ccd_exact(ctx, case):
+    """Every work-saving mode at once, at its most aggressive: the root
+    certificate on every query (the proposal at threshold 1, so the network's
+    prediction does not matter) and separation witnesses, over two calls (the
+    second skips node pairs the first one witnessed).  Contacts, per-pair
+    offsets and projected futures equal the oracle's bit for bit."""
+    s, pairs, mt = WORK_SAVING_CASES[case]()
+    if mt is None:
+        mt = np.minimum(s.last_dt[pairs[:, 0]], s.last_dt[pairs[:, 1]])
+    mt = np.broadcast_to(np.asarray(mt, dtype=np.float64), (len(pairs),)).copy()
+    ref_s = s.copy()
+    ref, ref_off, _, _ = O.ccd(ref_s, pairs, mt)
+    touched = np.unique(pairs.ravel())
+    net = D.Mlp(ctx, seed=1)
+    stats = []
+    try:
+        ctx.set_ccd_proposal(net, 1.0)
+        ctx.set_ccd_witnesses(True)
+        ctx.ccd_stats(reset=True)
+        for call in range(2):
+            gs = s.copy()
+            ctx.set_scene(gs)
+            c, off, _ = ctx.compare_trees_full_continuous(pairs, mt, capacity=1 << 22)
+            stats.append(ctx.ccd_stats(reset=True))
+            assert np.array_equal(off, ref_off), (case, call)
+            assert_bits_equal(c, ref, f"{case}: contacts, call {call}")
+            ctx.get_bodies(gs)
+            assert_bits_equal(gs.fut[touched], ref_s.fut[touched], f"{case}: futures, call {call}")
+    finally:
+        ctx.set_ccd_proposal(None)
+        ctx.set_ccd_witnesses(False)
+        net.close()
+    assert len(ref) > 0
+    assert stats[0]["pairs_seen"] == len(pairs)
+    print(case, stats)
