@@ -3,9 +3,9 @@
 // initInertiaDataSurface; model/inertia.cpp:20-84) for large mesh sets, such
 // as the 16,384 distinct noisy icospheres of the open-box scene.
 //
-// One thread per mesh, in the operation order of the library's host set-up
-// (host/d2g_scene.cpp mass_volume / mass_surface), so a mesh gets the same
-// bits on the GPU as on the host:
+// In the operation order of the library's host set-up (host/d2g_scene.cpp
+// mass_volume / mass_surface), so a mesh gets the same bits on the GPU as on
+// the host:
 //   * closed surfaces (volume model): the tetrahedra of the faces with the
 //     origin (the reference tetrahedralises with tetgen, absent here; the sum
 //     over face tetrahedra is the divergence theorem's exact volume
@@ -15,15 +15,18 @@
 //     the centroid-weighted centre of mass, then the point inertia tensors of
 //     the three vertices per face;
 //   * the inverse of the 3x3 tensor by cofactors.
-// Sequential per mesh: the sums keep the host's order (bit-identical), and
-// there are as many threads as meshes.
+// One warp per mesh: the lanes compute the terms of 32 faces at a time into
+// shared memory, then lane k adds accumulator k's terms face by face, so
+// every sum is the same left-to-right chain as on the host (bit-identical)
+// while the per-face arithmetic, nearly all of the FP64 work, runs 32 wide.
 #include "d2g_geom.cuh"
 #include "d2g_internal.hpp"
 
 namespace d2g {
 namespace {
 
-constexpr int kMassBlock = 64;
+constexpr int kMassWarps = 4;    // meshes per block
+constexpr int kMassStride = 29;  // terms per face slot (at most 27), odd: no bank conflicts
 
 __device__ V3 mvert(const double* V, const int32_t* F, int f, int k) {
     const double* p = V + 3 * (size_t)F[3 * (size_t)f + k];
@@ -32,7 +35,8 @@ __device__ V3 mvert(const double* V, const int32_t* F, int f, int k) {
 
 // model/inertia.cpp:20-73 tetrahedronInertiaTensor (Tonon 2005) with the
 // reference's placement of the product terms; `sign` carries the orientation.
-__device__ void tet_inertia_add(V3 a, V3 b, V3 c, V3 d, double sign, double* I) {
+// Writes the tetrahedron's 9 tensor entries (row major) to R.
+__device__ void tet_inertia_terms(V3 a, V3 b, V3 c, V3 d, double sign, double* R) {
     const double A[3] = {a.x, a.y, a.z}, B[3] = {b.x, b.y, b.z}, C[3] = {c.x, c.y, c.z}, D[3] = {d.x, d.y, d.z};
     const double detJ = dot(a - d, cross(b - d, c - d));
     auto sq = [&](int k) {
@@ -50,8 +54,15 @@ __device__ void tet_inertia_add(V3 a, V3 b, V3 c, V3 d, double sign, double* I) 
     const double iyz = -sign * detJ * pr(1, 2) / 120;
     const double ixy = -sign * detJ * pr(0, 2) / 120;
     const double ixz = -sign * detJ * pr(0, 1) / 120;
-    const double R[9] = {ixx, ixy, ixz, ixy, iyy, iyz, ixz, iyz, izz};
-    for (int k = 0; k < 9; k++) I[k] += R[k];
+    R[0] = ixx;
+    R[1] = ixy;
+    R[2] = ixz;
+    R[3] = ixy;
+    R[4] = iyy;
+    R[5] = iyz;
+    R[6] = ixz;
+    R[7] = iyz;
+    R[8] = izz;
 }
 
 __device__ void inv3_cofactor(const double* m, double* r) {
@@ -73,60 +84,101 @@ __device__ void inv3_cofactor(const double* m, double* r) {
 
 __device__ double area3(V3 A, V3 B, V3 C) { return 0.5 * norm(cross(A - C, B - C)); }
 
+// Adds the terms the warp's lanes wrote for faces [0, cnt) of a chunk to the
+// accumulator of this lane (lane < nacc), in face order; a face holds `per`
+// terms per accumulator, added in turn.
+__device__ double chain_add(double acc, const double (*T)[kMassStride], int cnt, int lane, int nacc, int per) {
+    if (lane < nacc)
+        for (int j = 0; j < cnt; j++)
+            for (int k = 0; k < per; k++) acc += T[j][per * lane + k];
+    __syncwarp();
+    return acc;
+}
+
 // out per mesh (22 doubles): volume, centre of mass (3), unit-density inertia
 // tensor about it (9, row major), its inverse (9).
-__global__ void __launch_bounds__(kMassBlock) k_mass_props(int n, const double* __restrict__ V,
-                                                           const int32_t* __restrict__ F,
-                                                           const int32_t* __restrict__ voff,
-                                                           const int32_t* __restrict__ foff,
-                                                           const uint8_t* __restrict__ surface, double thickness,
-                                                           double* __restrict__ out) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= n) return;
+__global__ void __launch_bounds__(32 * kMassWarps) k_mass_props(int n, const double* __restrict__ V,
+                                                                const int32_t* __restrict__ F,
+                                                                const int32_t* __restrict__ voff,
+                                                                const int32_t* __restrict__ foff,
+                                                                const uint8_t* __restrict__ surface, double thickness,
+                                                                double* __restrict__ out) {
+    __shared__ double terms[kMassWarps][32][kMassStride];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m = blockIdx.x * kMassWarps + warp;
+    if (m >= n) return;  // whole warps leave together
+    double(*T)[kMassStride] = terms[warp];
     const double* Vm = V + 3 * (size_t)voff[m];
     const int f0 = foff[m], f1 = foff[m + 1];
-    double vol = 0.0, I[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Ii[9];
-    V3 com = mk(0, 0, 0);
-    if (surface && surface[m]) {
-        for (int f = f0; f < f1; f++) {
-            const V3 A = mvert(Vm, F, f, 0), B = mvert(Vm, F, f, 1), C = mvert(Vm, F, f, 2);
-            const double tv = area3(A, B, C) * thickness;
-            vol += tv;
-            com = com + (((A + B) + C) * (1.0 / 3.0)) * tv;
-        }
-        com = com * (1.0 / vol);
-        for (int f = f0; f < f1; f++) {
-            const V3 A = mvert(Vm, F, f, 0) - com, B = mvert(Vm, F, f, 1) - com, C = mvert(Vm, F, f, 2) - com;
-            const double tv = area3(A, B, C) * thickness;
-            const V3 P[3] = {A, B, C};
-            for (int k = 0; k < 3; k++) {  // model/inertia.cpp:75-84 pointInertiaTensor
-                const double x = P[k].x, y = P[k].y, z = P[k].z;
-                const double pi[9] = {y * y + z * z, -x * y, -x * z, -x * y, x * x + z * z, -y * z,
-                                      -x * z, -y * z, x * x + y * y};
-                for (int j = 0; j < 9; j++) I[j] += tv * pi[j] / 3.0;
+    const bool shell = surface && surface[m];
+
+    // pass 1: lane 0 sums the volume, lanes 1..3 the centre of mass
+    double acc = 0.0;
+    for (int base = f0; base < f1; base += 32) {
+        const int f = base + lane, cnt = min(32, f1 - base);
+        if (f < f1) {
+            double* t = T[lane];
+            const V3 a = mvert(Vm, F, f, 0), b = mvert(Vm, F, f, 1), c = mvert(Vm, F, f, 2);
+            if (shell) {
+                const double tv = area3(a, b, c) * thickness;
+                const V3 w = (((a + b) + c) * (1.0 / 3.0)) * tv;
+                t[0] = tv;
+                t[1] = w.x;
+                t[2] = w.y;
+                t[3] = w.z;
+            } else {
+                const double v = dot(a, cross(b, c)) / 6.0;
+                const V3 w = ((a + b) + c) * (v / 4.0);
+                t[0] = v;
+                t[1] = w.x;
+                t[2] = w.y;
+                t[3] = w.z;
             }
         }
-    } else {
-        for (int f = f0; f < f1; f++) {
-            const V3 a = mvert(Vm, F, f, 0), b = mvert(Vm, F, f, 1), c = mvert(Vm, F, f, 2);
-            const double v = dot(a, cross(b, c)) / 6.0;
-            vol += v;
-            com = com + ((a + b) + c) * (v / 4.0);
-        }
-        com = com * (1.0 / vol);
-        for (int f = f0; f < f1; f++)
-            tet_inertia_add(mvert(Vm, F, f, 0) - com, mvert(Vm, F, f, 1) - com, mvert(Vm, F, f, 2) - com, mk(0, 0, 0),
-                            1.0, I);
+        __syncwarp();
+        acc = chain_add(acc, T, cnt, lane, 4, 1);
     }
-    inv3_cofactor(I, Ii);
-    double* o = out + 22 * (size_t)m;
-    o[0] = vol;
-    o[1] = com.x;
-    o[2] = com.y;
-    o[3] = com.z;
-    for (int k = 0; k < 9; k++) {
-        o[4 + k] = I[k];
-        o[13 + k] = Ii[k];
+    const double vol = __shfl_sync(0xffffffffu, acc, 0);
+    const double inv_vol = 1.0 / vol;
+    const V3 com = mk(__shfl_sync(0xffffffffu, acc, 1) * inv_vol, __shfl_sync(0xffffffffu, acc, 2) * inv_vol,
+                      __shfl_sync(0xffffffffu, acc, 3) * inv_vol);
+
+    // pass 2: lane k < 9 sums entry k of the inertia tensor about the centre of mass
+    acc = 0.0;
+    for (int base = f0; base < f1; base += 32) {
+        const int f = base + lane, cnt = min(32, f1 - base);
+        if (f < f1) {
+            double* t = T[lane];
+            const V3 A = mvert(Vm, F, f, 0) - com, B = mvert(Vm, F, f, 1) - com, C = mvert(Vm, F, f, 2) - com;
+            if (shell) {
+                const double tv = area3(A, B, C) * thickness;
+                const V3 P[3] = {A, B, C};
+                for (int k = 0; k < 3; k++) {  // model/inertia.cpp:75-84 pointInertiaTensor
+                    const double x = P[k].x, y = P[k].y, z = P[k].z;
+                    const double pi[9] = {y * y + z * z, -x * y, -x * z, -x * y, x * x + z * z, -y * z,
+                                          -x * z, -y * z, x * x + y * y};
+                    for (int j = 0; j < 9; j++) t[3 * j + k] = tv * pi[j] / 3.0;
+                }
+            } else {
+                tet_inertia_terms(A, B, C, mk(0, 0, 0), 1.0, t);
+            }
+        }
+        __syncwarp();
+        acc = chain_add(acc, T, cnt, lane, 9, shell ? 3 : 1);
+    }
+    double I[9], Ii[9];
+    for (int k = 0; k < 9; k++) I[k] = __shfl_sync(0xffffffffu, acc, k);
+    if (lane == 0) {
+        inv3_cofactor(I, Ii);
+        double* o = out + 22 * (size_t)m;
+        o[0] = vol;
+        o[1] = com.x;
+        o[2] = com.y;
+        o[3] = com.z;
+        for (int k = 0; k < 9; k++) {
+            o[4 + k] = I[k];
+            o[13 + k] = Ii[k];
+        }
     }
 }
 
@@ -136,7 +188,7 @@ int run_mass_properties(d2g_ctx* ctx, const double* d_V, const int32_t* d_F, con
                         const int32_t* d_foff, const uint8_t* d_surface, int n_meshes, double thickness,
                         double* d_out) {
     if (n_meshes > 0) {
-        k_mass_props<<<(n_meshes + kMassBlock - 1) / kMassBlock, kMassBlock, 0, ctx->stream>>>(
+        k_mass_props<<<(n_meshes + kMassWarps - 1) / kMassWarps, 32 * kMassWarps, 0, ctx->stream>>>(
             n_meshes, d_V, d_F, d_voff, d_foff, d_surface, thickness, d_out);
         ctx->eng.launches++;
     }

@@ -24,7 +24,13 @@ def test_device_mass_properties_match_host_and_oracle(gpu_required):
         V, F = icosphere(2 + k % 2, radius=0.3 + 0.05 * k, noise=0.2, seed=k)
         meshes.append((V + rng.normal(0, 0.3, 3), F))  # off-centre: the centre of mass is found, not assumed
         surface.append(0)
-    meshes.append(grid_mesh(4))  # a thin shell (the surface model, as static planes use)
+    for k in range(3):  # 80 faces: a chunk of 32 faces and a ragged last chunk
+        V, F = icosphere(1, radius=0.4, noise=0.3, seed=100 + k)
+        meshes.append((V + rng.normal(0, 0.3, 3), F))
+        surface.append(0)
+    meshes.append(grid_mesh(4))  # a thin shell (the surface model, as static planes use): 32 faces
+    surface.append(1)
+    meshes.append(grid_mesh(7))  # 98 faces
     surface.append(1)
     ctx = D.Context(0)
     try:
