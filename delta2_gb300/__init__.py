@@ -439,9 +439,11 @@ def broad_phase(scene):
 PROF_SOUP_FILTER, PROF_SOUP_CCD, PROF_CONN, PROF_NP, PROF_SOLVE = range(5)
 CCD_STATS = ["ee_tests_cut", "newton_iters_saved", "pairs_predicted_clear", "pairs_certified", "pairs_missed",
              "pairs_seen", "node_pairs_witnessed", "witnesses_written"]
-TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES, TUNE_SPIN_LIMIT, TUNE_GRID_CONTACTS = range(5)
+(TUNE_EE_FIRST_ITERS, TUNE_GRID_MIN_PARTS, TUNE_SOLVE_LANES, TUNE_SPIN_LIMIT, TUNE_GRID_CONTACTS,
+ TUNE_SOLVE_CLUSTER) = range(6)
 TUNE_NAMES = {"ee_first_iters": TUNE_EE_FIRST_ITERS, "grid_min_parts": TUNE_GRID_MIN_PARTS,
-              "solve_lanes": TUNE_SOLVE_LANES, "spin_limit": TUNE_SPIN_LIMIT, "grid_contacts": TUNE_GRID_CONTACTS}
+              "solve_lanes": TUNE_SOLVE_LANES, "spin_limit": TUNE_SPIN_LIMIT, "grid_contacts": TUNE_GRID_CONTACTS,
+              "solve_cluster": TUNE_SOLVE_CLUSTER}
 TUNE_NAMES_INV = {v: k for k, v in TUNE_NAMES.items()}
 
 

@@ -763,7 +763,9 @@ int d2g_ctx_set_tuning(d2g_ctx* c, int32_t key, int32_t value) {
     }
     if (value < 0 || (key == D2G_TUNE_EE_FIRST_ITERS && value > 10) ||
         (key == D2G_TUNE_SOLVE_LANES && value != 0 && value != 4 && value != 16) ||
-        ((key == D2G_TUNE_SPIN_LIMIT || key == D2G_TUNE_GRID_CONTACTS) && value < 1)) {
+        ((key == D2G_TUNE_SPIN_LIMIT || key == D2G_TUNE_GRID_CONTACTS) && value < 1) ||
+        (key == D2G_TUNE_SOLVE_CLUSTER && value != 0 && value != 1 && value != 2 && value != 4 && value != 8 &&
+         value != 16)) {
         set_error("tuning value out of range");
         return D2G_ERR_INVALID;
     }

@@ -165,7 +165,8 @@ struct Engine {
     DBuf<unsigned long long> sv_keys, sv_keys_out;
     DBuf<int32_t> sv_vals, sv_order, sv_wave_idx, sv_wave_off, sv_wave_cursor;
     DBuf<double> sv_static_imp, sv_sdelta;
-    DBuf<int32_t> sv_scon, sv_list, sv_grid;
+    DBuf<int32_t> sv_scon, sv_list, sv_grid, sv_cl_flags;
+    int sv_cl_fit[4] = {-1, -1, -1, -1};  // resident thread-block clusters of 16, 8, 4, 2 solve blocks
     DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
     // GPU broad phase (d2g_broadphase.cu)
     DBuf<float> bp_box;
@@ -211,7 +212,7 @@ struct Engine {
     size_t device_bytes = 0;
     int ccd_chunk = 0, np_chunk = 0;  // pair-chunk sizes that fitted the budget last time (0: whole calls)
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
-    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25, 16};
+    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25, 16, 0};
   // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing

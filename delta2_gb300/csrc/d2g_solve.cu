@@ -28,10 +28,10 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr int kSolveBlock = 256;
-constexpr int kGridMinContacts = 128;  // a cluster this large may take a cooperative grid
-constexpr int kGridMaxClusters = 8;    // ... when the call has at most this many clusters
-// ... and it has more parts than the context's D2G_TUNE_GRID_MIN_PARTS (default
-// 64): its waves can be wider than one block runs at full rate
+constexpr int kGridMinContacts = 128;    // a cluster this large may take a cooperative grid
+constexpr int kGridMaxClusters = 8;      // ... with more parts than D2G_TUNE_GRID_MIN_PARTS,
+                                         // when at most this many clusters qualify
+constexpr int kClusterMinContacts = 32;  // a cluster this large takes a thread-block cluster
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------ filtering ---
@@ -193,68 +193,69 @@ __device__ __forceinline__ V3 xf12(V3 p, const double* T) {
 
 __device__ __forceinline__ bool block_any(bool v) { return __syncthreads_or(v ? 1 : 0) != 0; }
 
-// Synchronisation of one cluster's solve: the threads of one block, or every
-// thread of a cooperative grid (all blocks resident) for a large cluster.
-// The grid barrier is a generation counter in global memory with the fences
-// of a grid-wide barrier; its wait is bounded, and a barrier that gives up
-// records the fact so the kernel can stop and report it.
+// Synchronisation of one cluster's solve: the threads of one block, the
+// blocks of a thread-block cluster (the hardware cluster barrier), or every
+// thread of a cooperative grid (all blocks resident) for a very large
+// cluster.  The grid barrier is a 64-bit arrival counter in global memory:
+// each block's thread 0 adds 1 with release semantics and waits, with
+// acquire loads, until the count reaches the blocks times the barriers
+// passed; the wait is bounded, and a barrier that gives up records the fact
+// so the kernel can stop and report it.
+enum SyncMode : int { kSyncBlock = 0, kSyncGrid = 1, kSyncCluster = 2 };
+
 struct SolveSync {
-    bool grid;
-    unsigned int* count;  // grid barrier arrivals
-    unsigned int* gen;    // grid barrier generation
-    int32_t* flags;       // grid: [0] fail, [1] levels, [2] static contacts, [3], [4] "moved" by parity, [5] spin error
-    unsigned int spin_limit;  // polls before a barrier wait gives up
+    int mode;
+    unsigned long long* count;  // grid barrier arrivals (monotonic within a launch)
+    unsigned long long* passed;  // grid: the block's barriers passed so far (shared memory)
+    int32_t* flags;       // [0] fail, [1] levels, [2] static contacts, [3], [4] "moved" by parity, [5] spin error
+    unsigned int spin_limit;  // polls before a grid barrier wait gives up
 };
 
-__device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
-    unsigned int v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ void red_add_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_i32(const int32_t* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ unsigned int atom_add_acq_rel_u32(unsigned int* p, unsigned int v) {
-    unsigned int old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-    return old;
-}
-__device__ __forceinline__ void st_relaxed_u32(unsigned int* p, unsigned int v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+// Every thread of the thread-block cluster; release / acquire at cluster
+// scope order the blocks' global and shared memory accesses across it.
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// Grid barrier: after __syncthreads each block's thread 0 arrives with an
-// acquire-release add (releasing its block's writes); the last to arrive
-// has acquired every block's writes, resets the count and releases the next
-// generation, which the others wait for with acquire loads.  A block reads
-// the generation before it arrives, so the value cannot move before it.
+// Grid barrier: after __syncthreads each block's thread 0 arrives with a
+// release add (releasing its block's writes) and polls with acquire loads
+// until every block has arrived as often as it has, then __syncthreads
+// hands the acquired writes to the block.  The barriers passed so far are
+// counted per block in shared memory (every block passes the same ones).
 __device__ bool solve_sync(const SolveSync& S) {
-    if (!S.grid) {
+    if (S.mode == kSyncBlock) {
         __syncthreads();
+        return true;
+    }
+    if (S.mode == kSyncCluster) {
+        cluster_barrier();
         return true;
     }
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned int my = ld_relaxed_u32(S.gen);
-        if (atom_add_acq_rel_u32(S.count, 1u) == gridDim.x - 1) {
-            st_relaxed_u32(S.count, 0u);
-            st_release_u32(S.gen, my + 1u);
-        } else {
-            unsigned int spins = 0;
-            while (ld_acquire_u32(S.gen) == my) {
-                if (++spins > S.spin_limit) {  // several seconds at the default: the other blocks are gone
-                    atomicExch(S.flags + 5, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
+        red_add_release_u64(S.count, 1ull);
+        const unsigned long long target = (unsigned long long)gridDim.x * ++*S.passed;
+        unsigned int spins = 0;
+        while (ld_acquire_u64(S.count) < target) {
+            if (++spins > S.spin_limit) {  // seconds at the default: the other blocks are gone
+                atomicExch(S.flags + 5, 1);
+                ok = 0;
+                break;
             }
         }
         s_ok = ok;
@@ -264,14 +265,15 @@ __device__ bool solve_sync(const SolveSync& S) {
 }
 
 // true when any thread of the cluster's solve passes v; slot 3 or 4 by the
-// iteration's parity (the other slot is cleared for the next iteration).
-__device__ bool solve_any(const SolveSync& S, bool v, int parity, bool* ok) {
-    if (!S.grid) return block_any(v);
+// iteration's parity (the other slot is cleared for the next iteration by
+// the first block, gb = 0).
+__device__ bool solve_any(const SolveSync& S, bool v, int parity, int gb, bool* ok) {
+    if (S.mode == kSyncBlock) return block_any(v);
     const bool blk = __syncthreads_or(v ? 1 : 0) != 0;
     if (threadIdx.x == 0 && blk) atomicOr(S.flags + 3 + parity, 1);
     *ok = solve_sync(S) && *ok;
-    const bool r = ((volatile int32_t*)S.flags)[3 + parity] != 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) S.flags[3 + (parity ^ 1)] = 0;
+    const bool r = ld_relaxed_i32(S.flags + 3 + parity) != 0;
+    if (gb == 0 && threadIdx.x == 0) S.flags[3 + (parity ^ 1)] = 0;
     return r;
 }
 
@@ -729,7 +731,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                     st3(bw[g].last_imp, now);
                 }
             }
-            converged = !solve_any(S, moved, it_n & 1, &ok);
+            converged = !solve_any(S, moved, it_n & 1, gb, &ok);
             if (!ok) {
                 if (tid == 0) status[k] = 3;
                 return;
@@ -816,7 +818,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 const int g = cl_parts[p0 + (k2 >> 1)];
                 if (!is_static[g]) integrate_one(bw[g], fut + 14 * (size_t)g, mass[g], t, k2 & 1);
             }
-            converged = !solve_any(S, big, (it_n + it_f) & 1, &ok);
+            converged = !solve_any(S, big, (it_n + it_f) & 1, gb, &ok);
             if (!ok) {
                 if (tid == 0) status[k] = 3;
                 return;
@@ -857,14 +859,32 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
 __global__ void __launch_bounds__(kSolveBlock) k_solve(int n_list, const int32_t* __restrict__ cl_list, SolveArgs a) {
     if ((int)blockIdx.x >= n_list) return;
     __shared__ int s_local[3];
-    const SolveSync S{false, nullptr, nullptr, nullptr, 0u};
+    const SolveSync S{kSyncBlock, nullptr, nullptr, nullptr, 0u};
     solve_body(cl_list ? cl_list[blockIdx.x] : (int)blockIdx.x, threadIdx.x, blockDim.x, 0, 1, s_local, S, a);
 }
 
 // Every block of a cooperative grid on cluster k (all blocks resident).
 __global__ void __launch_bounds__(kSolveBlock) k_solve_grid(int k, SolveSync S, SolveArgs a) {
+    __shared__ unsigned long long s_passed;
+    if (threadIdx.x == 0) s_passed = 0;
+    __syncthreads();
+    S.passed = &s_passed;
     solve_body(k, threadIdx.x * gridDim.x + blockIdx.x, gridDim.x * blockDim.x, blockIdx.x, gridDim.x, S.flags, S,
                a);
+}
+
+// The blocks of thread-block cluster c solve cluster cl_list[c] together
+// (every block of a hardware cluster is resident at once); flags: 16 ints
+// per hardware cluster, zeroed before the launch.
+__global__ void __launch_bounds__(kSolveBlock) k_solve_cl(const int32_t* __restrict__ cl_list,
+                                                          int32_t* __restrict__ flags, SolveArgs a) {
+    unsigned int rank, nrank, cid;
+    asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(nrank));
+    asm("mov.u32 %0, %%clusterid.x;" : "=r"(cid));
+    int32_t* f = flags + 16 * (size_t)cid;
+    const SolveSync S{kSyncCluster, nullptr, nullptr, f, 0u};
+    solve_body(cl_list[cid], threadIdx.x * nrank + rank, (int)(nrank * blockDim.x), (int)rank, (int)nrank, f, S, a);
 }
 
 // Sort key of Contact::operator< (contact.h:17-21) as orderable bits
@@ -955,6 +975,56 @@ int run_filter(d2g_ctx* ctx, const int32_t* d_off, const double* d_rec, int n_pa
     return D2G_OK;
 }
 
+// Thread-block clusters of `cs` solve blocks that can be resident at once
+// (cached per context).
+int max_solve_clusters(d2g_ctx* ctx, int cs, int* out) {
+    Engine& E = ctx->eng;
+    const int slot = cs == 16 ? 0 : cs == 8 ? 1 : cs == 4 ? 2 : 3;
+    if (E.sv_cl_fit[slot] < 0) {
+        if (cs > 8)
+            D2G_CUDA(cudaFuncSetAttribute((const void*)k_solve_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(kSolveBlock);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, (const void*)k_solve_cl, &cfg) != cudaSuccess) {
+            (void)cudaGetLastError();  // this size is not available: never chosen
+            n = 0;
+        }
+        E.sv_cl_fit[slot] = n;
+    }
+    *out = E.sv_cl_fit[slot];
+    return D2G_OK;
+}
+
+// k_solve_cl over n clusters (list d_list), cs blocks each.
+int launch_solve_cl(d2g_ctx* ctx, int cs, int n, const int32_t* d_list, int32_t* d_flags, const SolveArgs& a,
+                    cudaStream_t st) {
+    if (cs > 8)
+        D2G_CUDA(cudaFuncSetAttribute((const void*)k_solve_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(n * cs));
+    cfg.blockDim = dim3(kSolveBlock);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    D2G_CUDA(cudaLaunchKernelEx(&cfg, k_solve_cl, d_list, d_flags, a));
+    ctx->eng.launches++;
+    return D2G_OK;
+}
+
 // Solve clusters.  Contacts (14-double records in the reference's hit order,
 // clusters contiguous per d_con_off) with per-contact pair counts and warm
 // values (NaN = none).  Outputs: status / iteration counts per cluster, the
@@ -1023,33 +1093,83 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
         a.con_pair = d_con_pair;
         a.pair_warm = d_pair_warm;
         a.lanes = E.tune[D2G_TUNE_SOLVE_LANES];
-        // A large cluster among few is solved by a cooperative grid over the
-        // SMs; the others one block each.  A wave holds at most one contact
-        // per moving body; one block runs a wave of up to eight contacts at
-        // full rate (sixteen lanes each, one warp per SM sub-partition), so a
-        // cluster of more than D2G_TUNE_GRID_MIN_PARTS parts has waves wide
-        // enough to repay the grid barrier's ~3 us per wave.
-        std::vector<int32_t> small, big;
-        for (int c = 0; c < n_clusters; c++) {
+        // Where each cluster is solved.  A wave holds at most one contact per
+        // moving body and lasts about one contact's dependent FP64 chain when
+        // its warps each have an SM sub-partition to themselves: a block runs
+        // waves of up to eight contacts that way, a thread-block cluster of
+        // 16 blocks up to 128 (with a hardware barrier, ~0.2 us, between
+        // waves), a cooperative grid over all SMs any width (~1.5 us per
+        // grid barrier).  So a cluster with at least 128 contacts and more
+        // than D2G_TUNE_GRID_MIN_PARTS parts takes a grid when at most 8
+        // clusters of the call qualify (grids run one after another); any
+        // other cluster of at least 32 contacts takes a thread-block cluster
+        // (D2G_TUNE_SOLVE_CLUSTER blocks, or the most that lets every such
+        // cluster be resident at once); the rest one block each.  Blocks and
+        // thread-block clusters run side by side on two streams, the grids
+        // after them.
+        const int cl_setting = E.tune[D2G_TUNE_SOLVE_CLUSTER];
+        std::vector<int32_t> small, mid, big;
+        if (h_con_off && h_part_off)
+            for (int c = 0; c < n_clusters; c++)
+                if (h_con_off[c + 1] - h_con_off[c] >= kGridMinContacts &&
+                    h_part_off[c + 1] - h_part_off[c] > E.tune[D2G_TUNE_GRID_MIN_PARTS])
+                    big.push_back(c);
+        if ((int)big.size() > kGridMaxClusters) big.clear();
+        for (int c = 0, b = 0; c < n_clusters; c++) {
+            if (b < (int)big.size() && big[b] == c) {
+                b++;
+                continue;
+            }
             const int nck = h_con_off ? h_con_off[c + 1] - h_con_off[c] : 0;
-            const int npc = h_part_off ? h_part_off[c + 1] - h_part_off[c] : 0;
-            if (h_con_off && h_part_off && n_clusters <= kGridMaxClusters && nck >= kGridMinContacts &&
-                npc > E.tune[D2G_TUNE_GRID_MIN_PARTS])
-                big.push_back(c);
+            if (h_con_off && cl_setting != 1 && nck >= kClusterMinContacts)
+                mid.push_back(c);
             else
                 small.push_back(c);
         }
+        int cs = 1;  // blocks per thread-block cluster
+        if (!mid.empty()) {
+            if (cl_setting > 1) {
+                cs = cl_setting;
+            } else {
+                for (int cand : {16, 8, 4, 2}) {
+                    int fit = 0;
+                    RC(max_solve_clusters(ctx, cand, &fit));
+                    if (fit >= (int)mid.size()) {
+                        cs = cand;
+                        break;
+                    }
+                }
+            }
+            if (cs == 1) {  // too many to be resident at once: one block each
+                small.insert(small.end(), mid.begin(), mid.end());
+                std::sort(small.begin(), small.end());
+                mid.clear();
+            }
+        }
+        const bool all_small = mid.empty() && big.empty();
         const int pf = prof_mark_begin(ctx, PROF_SOLVE, n_con);
+        RC(E.sv_list.ensure(small.size() + mid.size() + 2));
         if (!small.empty()) {
             const int32_t* d_list = nullptr;
-            if (!big.empty()) {
-                RC(E.sv_list.ensure(small.size() + 1));
+            if (!all_small) {
                 D2G_CUDA(cudaMemcpyAsync(E.sv_list.p, small.data(), small.size() * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, s));
                 d_list = E.sv_list.p;
             }
             k_solve<<<(int)small.size(), kSolveBlock, 0, s>>>((int)small.size(), d_list, a);
             ctx->eng.launches++;
+        }
+        if (!mid.empty()) {
+            // on the second stream, beside the blocks
+            int32_t* d_mid = E.sv_list.p + small.size() + 1;
+            RC(E.sv_cl_flags.ensure(16 * mid.size() + 16));
+            D2G_CUDA(cudaMemcpyAsync(d_mid, mid.data(), mid.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+            D2G_CUDA(cudaMemsetAsync(E.sv_cl_flags.p, 0, (16 * mid.size() + 16) * sizeof(int32_t), s));
+            D2G_CUDA(cudaEventRecord(ctx->ev_fork, s));
+            D2G_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+            RC(launch_solve_cl(ctx, cs, (int)mid.size(), d_mid, E.sv_cl_flags.p, a, ctx->stream2));
+            D2G_CUDA(cudaEventRecord(ctx->ev_join, ctx->stream2));
+            D2G_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
         }
         if (!big.empty()) {
             int dev_sms = 0, per_sm = 0;
@@ -1060,9 +1180,9 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
             D2G_CUDA(cudaMemsetAsync(E.sv_grid.p, 0, (16 * big.size() + 16) * sizeof(int32_t), s));
             for (size_t b = 0; b < big.size(); b++) {
                 SolveSync S;
-                S.grid = true;
-                S.count = (unsigned int*)(E.sv_grid.p + 16 * b);
-                S.gen = (unsigned int*)(E.sv_grid.p + 16 * b + 1);
+                S.mode = kSyncGrid;
+                S.count = (unsigned long long*)(E.sv_grid.p + 16 * b);  // 8-byte aligned: 16 ints per cluster
+                S.passed = nullptr;
                 S.flags = E.sv_grid.p + 16 * b + 4;
                 S.spin_limit = (unsigned int)E.tune[D2G_TUNE_SPIN_LIMIT];
                 int k = big[b];

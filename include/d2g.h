@@ -245,8 +245,8 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
  *     edge-edge CCD test runs on one lane before the tests still running
  *     continue on four lanes each.
  *   D2G_TUNE_GRID_MIN_PARTS (default 64, >= 0): a cluster with at least 128
- *     contacts, among at most 8 clusters in a solve call, is solved by a
- *     cooperative grid over the SMs when it has more parts than this.
+ *     contacts and more parts than this is solved by a cooperative grid over
+ *     the SMs, when at most 8 clusters of the solve call qualify.
  *   D2G_TUNE_SOLVE_LANES (default 0; 0, 4 or 16): lanes per contact in the
  *     solve's normal-impulse waves; 0 takes sixteen for a wave narrow enough
  *     that its warps each have an SM sub-partition to themselves, else four.
@@ -260,6 +260,12 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
  *     takes one block per this many contacts of its cluster (at least 8
  *     blocks, at most one per SM): fewer blocks make each grid barrier
  *     cheaper, more spread a wide wave over more SMs.
+ *   D2G_TUNE_SOLVE_CLUSTER (default 0; 0, 1, 2, 4, 8 or 16): a cluster with
+ *     at least 32 contacts that does not take a grid is solved by a
+ *     thread-block cluster of this many blocks (waves between them on the
+ *     hardware cluster barrier); 0 takes the largest size at which every
+ *     such cluster of the call is resident at once (one block each when
+ *     none is), 1 solves them with one block each.
  * delta2_gb300/autotune.py measures candidate values on a workload and
  * writes them to a file that the Python layer applies. */
 #define D2G_TUNE_EE_FIRST_ITERS 0
@@ -267,7 +273,8 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
 #define D2G_TUNE_SOLVE_LANES 2
 #define D2G_TUNE_SPIN_LIMIT 3
 #define D2G_TUNE_GRID_CONTACTS 4
-#define D2G_TUNE_KEYS 5
+#define D2G_TUNE_SOLVE_CLUSTER 5
+#define D2G_TUNE_KEYS 6
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
 /* Memory cap (no reference counterpart): the bytes one level of a tree

@@ -165,22 +165,25 @@ def test_solve_matches_oracle(ctx, lanes):
         ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
 
 
-@pytest.mark.parametrize("lanes", [4, 16])
-@pytest.mark.parametrize("grid_min_parts", [128, 1000000], ids=["grid", "block"])
-def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, lanes):
+@pytest.mark.parametrize("grid_min_parts, solve_cluster, lanes", [
+    (128, 0, 4), (128, 0, 16), (1000000, 16, 4), (1000000, 16, 16), (1000000, 2, 0), (1000000, 1, 0)],
+    ids=["grid-4", "grid-16", "cluster16-4", "cluster16-16", "cluster2", "block"])
+def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, solve_cluster, lanes):
     # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling
     # at 0.5 m/s: one cluster of 144 moving bodies with hundreds of contacts,
-    # solved by the cooperative grid, or by one block when the part threshold
-    # is raised, with four or sixteen lanes per contact
-    default = ctx.get_tuning(D.TUNE_GRID_MIN_PARTS)
+    # solved by the cooperative grid (part threshold below 145), by a
+    # thread-block cluster of 16 or 2 blocks, or by one block, with four or
+    # sixteen lanes per contact (0: by wave width)
+    defaults = {k: ctx.get_tuning(k) for k in (D.TUNE_GRID_MIN_PARTS, D.TUNE_SOLVE_CLUSTER, D.TUNE_SOLVE_LANES)}
     ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, grid_min_parts)
+    ctx.set_tuning(D.TUNE_SOLVE_CLUSTER, solve_cluster)
     ctx.set_tuning(D.TUNE_SOLVE_LANES, lanes)
     s = _wide_cluster_scene()
     try:
         clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
     finally:
-        ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, default)
-        ctx.set_tuning(D.TUNE_SOLVE_LANES, 0)
+        for k, v in defaults.items():
+            ctx.set_tuning(k, v)
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
 
@@ -218,7 +221,9 @@ def test_grid_barrier_wait_runs_out_then_the_context_recovers(ctx):
     assert max(len(h) for _, _, h, _, _ in inputs) >= 128
     default = ctx.get_tuning(D.TUNE_SPIN_LIMIT)
     assert default == 1 << 25
+    parts_default = ctx.get_tuning(D.TUNE_GRID_MIN_PARTS)
     ctx.set_scene(s.copy())
+    ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, 64)  # the 145-part cluster takes the grid
     ctx.set_tuning(D.TUNE_SPIN_LIMIT, 1)
     try:
         with pytest.raises(D.D2GError, match="grid barrier") as e:
@@ -226,7 +231,10 @@ def test_grid_barrier_wait_runs_out_then_the_context_recovers(ctx):
         assert e.value.code == 3  # D2G_SPIN_LIMIT
     finally:
         ctx.set_tuning(D.TUNE_SPIN_LIMIT, default)
-    solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+    try:
+        solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+    finally:
+        ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, parts_default)
 
 
 def test_ee_first_iters_do_not_change_results(ctx):
