@@ -13,6 +13,9 @@
 //              by its Maclaurin series (30 terms) on [0, 1/2].
 //   log      : frexp reduction and log(m) = 2*atanh((m-1)/(m+1)) (set-up only).
 //   x^(3/2)  : x*sqrt(x).
+//   x / y    : with y's reciprocal known (m_div_recip), Markstein's
+//              correction of x * (1 / y); the correctly rounded quotient,
+//              the same bits as the division.
 //
 // Every kernel translation unit is compiled with -fmad=false and every host
 // unit with -ffp-contract=off, so each operation is rounded on its own and
@@ -20,6 +23,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define D2G_HD __host__ __device__ __forceinline__
@@ -162,6 +166,47 @@ inline double m_log(double x) {
     for (int n = 19; n >= 1; n--) p = 1.0 / (2.0 * n + 1.0) + z * p;
     const double ls = 2.0 * (s + (s * z) * p);
     return ls + (double)e * 0.6931471805599453;
+}
+
+// The biased exponent field of v (0 for zeros and subnormals, 2047 for
+// infinities and NaNs).
+D2G_HD uint64_t m_bits(double v) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(v);
+#else
+    uint64_t b;
+    std::memcpy(&b, &v, sizeof b);
+    return b;
+#endif
+}
+
+D2G_HD int m_exp_field(double v) { return (int)((m_bits(v) >> 52) & 0x7ff); }
+
+D2G_HD bool m_is_zero(double v) { return (m_bits(v) << 1) == 0; }
+
+// x / y rounded to nearest, given ry = 1 / y rounded to nearest (P. W.
+// Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = RN(x ry) lies
+// within one ulp of x / y, the residual r = x - q y is exact when formed by
+// one fused multiply-add, and RN(q + r ry) is the correctly rounded
+// quotient.  The argument needs q and y well inside the exponent range (so
+// r neither underflows nor overflows): for others it divides.  A zero x
+// gives q, which carries the quotient's sign.  Three FP64 operations in
+// place of a division when a divisor repeats (masses, time steps, counts).
+D2G_HD double m_div_recip(double x, double y, double ry) {
+    const double q = x * ry;
+    const int ey = m_exp_field(y);
+    if (ey < 573 || ey > 1473) return x / y;  // |y| outside [2^-450, 2^451)
+    if (m_is_zero(x)) return q;
+    const int eq = m_exp_field(q);
+    if (eq < 573 || eq > 1473) return x / y;
+#ifdef __CUDA_ARCH__
+    const double r = fma(-q, y, x);
+    return fma(r, ry, q);
+#else
+    const double r = std::fma(-q, y, x);
+    return std::fma(r, ry, q);
+#endif
 }
 
 }  // namespace d2g

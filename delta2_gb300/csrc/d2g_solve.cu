@@ -134,6 +134,7 @@ struct BodyWork {
     double T_FS[12], T_FSf[12], T_cur[12];
     double Iinv[9];  // R(fut.q) * ii * R(fut.q)^T, constant during a solve
     double imp[3], rimp[3], ioff[3], roff[3], last_imp[3];
+    double rmass;  // 1 / mass, for m_div_recip
     int last_level;
 };
 
@@ -142,6 +143,7 @@ struct ConWork {
     double local_A[3], local_B[3], n[3];
     double start_dist, mass_eff, outer, impulse, impulse_offset;
     double slop, damp_m;  // per-solve constants of the normal loop: its slop and damp * mass_eff
+    double rcnt;          // 1 / pair_cnt, for m_div_recip
     double last_fi[3], last_rot_A[3], last_rot_B[3], upd_total[3];
     int a, b, level, pair_cnt;
     int spos;  // position among the contacts touching a static body, -1 if none
@@ -169,9 +171,12 @@ __device__ void integrate_one(BodyWork& w, const double* fut, double mass, doubl
     const State f = load_state(fut);
     const V3 imp = ld3(w.imp), ioff = ld3(w.ioff), rimp = ld3(w.rimp), roff = ld3(w.roff);
     State u = f;
-    u.v = f.v + imp / mass;
-    const V3 xa = f.x + (ioff / mass) * t;
-    const V3 xb = xa + (imp / mass) * t;
+    const V3 im = mk(m_div_recip(imp.x, mass, w.rmass), m_div_recip(imp.y, mass, w.rmass),
+                     m_div_recip(imp.z, mass, w.rmass));
+    u.v = f.v + im;
+    const V3 xa = f.x + mk(m_div_recip(ioff.x, mass, w.rmass), m_div_recip(ioff.y, mass, w.rmass),
+                           m_div_recip(ioff.z, mass, w.rmass)) * t;
+    const V3 xb = xa + im * t;
     u.x = variant ? xb : xa;
     u.L = f.L + rimp;
     const V3 La = f.L + t * roff;
@@ -315,7 +320,7 @@ struct SolveArgs {
 // contacts; warps are dealt to SMs first, then to the SMs' sub-partitions,
 // as in the four-lane form.
 __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __restrict__ widx, int c0, int G,
-                                              int gb, double t, const SolveArgs& a) {
+                                              int gb, double t, double rt, const SolveArgs& a) {
     const int lane = threadIdx.x & 31;
     const int side = lane & 1, variant = (lane >> 1) & 1, c = (lane >> 2) & 3;
     const int cc = c < 3 ? c : 0;   // the w lane repeats component x in vector work
@@ -354,7 +359,7 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         const double imp1 = dmax(imp0 + dimp, 0.0);
         const double u = (-ncc) * (imp1 - imp0);
         const double pen = outer - d1;
-        const double doff = d1 < outer ? (C.damp_m * dmax(0.0, pen - C.slop)) / t : -off0;
+        const double doff = d1 < outer ? m_div_recip(C.damp_m * dmax(0.0, pen - C.slop), t, rt) : -off0;
         const double off1 = dmax(off0 + doff, 0.0);
         const double uo = (-ncc) * (off1 - off0);
         // this side's impulse sums after the contact: imp + us,
@@ -367,9 +372,9 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         // integrate_one on these sums, component cc
         const double* F = a.fut + 14 * (size_t)g;
         const double ms = a.mass[g];
-        const double im = imp / ms;
+        const double im = m_div_recip(imp, ms, W.rmass);
         const double vnew = F[11 + cc] + im;
-        const double xa = F[8 + cc] + (ioff / ms) * t;
+        const double xa = F[8 + cc] + m_div_recip(ioff, ms, W.rmass) * t;
         const double xb = xa + im * t;
         const double xnew = variant ? xb : xa;
         const double Lnew = F[5 + cc] + rimp;
@@ -468,6 +473,76 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         }                                \
     } while (0)
 
+// One chunk of a wave of the friction loop's ordered accumulation
+// (sequential_impulses.cpp:560-607) with four lanes per contact: lane bits
+// 0-1 pick the component (x, y, z; the fourth lane repeats x and writes
+// nothing), eight contacts per warp.  Each lane evaluates its component of
+// the reference's vector expressions operation for operation; the cross
+// products and norms gather the other components with shuffles.
+// Returns whether a contact of this lane's quad changed an impulse by more
+// than 1e-4 (the loop's convergence test).
+__device__ __forceinline__ bool friction_accumulate4(int base, int end4, const int32_t* __restrict__ widx,
+                                                     int w0, int c0, const SolveArgs& a) {
+    const int lane = threadIdx.x & 31, quad = lane & ~3, c = lane & 3;
+    const int cc = c < 3 ? c : 0;
+    const int c1 = cc == 2 ? 0 : cc + 1, c2 = cc == 0 ? 2 : cc - 1;  // cross: a[c1] b[c2] - a[c2] b[c1]
+    const int qq = base + lane;
+    const bool act = qq < end4;
+    ConWork& C = a.cw[c0 + widx[act ? (qq >> 2) : w0]];
+    BodyWork &A = a.bw[C.a], &B = a.bw[C.b];
+    const bool sa = a.is_static[C.a], sb = a.is_static[C.b];
+    const double cnt = (double)C.pair_cnt;
+    const double* TA = A.T_FS + 4 * cc;
+    const double* TB = B.T_FS + 4 * cc;
+    const double p1A = ((TA[0] * C.local_A[0] + TA[1] * C.local_A[1]) + TA[2] * C.local_A[2]) + TA[3] * 1.0;
+    const double p1B = ((TB[0] * C.local_B[0] + TB[1] * C.local_B[1]) + TB[2] * C.local_B[2]) + TB[3] * 1.0;
+    const double lf = C.upd_total[cc];
+    const double u = m_div_recip(lf - C.last_fi[cc], cnt, C.rcnt);
+    const double ux = shfl_d(u, quad), uy = shfl_d(u, quad | 1), uz = shfl_d(u, quad | 2);
+    const double nu = sqrt((ux * ux + uy * uy) + uz * uz);
+    // rfA = (-lf) x (p1A - xA), rfB = lf x (p1B - xB) (calc_torque with -lf)
+    const double rA = p1A - A.FS[8 + cc], rB = p1B - B.FS[8 + cc];
+    const double nlf = -lf;
+    const double rA1 = shfl_d(rA, quad | c1), rA2 = shfl_d(rA, quad | c2);
+    const double rB1 = shfl_d(rB, quad | c1), rB2 = shfl_d(rB, quad | c2);
+    const double nlf1 = shfl_d(nlf, quad | c1), nlf2 = shfl_d(nlf, quad | c2);
+    const double lf1 = shfl_d(lf, quad | c1), lf2 = shfl_d(lf, quad | c2);
+    const double rfA = nlf1 * rA2 - nlf2 * rA1;
+    const double rfB = lf1 * rB2 - lf2 * rB1;
+    const double uo = m_div_recip(0.0 - 0.0, cnt, C.rcnt);
+    const double uox = shfl_d(uo, quad), uoy = shfl_d(uo, quad | 1), uoz = shfl_d(uo, quad | 2);
+    const double nuo = sqrt((uox * uox + uoy * uoy) + uoz * uoz);
+    // roff: (-uo) x (p1A - xA) for A, uo x (p1B - xB) for B (calc_torque with uo, -uo)
+    const double nuo_ = -uo;
+    const double nuo1 = shfl_d(nuo_, quad | c1), nuo2 = shfl_d(nuo_, quad | c2);
+    const double uo1 = shfl_d(uo, quad | c1), uo2 = shfl_d(uo, quad | c2);
+    const double roA = nuo1 * rA2 - nuo2 * rA1;
+    const double roB = uo1 * rB2 - uo2 * rB1;
+    __syncwarp();
+    if (act && c < 3) {
+        C.last_fi[c] = lf;
+        double sd = 0.0;
+        if (!sa)
+            A.imp[c] = A.imp[c] + u;
+        else
+            sd = u;
+        if (!sb)
+            B.imp[c] = B.imp[c] - u;
+        else
+            sd = -u;
+        if (C.spos >= 0) a.sdelta[3 * (size_t)(c0 + C.spos) + c] = sd;
+        if (!sa) A.rimp[c] = (A.rimp[c] - C.last_rot_A[c]) + rfA;
+        if (!sb) B.rimp[c] = (B.rimp[c] - C.last_rot_B[c]) + rfB;
+        C.last_rot_A[c] = rfA;
+        C.last_rot_B[c] = rfB;
+        if (!sa) A.ioff[c] = A.ioff[c] + uo;
+        if (!sb) B.ioff[c] = B.ioff[c] - uo;
+        if (!sa) A.roff[c] = A.roff[c] + roA;
+        if (!sb) B.roff[c] = B.roff[c] + roB;
+    }
+    return act && (nu > 1e-4 || nuo > 1e-4);
+}
+
 // SequentialImpulses::solve of cluster k.  tid / nt: this thread's index
 // among the cluster's threads and their count; G blocks cooperate (G = 1 for
 // one block), gb is this block's index among them.  In a grid the indices
@@ -493,6 +568,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
     const int c0 = cl_con_off[k], c1 = cl_con_off[k + 1];
     const int nc = c1 - c0;
     const double t = cl_step[k];
+    const double rt = 1.0 / t;  // for m_div_recip
     bool ok = true;
 
     // ---- contacts in sorted order: local frames, normal mass, failure test (:109-168)
@@ -505,6 +581,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
         C.a = (int)h[11];
         C.b = (int)h[12];
         C.pair_cnt = pair_cnt[order[c0 + i]];
+        C.rcnt = 1.0 / (double)C.pair_cnt;
         C.start_dist = norm(A - B);
         if (C.start_dist < 1e-6 && t > 1e-4) atomicExch(&shv[0], 1);
         double T[16], Ti[16];
@@ -541,6 +618,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
         const int g = cl_parts[i];
         BodyWork& W = bw[g];
         const double m = mass[g];
+        W.rmass = 1.0 / m;
         const V3 f = mk(m * 0.0, m * 0.0, m * gravity_z);
         st3(W.imp, f * t);
         for (int q = 0; q < 3; q++) W.rimp[q] = W.ioff[q] = W.roff[q] = 0.0;
@@ -656,7 +734,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 // take sixteen lanes per contact, wider ones four.
                 const int wl = woff[l + 1] - woff[l];
                 if (a.lanes == 16 || (a.lanes == 0 && (wl + 1) / 2 <= 4 * G)) {
-                    normal_wave16(woff[l], woff[l + 1], widx, c0, G, gb, t, a);
+                    normal_wave16(woff[l], woff[l + 1], widx, c0, G, gb, t, rt, a);
                     SYNC();
                     continue;
                 }
@@ -692,7 +770,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                     const double imp1 = dmax(imp0 + dimp, 0.0);
                     const V3 u = (-n) * (imp1 - imp0);
                     const double pen = outer - d1;
-                    const double doff = d1 < outer ? (C.damp_m * dmax(0.0, pen - C.slop)) / t : -off0;
+                    const double doff = d1 < outer ? m_div_recip(C.damp_m * dmax(0.0, pen - C.slop), t, rt) : -off0;
                     const double off1 = dmax(off0 + doff, 0.0);
                     const V3 uo = (-n) * (off1 - off0);
                     __syncwarp();
@@ -766,8 +844,8 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 const V3 rB = ld3(h + 3) - ld3(fut + 14 * (size_t)C.b + 8);
                 const V3 tan = normalized(vt);
                 double kt = 0.0;
-                if (!sa) kt += 1.0 / mass[C.a] + quad_form(cross(rA, tan), ii + 9 * (size_t)C.a);
-                if (!sb) kt += 1.0 / mass[C.b] + quad_form(cross(rB, tan), ii + 9 * (size_t)C.b);
+                if (!sa) kt += A.rmass + quad_form(cross(rA, tan), ii + 9 * (size_t)C.a);  // 1.0 / mass
+                if (!sb) kt += B.rmass + quad_form(cross(rB, tan), ii + 9 * (size_t)C.b);
                 const double mit = kt < 1e-6 ? 0.0 : 1.0 / kt;
                 const V3 dfi = ((-vt) * mit) * 0.9;
                 V3 total = ld3(C.last_fi) + dfi;
@@ -776,41 +854,11 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
             }
             SYNC();
             bool big = false;
-            for (int l = 0; l < levels; l++) {  // pass 2: ordered accumulation
-                for (int q = woff[l] + tid; q < woff[l + 1]; q += nt) {
-                    ConWork& C = cw[c0 + widx[q]];
-                    BodyWork &A = bw[C.a], &B = bw[C.b];
-                    const bool sa = is_static[C.a], sb = is_static[C.b];
-                    const double cnt = (double)C.pair_cnt;
-                    const V3 p1A = xf12(ld3(C.local_A), A.T_FS), p1B = xf12(ld3(C.local_B), B.T_FS);
-                    const V3 u = (ld3(C.upd_total) - ld3(C.last_fi)) / cnt;
-                    st3(C.last_fi, ld3(C.upd_total));
-                    V3 sd = mk(0, 0, 0);
-                    if (!sa)
-                        st3(A.imp, ld3(A.imp) + u);
-                    else
-                        sd = u;
-                    if (!sb)
-                        st3(B.imp, ld3(B.imp) - u);
-                    else
-                        sd = -u;
-                    if (C.spos >= 0) st3(sdelta + 3 * (size_t)(c0 + C.spos), sd);
-                    if (norm(u) > 1e-4) big = true;
-                    const V3 rfA = calc_torque(ld3(C.last_fi), p1A, ld3(A.FS + 8));
-                    const V3 rfB = calc_torque(-ld3(C.last_fi), p1B, ld3(B.FS + 8));
-                    if (!sa) st3(A.rimp, ld3(A.rimp) - ld3(C.last_rot_A));
-                    if (!sb) st3(B.rimp, ld3(B.rimp) - ld3(C.last_rot_B));
-                    st3(C.last_rot_A, rfA);
-                    st3(C.last_rot_B, rfB);
-                    if (!sa) st3(A.rimp, ld3(A.rimp) + rfA);
-                    if (!sb) st3(B.rimp, ld3(B.rimp) + rfB);
-                    const V3 uo = (mk(0, 0, 0) - mk(0, 0, 0)) / cnt;
-                    if (!sa) st3(A.ioff, ld3(A.ioff) + uo);
-                    if (!sb) st3(B.ioff, ld3(B.ioff) - uo);
-                    if (norm(uo) > 1e-4) big = true;
-                    if (!sa) st3(A.roff, ld3(A.roff) + calc_torque(uo, p1A, ld3(A.FS + 8)));
-                    if (!sb) st3(B.roff, ld3(B.roff) + calc_torque(-uo, p1B, ld3(B.FS + 8)));
-                }
+            for (int l = 0; l < levels; l++) {  // pass 2: ordered accumulation, wave by wave
+                const int end4 = 4 * woff[l + 1];
+                const int wslot = (int)(threadIdx.x >> 5) * G + gb, nwarps = (int)(blockDim.x >> 5) * G;
+                for (int base = 4 * woff[l] + 32 * wslot; base < end4; base += 32 * nwarps)
+                    big = friction_accumulate4(base, end4, widx, woff[l], c0, a) || big;
                 SYNC();
             }
             // (the static bodies' impulse sums are read only by the normal loop's test)
