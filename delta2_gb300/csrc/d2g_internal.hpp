@@ -212,7 +212,7 @@ struct Engine {
     size_t device_bytes = 0;
     int ccd_chunk = 0, np_chunk = 0;  // pair-chunk sizes that fitted the budget last time (0: whole calls)
     // launch-shape settings (d2g_ctx_set_tuning): speed only, results identical
-    int tune[D2G_TUNE_KEYS] = {2, 64, 0, 1 << 25, 16, 0};
+    int tune[D2G_TUNE_KEYS] = {2, 512, 0, 1 << 25, 16, 0};
   // cub_tmp2: scans on the context's second stream
     DBuf<int32_t> scratch_i32;  // small device scalars
     // instrumentation: kernel launches issued, and optional per-kernel event timing

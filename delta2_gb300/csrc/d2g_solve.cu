@@ -305,6 +305,21 @@ struct SolveArgs {
     int lanes;  // normal-loop lanes per contact: 0 = by wave width, 4 or 16
 };
 
+// This lane's contact (index within its cluster) and body in the warp's
+// first task of a sixteen-lane wave [n0, n1), or (-1, -1) when the warp has
+// no task in it.  Loaded before the barrier that precedes the wave (the
+// schedule does not change during the loop), so the wave starts with one
+// round of loads instead of three dependent ones.
+__device__ __forceinline__ int2 wave16_first(int n0, int n1, const int32_t* __restrict__ widx, int c0, int G,
+                                             int gb, const SolveArgs& a) {
+    const int lane = threadIdx.x & 31, side = lane & 1;
+    const int wslot = (int)(threadIdx.x >> 5) * G + gb;
+    if (wslot >= (n1 - n0 + 1) >> 1) return make_int2(-1, -1);
+    const int q = n0 + 2 * wslot + (lane >> 4);
+    const int ci = widx[q < n1 ? q : n0];
+    return make_int2(ci, side ? a.cw[c0 + ci].b : a.cw[c0 + ci].a);
+}
+
 // One wave of the normal loop (sequential_impulses.cpp:239-378: per contact
 // the normal and offset impulses, then updateState :46-70 and
 // updateStateImmediate :72-96 of both bodies) with sixteen lanes per
@@ -320,7 +335,7 @@ struct SolveArgs {
 // contacts; warps are dealt to SMs first, then to the SMs' sub-partitions,
 // as in the four-lane form.
 __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __restrict__ widx, int c0, int G,
-                                              int gb, double t, double rt, const SolveArgs& a) {
+                                              int gb, double t, double rt, int2 pre, const SolveArgs& a) {
     const int lane = threadIdx.x & 31;
     const int side = lane & 1, variant = (lane >> 1) & 1, c = (lane >> 2) & 3;
     const int cc = c < 3 ? c : 0;   // the w lane repeats component x in vector work
@@ -331,8 +346,15 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
     for (int task = wslot; task < tasks; task += nwarps) {
         const int q = n0 + 2 * task + (lane >> 4);
         const bool act = q < n1;
-        ConWork& C = a.cw[c0 + widx[act ? q : n0]];
-        const int g = side ? C.b : C.a;
+        int ci, g;
+        if (task == wslot && pre.x >= 0) {  // loaded before the barrier
+            ci = pre.x;
+            g = pre.y;
+        } else {
+            ci = widx[act ? q : n0];
+            g = side ? a.cw[c0 + ci].b : a.cw[c0 + ci].a;
+        }
+        ConWork& C = a.cw[c0 + ci];
         BodyWork& W = a.bw[g];
         const bool st = a.is_static[g];
         // this side's contact point p1 = T_FS local and its velocity
@@ -372,9 +394,12 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         // integrate_one on these sums, component cc
         const double* F = a.fut + 14 * (size_t)g;
         const double ms = a.mass[g];
-        const double im = m_div_recip(imp, ms, W.rmass);
+        // imp / ms on the FS lanes, ioff / ms on the FSf lanes, then swapped
+        const double qm = m_div_recip(variant ? ioff : imp, ms, W.rmass);
+        const double qm2 = shfl_d(qm, lane ^ 2);
+        const double im = variant ? qm2 : qm, iom = variant ? qm : qm2;
         const double vnew = F[11 + cc] + im;
-        const double xa = F[8 + cc] + m_div_recip(ioff, ms, W.rmass) * t;
+        const double xa = F[8 + cc] + iom * t;
         const double xb = xa + im * t;
         const double xnew = variant ? xb : xa;
         const double Lnew = F[5 + cc] + rimp;
@@ -728,13 +753,21 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 for (int q = 0; q < 3; q++) bw[g].last_imp[q] = bw[g].imp[q];
         }
         SYNC();
+        // Narrow waves (a warp of two contacts per SM sub-partition) take
+        // sixteen lanes per contact, wider ones four.  The next wave's bounds
+        // and first sixteen-lane task are loaded before each barrier.
+        auto lanes16 = [&](int w0, int w1) { return a.lanes == 16 || (a.lanes == 0 && (w1 - w0 + 1) / 2 <= 4 * G); };
+        int n0 = woff[0], n1 = woff[1];
+        int2 pre = lanes16(n0, n1) ? wave16_first(n0, n1, widx, c0, G, gb, a) : make_int2(-1, -1);
         while (!converged && it_n < 1000) {
             for (int l = 0; l < levels; l++) {
-                // Narrow waves (a warp of two contacts per SM sub-partition)
-                // take sixteen lanes per contact, wider ones four.
-                const int wl = woff[l + 1] - woff[l];
-                if (a.lanes == 16 || (a.lanes == 0 && (wl + 1) / 2 <= 4 * G)) {
-                    normal_wave16(woff[l], woff[l + 1], widx, c0, G, gb, t, rt, a);
+                const int w0 = n0, w1 = n1;
+                const int ln = l + 1 < levels ? l + 1 : 0;
+                n0 = woff[ln];
+                n1 = woff[ln + 1];
+                if (lanes16(w0, w1)) {
+                    normal_wave16(w0, w1, widx, c0, G, gb, t, rt, pre, a);
+                    pre = lanes16(n0, n1) ? wave16_first(n0, n1, widx, c0, G, gb, a) : make_int2(-1, -1);
                     SYNC();
                     continue;
                 }
@@ -742,13 +775,13 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 // picks the body side (A, B), bit 1 the integrated state (FS,
                 // FSf).  FP64 latency, not lane count, bounds a wave, so the
                 // sides and the four integrations run side by side.
-                const int end4 = 4 * woff[l + 1];
+                const int end4 = 4 * w1;
                 const int wslot = (int)(threadIdx.x >> 5) * G + gb, nwarps = (int)(blockDim.x >> 5) * G;
-                for (int base = 4 * woff[l] + 32 * wslot; base < end4; base += 32 * nwarps) {
+                for (int base = 4 * w0 + 32 * wslot; base < end4; base += 32 * nwarps) {
                     const int lane = threadIdx.x & 31, quad = lane & ~3, side = lane & 1, variant = (lane >> 1) & 1;
                     const int qq = base + lane;
                     const bool act = qq < end4;
-                    ConWork& C = cw[c0 + widx[act ? (qq >> 2) : woff[l]]];
+                    ConWork& C = cw[c0 + widx[act ? (qq >> 2) : w0]];
                     const int g = side ? C.b : C.a;
                     BodyWork& W = bw[g];
                     const bool st = is_static[g];
@@ -790,6 +823,7 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                     __syncwarp();
                     if (act && !st) integrate_one(W, fut + 14 * (size_t)g, mass[g], t, variant);
                 }
+                pre = lanes16(n0, n1) ? wave16_first(n0, n1, widx, c0, G, gb, a) : make_int2(-1, -1);
                 SYNC();
             }
             // convergence over every particle of the cluster (:380-387)

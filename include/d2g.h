@@ -244,9 +244,9 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
  *   D2G_TUNE_EE_FIRST_ITERS (default 2, 0..10): Newton iterations an
  *     edge-edge CCD test runs on one lane before the tests still running
  *     continue on four lanes each.
- *   D2G_TUNE_GRID_MIN_PARTS (default 64, >= 0): a cluster with at least 128
- *     contacts and more parts than this is solved by a cooperative grid over
- *     the SMs, when at most 8 clusters of the solve call qualify.
+ *   D2G_TUNE_GRID_MIN_PARTS (default 512, >= 0): a cluster with at least
+ *     128 contacts and more parts than this is solved by a cooperative grid
+ *     over the SMs, when at most 8 clusters of the solve call qualify.
  *   D2G_TUNE_SOLVE_LANES (default 0; 0, 4 or 16): lanes per contact in the
  *     solve's normal-impulse waves; 0 takes sixteen for a wave narrow enough
  *     that its warps each have an SM sub-partition to themselves, else four.
