@@ -557,6 +557,13 @@ class Context:
         _check(lib().d2g_ctx_get_tuning(self.h, int(key), C.byref(v)))
         return v.value
 
+    def solve_layout(self):
+        """How the last solve call spread its clusters: counts per layout and
+        the hardware-cluster sizes used."""
+        v = np.zeros(4, np.int32)
+        _check(lib().d2g_ctx_solve_layout(self.h, _p(v, I32P), 4))
+        return {"block": int(v[0]), "thread_block_cluster": int(v[1]), "grid": int(v[2]), "cluster_size": int(v[3])}
+
     def set_level_budget(self, nbytes):
         """Cap the bytes a traversal level may use (0: a sixth of the device);
         larger calls run in chunks of body pairs, with identical results."""

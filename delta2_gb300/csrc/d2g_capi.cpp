@@ -792,6 +792,15 @@ int d2g_ctx_get_tuning(d2g_ctx* c, int32_t key, int32_t* value) {
     return D2G_OK;
 }
 
+int d2g_ctx_solve_layout(d2g_ctx* c, int32_t* layout, int32_t n) {
+    if (!c || !layout || n < D2G_SOLVE_LAYOUT) {
+        set_error("null argument or fewer than D2G_SOLVE_LAYOUT entries");
+        return D2G_ERR_INVALID;
+    }
+    for (int i = 0; i < D2G_SOLVE_LAYOUT; i++) layout[i] = c->eng.sv_layout[i];
+    return D2G_OK;
+}
+
 int d2g_ctx_launches(d2g_ctx* c, int64_t* launches) {
     if (!c || !launches) {
         set_error("null argument");

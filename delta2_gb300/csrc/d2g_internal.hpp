@@ -167,6 +167,7 @@ struct Engine {
     DBuf<double> sv_static_imp, sv_sdelta;
     DBuf<int32_t> sv_scon, sv_list, sv_grid, sv_cl_flags;
     int sv_cl_fit[4] = {-1, -1, -1, -1};  // resident thread-block clusters of 16, 8, 4, 2 solve blocks
+    int sv_layout[4] = {0, 0, 0, 0};  // the last solve call's layout (d2g_ctx_solve_layout)
     DBuf<unsigned char> sv_bw_raw, sv_cw_raw;
     // GPU broad phase (d2g_broadphase.cu)
     DBuf<float> bp_box;

@@ -1229,6 +1229,10 @@ int run_solve(d2g_ctx* ctx, int n_clusters, const int32_t* d_part_off, const int
             }
         }
         const bool all_small = mid.empty() && big.empty();
+        E.sv_layout[0] = (int)small.size();
+        E.sv_layout[1] = (int)mid.size();
+        E.sv_layout[2] = (int)big.size();
+        E.sv_layout[3] = mid.empty() ? 0 : cs;
         const int pf = prof_mark_begin(ctx, PROF_SOLVE, n_con);
         RC(E.sv_list.ensure(small.size() + mid.size() + 2));
         if (!small.empty()) {

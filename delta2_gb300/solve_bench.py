@@ -116,8 +116,8 @@ def main():
             for key, v in saved.items():
                 ctx.set_tuning(key, v)
             print(json.dumps({"layout": name, "ms": [round(x, 2) for x in ms], "parts": len(parts),
-                              "contacts": int(len(con)), "iterations": list(got[1]), "status": got[0]}),
-                  flush=True)
+                              "contacts": int(len(con)), "iterations": list(got[1]), "status": got[0],
+                              "solved_by": ctx.solve_layout()}), flush=True)
     finally:
         ctx.close()
 

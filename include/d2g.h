@@ -277,6 +277,12 @@ int d2g_ctx_ccd_stats(d2g_ctx* ctx, int32_t reset, int64_t* stats, int32_t n);
 #define D2G_TUNE_KEYS 6
 int d2g_ctx_set_tuning(d2g_ctx* ctx, int32_t key, int32_t value);
 int d2g_ctx_get_tuning(d2g_ctx* ctx, int32_t key, int32_t* value);
+/* How the last solve call (d2g_solve_clusters or a stepper round) spread its
+ * clusters (no reference counterpart; diagnostics): 0 clusters solved by one
+ * block, 1 by thread-block clusters, 2 by cooperative grids, 3 the
+ * thread-block clusters' blocks. */
+#define D2G_SOLVE_LAYOUT 4
+int d2g_ctx_solve_layout(d2g_ctx* ctx, int32_t* layout, int32_t n);
 /* Memory cap (no reference counterpart): the bytes one level of a tree
  * traversal (discrete narrow phase or CCD) may use for its buffers; 0 (the
  * default) means a sixth of the device memory.  A call whose level would

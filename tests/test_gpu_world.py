@@ -181,9 +181,17 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, solve_cluster, l
     s = _wide_cluster_scene()
     try:
         clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=128)
+        layout = ctx.solve_layout()
     finally:
         for k, v in defaults.items():
             ctx.set_tuning(k, v)
+    # the cluster took the layout the settings ask for
+    if grid_min_parts == 128:
+        assert layout["grid"] == 1, layout
+    elif solve_cluster == 1:
+        assert layout["block"] == 1, layout
+    else:
+        assert layout["thread_block_cluster"] == 1 and layout["cluster_size"] == solve_cluster, layout
     assert max(len(parts) for parts, _ in clusters) > 128
     assert max(len(h) for h in hits) >= 128
 
