@@ -814,12 +814,17 @@ __device__ __forceinline__ void record_no_contact(PrimResult* out, int32_t* hit)
     if (hit) *hit = 0;
 }
 
-__device__ __forceinline__ void warp_survivors(int j, bool keep, uint32_t* mask, int32_t* cnt, int n_total) {
+// A warp's surviving tests appended to list (lane order within the warp,
+// warps in arrival order; the tests' results do not depend on the order), the
+// list's length in *count.
+__device__ __forceinline__ void warp_append(int j, bool keep, int32_t* list, int32_t* count) {
     const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if ((threadIdx.x & 31) == 0 && j < n_total) {
-        mask[j >> 5] = m;
-        cnt[j >> 5] = __popc(m);
-    }
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = j;
 }
 
 __global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, const int32_t* __restrict__ items,
@@ -830,7 +835,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, c
                                                         const float* __restrict__ tri32,
                                                         const float* __restrict__ search, PrimResult* __restrict__ sub,
                                                         PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
-                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt,
+                                                        int32_t* __restrict__ list, int32_t* __restrict__ count,
                                                         int use_bounds) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
@@ -859,7 +864,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_pt(int n_tp, int n_total, c
         keep = !use_bounds || !(box_gap(bp, bq) > thr + (1e-3f + 4e-6f * (mag + thr)));  // NaN keeps the test
         if (!keep) record_no_contact(w.out, w.hit);
     }
-    warp_survivors(j, keep, mask, cnt, n_total);
+    warp_append(j, keep, list, count);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, const int32_t* __restrict__ items,
@@ -870,7 +875,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, c
                                                         const float* __restrict__ tri32,
                                                         const float* __restrict__ search, PrimResult* __restrict__ sub,
                                                         PrimResult* __restrict__ cres, int32_t* __restrict__ chit,
-                                                        uint32_t* __restrict__ mask, int32_t* __restrict__ cnt,
+                                                        int32_t* __restrict__ list, int32_t* __restrict__ count,
                                                         int use_bounds) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
@@ -896,7 +901,7 @@ __global__ void __launch_bounds__(kBlock) k_ccd_mask_ee(int n_tp, int n_total, c
         keep = !use_bounds || !(box_gap(ba, bb) > thr + (1e-3f + 4e-6f * (mag + thr)));
         if (!keep) record_no_contact(w.out, w.hit);
     }
-    warp_survivors(j, keep, mask, cnt, n_total);
+    warp_append(j, keep, list, count);
 }
 
 __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, const int32_t* __restrict__ items,
@@ -971,7 +976,7 @@ __global__ void __launch_bounds__(kPrimBlock) k_prim_pt(int n_tp, int n_total, c
 //                iterations with about half the instructions per iteration,
 //                on few enough warps that each has an SMSP to itself.
 // Each test performs exactly the operations of edge_edge_ccd, in order.
-constexpr int kEeFirstItersDefault = 2;  // the first-pass iteration cap (context setting D2G_TUNE_EE_FIRST_ITERS)
+// The first pass's iteration cap is the context setting D2G_TUNE_EE_FIRST_ITERS (default 2).
 constexpr int kEeRec = 10;  // saved test: t, min_dist, P, Q, toc, iterations done (the edges are recomputed)
 struct EeArgs {
     int n_tp, n_conn;
@@ -1740,10 +1745,10 @@ void prof_collect(d2g_ctx* ctx) {
 constexpr int kScanThreads = 1024, kScanPer = 8, kScanChunk = kScanThreads * kScanPer;
 static_assert(kScanThreads == 32 * 32, "the warp-sum scan assumes 32 warps");
 constexpr int kScanOneBlock = 4 * kScanChunk;  // larger arrays go to cub
-struct ScanSeg {
-    const int32_t* in[2];
-    int32_t* out[2];
-    int n[2];
+struct ScanSeg {  // up to four independent scans, one block each
+    const int32_t* in[4];
+    int32_t* out[4];
+    int n[4];
 };
 __global__ void __launch_bounds__(kScanThreads) k_scan1(ScanSeg sg) {
     __shared__ int32_t buf[kScanChunk];
@@ -1813,6 +1818,7 @@ int scan_on(cudaStream_t st, DBuf<uint8_t>& tmp, const int32_t* in, int32_t* out
     return D2G_OK;
 }
 int scan(d2g_ctx* ctx, const int32_t* in, int32_t* out, int n) {
+    if (n <= kScanOneBlock) ctx->eng.launches++;  // this library's scan kernel (larger ones are cub's)
     return scan_on(ctx->stream, ctx->eng.cub_tmp, in, out, n);
 }
 // Two independent scans on the context's stream (one launch when both are small).
@@ -1826,10 +1832,31 @@ int scan2(d2g_ctx* ctx, const int32_t* in0, int32_t* out0, int n0, const int32_t
         sg.out[1] = out1;
         sg.n[1] = n1;
         k_scan1<<<2, kScanThreads, 0, ctx->stream>>>(sg);
+        ctx->eng.launches++;
         return D2G_OK;
     }
     if (int rc = scan(ctx, in0, out0, n0)) return rc;
     return scan(ctx, in1, out1, n1);
+}
+
+// Four scans in one launch when each fits one block, else one by one.
+int scan4(d2g_ctx* ctx, const int32_t* const* in, int32_t* const* out, const int* n) {
+    ScanSeg sg;
+    bool one = true;
+    for (int i = 0; i < 4; i++) {
+        sg.in[i] = in[i];
+        sg.out[i] = out[i];
+        sg.n[i] = n[i];
+        one = one && n[i] <= kScanOneBlock;
+    }
+    if (one) {
+        k_scan1<<<4, kScanThreads, 0, ctx->stream>>>(sg);
+        ctx->eng.launches++;
+        return D2G_OK;
+    }
+    for (int i = 0; i < 4; i++)
+        if (int rc = scan(ctx, in[i], out[i], n[i])) return rc;
+    return D2G_OK;
 }
 
 // Read k device int32 scalars (after the stream's pending work).
@@ -2096,9 +2123,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
                    ctx->tris.p, ctx->tri32.p, ctx->geo_eps.p, skip, eskip, E.flags.p);
             prof_end(ctx, pff);
         }
-        RC(scan(ctx, E.flags.p, E.flag_off.p, n_slots));
         if (n_conn > 0) LAUNCH(k_conn_nn, n_conn, n_conn, E.conn.p, ctx->ntris.p, E.nn_cnt.p);
-        RC(scan(ctx, E.nn_cnt.p, E.nn_off.p, n_conn));
+        RC(scan2(ctx, E.flags.p, E.flag_off.p, n_slots, E.nn_cnt.p, E.nn_off.p, n_conn));
         int32_t tot1[2];
         const int32_t* src1[2] = {E.flag_off.p + n_slots, E.nn_off.p + n_conn};
         RC(read_scalars(ctx, src1, 2, tot1));
@@ -2130,20 +2156,14 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         if (n_soup > 0) LAUNCH(k_compact, n_slots, n_slots, E.flags.p, E.flag_off.p, E.items.p);
         const int n_pt = 6 * K + 6 * P, n_ee = 9 * K + 9 * P;
         // FP32 bounds drop the tests that cannot hit; the FP64 kernels run on
-        // the compacted survivors
-        const int w_pt = (n_pt + 31) / 32, w_ee = (n_ee + 31) / 32;
-        RC(E.ccd_mask.ensure((size_t)w_pt + w_ee + 2));
-        RC(E.ccd_cnt.ensure((size_t)w_pt + w_ee + 2));
-        RC(E.ccd_off.ensure((size_t)w_pt + w_ee + 4));
+        // the survivors, which the bound kernels append to their lists
+        RC(E.ccd_cnt.ensure(2));
         RC(E.ccd_list.ensure((size_t)n_pt + n_ee + 2));
-        uint32_t* mask_pt = E.ccd_mask.p;
-        uint32_t* mask_ee = E.ccd_mask.p + w_pt;
         int32_t* cnt_pt = E.ccd_cnt.p;
-        int32_t* cnt_ee = E.ccd_cnt.p + w_pt;
-        int32_t* off_pt = E.ccd_off.p;
-        int32_t* off_ee = E.ccd_off.p + w_pt + 1;
+        int32_t* cnt_ee = E.ccd_cnt.p + 1;
         int32_t* list_pt = E.ccd_list.p;
         int32_t* list_ee = E.ccd_list.p + n_pt;
+        D2G_CUDA(cudaMemsetAsync(E.ccd_cnt.p, 0, 2 * sizeof(int32_t), s));
         if (n_ee > 0) {
             RC(E.ee_rec.ensure((size_t)kEeRec * n_ee));
             RC(E.ee_work.ensure(n_ee));
@@ -2160,10 +2180,8 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         if (n_ee > 0) {
             k_ccd_mask_ee<<<nblocks(n_ee), kBlock, 0, s_ee>>>(K, n_ee, E.items.p, E.soup.p, E.conn.p, E.nn_off.p,
                                                             n_conn, E.pm32c.p, ctx->ntris.p, ctx->tri32.p,
-                                                            E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_ee,
+                                                            E.search.p, E.sub.p, E.cres.p, E.chit.p, list_ee,
                                                             cnt_ee, E.fp32_bounds ? 1 : 0);
-            RC(scan_on(s_ee, fork ? E.cub_tmp2 : E.cub_tmp, cnt_ee, off_ee, w_ee));
-            k_np_items<<<nblocks(n_ee), kBlock, 0, s_ee>>>(n_ee, mask_ee, off_ee, list_ee);
             const int pf = prof_begin(ctx, PROF_CONN, n_ee, s_ee);
             EeArgs ea;
             ea.n_tp = K;
@@ -2186,22 +2204,20 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             ea.certificates = E.certificates ? 1 : 0;
             ea.ca_stats = E.ccd_stats.p;
             D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
-            k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, off_ee + w_ee, E.pm.p,
+            k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, cnt_ee, E.pm.p,
                                                                           ctx->tris.p, ea);
             k_ee_rest4<<<ee_grid, kBlock, 0, s_ee>>>(ea);
             ctx->eng.launches += 2;
             prof_end(ctx, pf, s_ee);
-            ctx->eng.launches += 2;  // mask, items
+            ctx->eng.launches += 1;  // the bound kernel
         }
         if (n_pt > 0) {
             LAUNCH(k_ccd_mask_pt, n_pt, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm32c.p,
-                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, mask_pt, cnt_pt,
+                   ctx->ntris.p, ctx->tri32.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_pt, cnt_pt,
                    E.fp32_bounds ? 1 : 0);
-            RC(scan(ctx, cnt_pt, off_pt, w_pt));
-            LAUNCH(k_np_items, n_pt, n_pt, mask_pt, off_pt, list_pt);
             const int pf = prof_begin(ctx, PROF_SOUP_CCD, n_pt);
             LAUNCHB(k_prim_pt, n_pt, kPrimBlock, K, n_pt, E.items.p, E.soup.p, E.conn.p, E.nn_off.p, n_conn, E.pm.p,
-                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_pt, off_pt + w_pt);
+                    ctx->ntris.p, ctx->tris.p, E.search.p, E.sub.p, E.cres.p, E.chit.p, list_pt, cnt_pt);
             prof_end(ctx, pf);
         }
         if (fork) {
@@ -2213,7 +2229,6 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             LAUNCH(k_soup_fold, K, K, E.items.p, E.soup.p, E.sub.p, E.search.p, E.res.p, E.hit.p, E.entry_hits.p,
                    ctx->nodes.p, E.flags.p);
         }
-        RC(scan2(ctx, E.flags.p, E.flag_off.p, K, E.chit.p, E.cflag_off.p, 15 * P));
         RC(E.cnt_a.ensure(n_soup + 1));
         RC(E.cnt_b.ensure(n_soup + 1));
         RC(E.off_a.ensure(n_soup + 1));
@@ -2226,7 +2241,12 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         }
         if (n_soup > 0)
             LAUNCH(k_expand_count, n_soup, n_soup, E.soup.p, E.entry_hits.p, ctx->nodes.p, 1, E.cnt_a.p, E.cnt_b.p);
-        RC(scan2(ctx, E.cnt_a.p, E.off_a.p, n_soup, E.cnt_b.p, E.off_b.p, n_soup));
+        {  // final flags of soup and leaf-pair tests, children of soup node pairs: one launch
+            const int32_t* sin[4] = {E.flags.p, E.chit.p, E.cnt_a.p, E.cnt_b.p};
+            int32_t* sout[4] = {E.flag_off.p, E.cflag_off.p, E.off_a.p, E.off_b.p};
+            const int sn[4] = {K, 15 * P, n_soup, n_soup};
+            RC(scan4(ctx, sin, sout, sn));
+        }
         int32_t tot2[4];
         const int32_t* src2[4] = {E.flag_off.p + K, E.cflag_off.p + 15 * P, E.off_a.p + n_soup, E.off_b.p + n_soup};
         RC(read_scalars(ctx, src2, 4, tot2));

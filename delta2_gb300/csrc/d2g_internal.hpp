@@ -152,10 +152,9 @@ struct Engine {
     DBuf<int32_t> flt_idx, flt_order, flt_keep, flt_pos, flt_cnt, flt_off, np_tri;
     DBuf<unsigned long long> flt_keys, flt_keys_s;
     DBuf<double> flt_mid;
-    // CCD candidates: FP32 poses (8 per pair), survivor masks, counts, lists
+    // CCD candidates: FP32 poses (8 per pair), survivor counts and lists
     DBuf<float> pm32c;
-    DBuf<uint32_t> ccd_mask;
-    DBuf<int32_t> ccd_cnt, ccd_off, ccd_list;
+    DBuf<int32_t> ccd_cnt, ccd_list;  // CCD survivors: counts (point-triangle, edge-edge) and lists
     // discrete narrow-phase candidates: FP32 poses, survivor masks and offsets
     DBuf<float> pm32;
     DBuf<uint32_t> np_mask;
