@@ -2157,17 +2157,17 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
         const int n_pt = 6 * K + 6 * P, n_ee = 9 * K + 9 * P;
         // FP32 bounds drop the tests that cannot hit; the FP64 kernels run on
         // the survivors, which the bound kernels append to their lists
-        RC(E.ccd_cnt.ensure(2));
+        RC(E.ccd_cnt.ensure(3));
         RC(E.ccd_list.ensure((size_t)n_pt + n_ee + 2));
         int32_t* cnt_pt = E.ccd_cnt.p;
         int32_t* cnt_ee = E.ccd_cnt.p + 1;
+        int32_t* cnt_rest = E.ccd_cnt.p + 2;  // edge-edge tests continued by k_ee_rest4
         int32_t* list_pt = E.ccd_list.p;
         int32_t* list_ee = E.ccd_list.p + n_pt;
-        D2G_CUDA(cudaMemsetAsync(E.ccd_cnt.p, 0, 2 * sizeof(int32_t), s));
+        D2G_CUDA(cudaMemsetAsync(E.ccd_cnt.p, 0, 3 * sizeof(int32_t), s));
         if (n_ee > 0) {
             RC(E.ee_rec.ensure((size_t)kEeRec * n_ee));
             RC(E.ee_work.ensure(n_ee));
-            RC(E.ee_count.ensure(1));
         }
         // The point-triangle and edge-edge chains touch disjoint outputs: the
         // edge-edge chain runs on the second stream beside the other.
@@ -2199,11 +2199,10 @@ int run_ccd(d2g_ctx* ctx, const int32_t* d_pairs, const double* d_max_time, int 
             ea.tris = ctx->tris.p;
             ea.rec = E.ee_rec.p;
             ea.work = E.ee_work.p;
-            ea.count = E.ee_count.p;
+            ea.count = cnt_rest;
             ea.first_iters = E.tune[D2G_TUNE_EE_FIRST_ITERS];
             ea.certificates = E.certificates ? 1 : 0;
             ea.ca_stats = E.ccd_stats.p;
-            D2G_CUDA(cudaMemsetAsync(E.ee_count.p, 0, sizeof(int32_t), s_ee));
             k_ee_first<<<nblocks(n_ee, kPrimBlock), kPrimBlock, 0, s_ee>>>(n_ee, list_ee, cnt_ee, E.pm.p,
                                                                           ctx->tris.p, ea);
             k_ee_rest4<<<ee_grid, kBlock, 0, s_ee>>>(ea);

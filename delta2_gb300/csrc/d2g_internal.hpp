@@ -203,7 +203,7 @@ struct Engine {
     DBuf<uint8_t> cub_tmp, cub_tmp2;
     // phased edge-edge CCD (d2g_engine.cu)
     DBuf<double> ee_rec;
-    DBuf<int32_t> ee_work, ee_count;
+    DBuf<int32_t> ee_work;
     int ee_grid = 0;  // k_ee_rest4 grid (every block resident)
     // traversal chunking: root entries of the call's pairs; a byte budget for
     // a level's buffers (0: a third of the device memory)
