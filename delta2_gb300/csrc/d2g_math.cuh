@@ -8,7 +8,8 @@
 //
 //   sin, cos : Cody & Waite (1980) reduction x = k*pi/2 + r with pi/2 split
 //              into three parts (33-bit head), then the Maclaurin series of
-//              sin(r) through r^19 and cos(r) through r^18 by Horner's rule.
+//              sin(r) through r^19 and cos(r) through r^18 by Horner's rule,
+//              each step one fused multiply-add.
 //   acos     : pi/2 - asin(x) for x <= 1/2, else 2*asin(sqrt((1-x)/2)); asin
 //              by its Maclaurin series (30 terms) on [0, 1/2].
 //   log      : frexp reduction and log(m) = 2*atanh((m-1)/(m+1)) (set-up only).
@@ -18,8 +19,9 @@
 //              the same bits as the division.
 //
 // Every kernel translation unit is compiled with -fmad=false and every host
-// unit with -ffp-contract=off, so each operation is rounded on its own and
-// the results are the same bits on the GPU, on x86-64 and on Arm.
+// unit with -ffp-contract=off, so each operation is rounded on its own (the
+// fused multiply-adds written out as such are single IEEE operations) and the
+// results are the same bits on the GPU, on x86-64 and on Arm.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -32,6 +34,16 @@
 #endif
 
 namespace d2g {
+
+// x y + z rounded once (the IEEE fused multiply-add, the same on every
+// machine).
+D2G_HD double m_fma(double x, double y, double z) {
+#ifdef __CUDA_ARCH__
+    return fma(x, y, z);
+#else
+    return std::fma(x, y, z);
+#endif
+}
 
 // Horner coefficients, highest order first, of sin(r) = r + r z S(z) and
 // cos(r) = 1 + z C(z), z = r^2.
@@ -57,10 +69,10 @@ D2G_HD double m_kernel_sincos(double r, bool cosine) {
 #ifdef __CUDA_ARCH__
 #pragma unroll
 #endif
-    for (int i = 1; i < 9; i++) p = m_sincos_coef(i, cosine) + z * p;
+    for (int i = 1; i < 9; i++) p = m_fma(z, p, m_sincos_coef(i, cosine));  // Horner steps as fused multiply-adds
     const double a = cosine ? z : r * z;
     const double b = cosine ? 1.0 : r;
-    return b + a * p;  // sin: r + (r z) S, cos: 1 + z C
+    return m_fma(a, p, b);  // sin: r + (r z) S, cos: 1 + z C
 }
 
 D2G_HD double m_kernel_sin(double r) { return m_kernel_sincos(r, false); }

@@ -359,11 +359,18 @@ __device__ __forceinline__ void normal_wave16(int n0, int n1, const int32_t* __r
         const bool st = a.is_static[g];
         // this side's contact point p1 = T_FS local and its velocity
         // v1 = v + (ii L) x (p1 - x) (State::pointVelocity), component cc
+        // (p1 on the FS lanes and ii L on the FSf lanes in one instruction
+        // stream, each with its own operations in its order, then swapped)
         const double* lp = side ? C.local_B : C.local_A;
         const double* Tr = W.T_FS + 4 * cc;
-        const double p1 = ((Tr[0] * lp[0] + Tr[1] * lp[1]) + Tr[2] * lp[2]) + Tr[3] * 1.0;
         const double* Ir = a.ii + 9 * (size_t)g + 3 * cc;
-        const double wv = (Ir[0] * W.FS[5] + Ir[1] * W.FS[6]) + Ir[2] * W.FS[7];
+        const double* X = variant ? Ir : Tr;
+        const double* Y = variant ? W.FS + 5 : lp;
+        const double dot3 = (X[0] * Y[0] + X[1] * Y[1]) + X[2] * Y[2];
+        const double mine = variant ? dot3 : dot3 + Tr[3] * 1.0;
+        const double other = shfl_d(mine, lane ^ 2);
+        const double p1 = variant ? other : mine;
+        const double wv = variant ? mine : other;
         const double r = p1 - W.FS[8 + cc];
         const double w1 = shfl_d(wv, s1), w2 = shfl_d(wv, s2), r1 = shfl_d(r, s1), r2 = shfl_d(r, s2);
         const double v1s = W.FS[11 + cc] + (w1 * r2 - w2 * r1);

@@ -7,11 +7,13 @@
 // in the last bit for some arguments, which would make a bit-exact comparison
 // between this oracle and the GPU kernels impossible.  Both sides therefore
 // evaluate these functions with the SAME published methods, in the same
-// operation order, without fused multiply-add:
+// operation order, with no fused multiply-add but the ones written out:
 //   * sin / cos : Cody & Waite (1980) additive range reduction by pi/2 with a
 //                 three-part split of pi/2, then the Maclaurin series of sin
 //                 and cos on [-pi/4, pi/4] (terms through r^19 / r^18),
-//                 evaluated by Horner's rule.
+//                 evaluated by Horner's rule, each step (and the final
+//                 r + (r z) p, 1 + z p) one fused multiply-add (std::fma,
+//                 correctly rounded on every IEEE machine).
 //   * asin / acos: Maclaurin series of asin on [0, 1/2] (30 terms); acos(x)
 //                 = pi/2 - asin(x) for x <= 1/2 and 2 asin(sqrt((1-x)/2))
 //                 otherwise.
@@ -38,30 +40,30 @@ static const double kLn2 = 0.6931471805599453;
 inline double kernel_sin(double r) {
     const double z = r * r;
     double p = -8.22063524662433e-18;
-    p = 2.8114572543455206e-15 + z * p;
-    p = -7.647163731819816e-13 + z * p;
-    p = 1.6059043836821613e-10 + z * p;
-    p = -2.505210838544172e-08 + z * p;
-    p = 2.7557319223985893e-06 + z * p;
-    p = -0.0001984126984126984 + z * p;
-    p = 0.008333333333333333 + z * p;
-    p = -0.16666666666666666 + z * p;
-    return r + (r * z) * p;
+    p = std::fma(z, p, 2.8114572543455206e-15);
+    p = std::fma(z, p, -7.647163731819816e-13);
+    p = std::fma(z, p, 1.6059043836821613e-10);
+    p = std::fma(z, p, -2.505210838544172e-08);
+    p = std::fma(z, p, 2.7557319223985893e-06);
+    p = std::fma(z, p, -0.0001984126984126984);
+    p = std::fma(z, p, 0.008333333333333333);
+    p = std::fma(z, p, -0.16666666666666666);
+    return std::fma(r * z, p, r);
 }
 
 // cos(r) on |r| <= pi/4: 1 + z*(C1 + z*(C2 + ... + z*C9)).
 inline double kernel_cos(double r) {
     const double z = r * r;
     double p = -1.5619206968586225e-16;
-    p = 4.779477332387385e-14 + z * p;
-    p = -1.1470745597729725e-11 + z * p;
-    p = 2.08767569878681e-09 + z * p;
-    p = -2.755731922398589e-07 + z * p;
-    p = 2.48015873015873e-05 + z * p;
-    p = -0.001388888888888889 + z * p;
-    p = 0.041666666666666664 + z * p;
-    p = -0.5 + z * p;
-    return 1.0 + z * p;
+    p = std::fma(z, p, 4.779477332387385e-14);
+    p = std::fma(z, p, -1.1470745597729725e-11);
+    p = std::fma(z, p, 2.08767569878681e-09);
+    p = std::fma(z, p, -2.755731922398589e-07);
+    p = std::fma(z, p, 2.48015873015873e-05);
+    p = std::fma(z, p, -0.001388888888888889);
+    p = std::fma(z, p, 0.041666666666666664);
+    p = std::fma(z, p, -0.5);
+    return std::fma(z, p, 1.0);
 }
 
 // Reduce x to r in [-pi/4, pi/4] and quadrant q = k mod 4 (x = k*pi/2 + r).
