@@ -773,8 +773,11 @@ __device__ void solve_body(int k, int tid, int nt, int gb, int G, int* shv, cons
                 n0 = woff[ln];
                 n1 = woff[ln + 1];
                 if (lanes16(w0, w1)) {
+                    // the next wave's first task, loaded while this wave computes
+                    const int2 pre_next =
+                        lanes16(n0, n1) ? wave16_first(n0, n1, widx, c0, G, gb, a) : make_int2(-1, -1);
                     normal_wave16(w0, w1, widx, c0, G, gb, t, rt, pre, a);
-                    pre = lanes16(n0, n1) ? wave16_first(n0, n1, widx, c0, G, gb, a) : make_int2(-1, -1);
+                    pre = pre_next;
                     SYNC();
                     continue;
                 }
