@@ -174,6 +174,16 @@ def test_tuning_file_loader(tmp_path):
     assert set(got) <= set(D.TUNE_NAMES)
 
 
+def test_grid_threshold_choice():
+    # the fastest total wins; within 1% of it, the smallest threshold (the
+    # piles the tuner times stop at 401 parts, larger clusters gain from the grid)
+    from delta2_gb300 import autotune
+
+    assert autotune.choose_grid_threshold({64: 135.9, 512: 129.08, 1000000: 129.07}) == 512
+    assert autotune.choose_grid_threshold({64: 100.0, 512: 120.0, 1000000: 130.0}) == 64
+    assert autotune.choose_grid_threshold({64: 140.0, 512: 131.0, 1000000: 129.0}) == 1000000
+
+
 def test_open_box_scene_and_parallel_trees():
     # the noisy-icosphere scene: one static open box, then one mesh and tree per
     # body built on all host cores from per-mesh streams (same trees every time)
