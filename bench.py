@@ -656,6 +656,18 @@ def batched_steps(local_rank, args, net):
     torch.cuda.synchronize()
     ccd_b = time.perf_counter() - t0
     ref_c, ref_off, _ = ctx.compare_trees_full_continuous(g_pairs, g_mt, capacity=1 << 23)
+    # the same batched call without the learned proposal (FP32 bounds and the
+    # cut-off kept): what the network and its certificate add on this batch
+    configure(ctx, {**LEARNED, "proposal": False})
+    ctx.compare_trees_full_continuous_device(d_pairs.data_ptr(), d_mt.data_ptr(), len(g_pairs))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        ctx.compare_trees_full_continuous_device(d_pairs.data_ptr(), d_mt.data_ptr(), len(g_pairs))
+    torch.cuda.synchronize()
+    ccd_nb = time.perf_counter() - t0
+    nb_c, nb_off, _ = ctx.compare_trees_full_continuous(g_pairs, g_mt, capacity=1 << 23)
+    same_nb = bool(np.array_equal(nb_off, ref_off) and np.array_equal(nb_c.view(np.uint64), ref_c.view(np.uint64)))
     ctx.close()
     # ---- plain GPU path, one scene at a time
     ctxs = []
@@ -709,7 +721,8 @@ def batched_steps(local_rank, args, net):
             "learned_batched_vs_plain_gpu_steps": (k / wall) / (k / wall_plain),
             "ccd": {"pair_queries": n_q, "learned_batched": n_q * k / ccd_b, "plain_gpu": n_q * k / ccd_p,
                     "unit": "pair-queries/s", "learned_batched_vs_plain_gpu": ccd_p / ccd_b,
-                    "contacts": int(len(ref_c)), "identical_contacts": bool(same)},
+                    "batched_without_proposal": n_q * k / ccd_nb, "proposal_gain": ccd_nb / ccd_b,
+                    "contacts": int(len(ref_c)), "identical_contacts": bool(same and same_nb)},
             "proposal_per_step": {kk: v / k for kk, v in prop_stats.items() if v},
             "phase_ms_per_step": {kk: v / k for kk, v in phases.items() if kk != "reserved"},
             "stats_per_step": {kk: v / k for kk, v in stats.items()}}, scenes
