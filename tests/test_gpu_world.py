@@ -196,6 +196,32 @@ def test_solve_wide_cluster_matches_oracle(ctx, grid_min_parts, solve_cluster, l
     assert max(len(h) for h in hits) >= 128
 
 
+def test_solve_several_thread_block_clusters_in_one_launch(ctx):
+    """Two piles of 72 touching cubes, 4 m apart: two clusters of hundreds of
+    contacts solved by one launch of 16-block thread-block clusters (fixed
+    size, then the automatic choice), bit for bit against the oracle."""
+    s = _wide_cluster_scene()
+    far = s.cur[:, 9] > 0.0  # the cubes of the upper half in y (index 0 is the ground)
+    far[0] = False
+    for arr in (s.cur, s.fut, s.last):
+        arr[far, 9] += 4.0
+    defaults = {k: ctx.get_tuning(k) for k in (D.TUNE_GRID_MIN_PARTS, D.TUNE_SOLVE_CLUSTER)}
+    try:
+        for size in (16, 0):
+            ctx.set_tuning(D.TUNE_GRID_MIN_PARTS, 1000000)
+            ctx.set_tuning(D.TUNE_SOLVE_CLUSTER, size)
+            clusters, hits = solve_against_oracle(ctx, s.copy(), s, min_contacts=256)
+            layout = ctx.solve_layout()
+            big = sum(1 for h in hits if len(h) >= 32)
+            assert big == 2, [len(h) for h in hits]
+            assert layout["thread_block_cluster"] == 2 and layout["cluster_size"] >= 2, layout
+            if size:
+                assert layout["cluster_size"] == size, layout
+    finally:
+        for k, v in defaults.items():
+            ctx.set_tuning(k, v)
+
+
 def _wide_cluster_scene():
     # 144 axis-aligned unit cubes 1 cm apart and 1 cm above the ground, falling at 0.5 m/s
     s = D.make_scene(1, nx=12, ny=12, nz=1, spacing=1.01, speed_sigma=0.0)
