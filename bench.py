@@ -425,7 +425,8 @@ def run_ours(args):
             "steps_per_s": batch_line["learned_batched_vs_plain_gpu_steps"],
             "identical_contacts": batch_line["ccd"]["identical_contacts"],
             "workload": f"batched configuration, {batch_line['scenes']} scenes, {batch_line['bodies']} bodies",
-            "single_scene_ccd_learned_vs_plain_gpu": modes.get("learned_vs_plain_gpu")},
+            "single_scene_ccd_learned_vs_plain_gpu": modes.get("learned_vs_plain_gpu"),
+            "ccd_learned_proposal_alone": batch_line["ccd"]["proposal_gain"]},
         "batched_steps": batch_line,
         "per_step": {"contacts": int(n_contacts), "node_pairs": int(counters[0]), "primitive_tests": int(counters[1]),
                      "leaf_pairs": int(counters[2]), "levels": int(counters[3])},
